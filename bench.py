@@ -1,0 +1,365 @@
+"""Benchmark of the density-matrix hot path on GB300.
+
+Workload (the 14-qubit FP64 configuration): a Pauli vector of 14 qubits in
+the full ``general(2)`` basis (4^14 = 268,435,456 float64 entries, 2.15 GB)
+on one GPU.  One step applies 7 noisy-CZ 16x16 PTMs (CZ followed by
+amplitude + phase damping on both qubits, seeded T1/T2) on uniformly random
+ordered qubit pairs, so every stride class occurs.  The vector (2.15 GB) is
+larger than L2 (129 MB), so no flush is needed between steps.
+
+Prints ONE JSON line (rank 0).  ``value`` = 2q-PTM applications per second
+with the state resident in HBM; ``e2e`` = the same through the public API
+(host numpy PTMs passed per call, the trace read back every step);
+``roofline`` = the dominant kernel's algorithmic bytes per launch over its
+CUDA-event duration against the measured HBM copy peak; ``cpu_baseline`` =
+the oracle (numpy einsum restatement of the reference backend) on the host
+cores for a bounded sample.
+
+``--impl reference`` times the reference's CPU implementation of the path
+(the oracle port of PauliVectorNumpy, all host threads) on the same
+workload and prints the same line with ``"impl": "reference"``.
+
+With ``--gpus N > 1`` (torchrun) every rank runs an independent replica
+(the path is not sharded; no collective on the data path); value = all
+ranks' applications / max rank time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = 14
+APPS_PER_STEP = 7
+METRIC = ('2q-PTM apps/s & HBM GB/s (14q fp64); batched fp32 fwd+adjoint vs '
+          'plain, err<1e-6')
+WORKLOAD = ('14-qubit FP64 Pauli vector (4^14 entries, 2.15 GB); step = 7 '
+            'noisy-CZ 16x16 PTMs on uniformly random ordered qubit pairs')
+
+
+def _peaks():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,'
+             'clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,'
+             'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index),
+                 '--query-gpu=' + self.QUERY, '--format=csv,noheader,nounits',
+                 '-lms', '100'], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [],
+                    'samples': 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap']
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == 'active':
+                    reasons.add(name)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {'sm_mhz': med, 'sm_max_mhz': smax, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+def cpu_baseline_sample(n_apps, seed=123):
+    """Time the oracle (numpy einsum restatement of PauliVectorNumpy) on
+    `n_apps` noisy-CZ applications of the 14-qubit workload."""
+    import numpy as np
+    from oracle import pauli_vector_np as O
+    from quantumsim_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    pv = rng.standard_normal((4,) * N_QUBITS) * 2.0 ** -14
+    ops = workloads.config1_2q_batch(seed, N_QUBITS, n_apps + 1)
+    pv = O.apply_ptm(pv, ops[0][1], *ops[0][2])  # warm-up
+    t0 = time.perf_counter()
+    for _, ptm, qs in ops[1:]:
+        pv = O.apply_ptm(pv, ptm, *qs)
+    dt = time.perf_counter() - t0
+    return n_apps / dt, dt
+
+
+def run_reference(args):
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, _ = cpu_baseline_sample(1, seed=1000 + i)
+        if i >= args.warmup:
+            vals.append(v)
+    value = len(vals) / sum(1.0 / v for v in vals)
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value,
+        'unit': 'apps/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': 1000.0 / value,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64', 'data': 'synthetic',
+        'config': {'workload': WORKLOAD, 'n_qubits': N_QUBITS,
+                   'sample': '1 noisy-CZ application per step'},
+        'cpu_baseline': {'value': value, 'unit': 'apps/s', 'cores': cores,
+                         'kind': 'port',
+                         'sample': '1 application of the 14-qubit 2q '
+                                   'workload per step (numpy einsum, '
+                                   'OpenBLAS threads = cores)'},
+        'e2e': {'value': value, 'unit': 'apps/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl')
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads, ops as qops
+
+    dev = torch.device('cuda', local)
+    n_entries = 4 ** N_QUBITS
+    s = qg.PauliVectorGB300([bases.general(2)] * N_QUBITS, force=True,
+                            device=dev)
+    # a generic mixed state: one layer of the circuit (rotations + CZs)
+    rng = np.random.default_rng(7 + rank)
+    t1, t2 = workloads.coherence_times(rng, N_QUBITS)
+    for op in workloads.config1_layer(rng, N_QUBITS, t1, t2, 7):
+        s.apply_ptm(op[1], *op[2])
+    torch.cuda.synchronize()
+
+    n_steps = args.warmup + args.steps
+    steps = [workloads.config1_2q_batch(1000 * rank + i, N_QUBITS,
+                                        APPS_PER_STEP) for i in range(n_steps)]
+    stream = torch.cuda.current_stream(dev)
+
+    def step(ops_):
+        for _, ptm, qs in ops_:
+            s.apply_ptm(ptm, *qs)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing (value)
+    for i in range(args.warmup):
+        step(steps[i])
+    sampler = ClockSampler(local)
+    barrier()
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.warmup, n_steps):
+        step(steps[i])
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    apps = args.steps * APPS_PER_STEP
+    value = apps * world / (ms / 1e3)
+    bytes_per_app = 2 * n_entries * 8
+
+    # ---- per-launch durations of the dominant kernel (same stream)
+    per = []
+    probe = steps[args.warmup] if args.steps else steps[0]
+    for _, ptm, qs in probe * 2:
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        s.apply_ptm(ptm, *qs)
+        b.record(stream)
+        per.append((a, b))
+    torch.cuda.synchronize()
+    launch_ms = sum(a.elapsed_time(b) for a, b in per) / len(per)
+    peak, peak_kind = _peaks()
+    achieved = bytes_per_app / (launch_ms / 1e3) / 1e9
+    traffic = args.traffic if args.traffic else None
+
+    # ---- per-target breakdown (1q positions, 2q stride classes)
+    per_target = {}
+    if not args.no_sweep:
+        for q in range(N_QUBITS):
+            ptm = workloads.noisy_1q(rng, t1[q], t2[q])
+            per_target['1q_q{}'.format(q)] = _time_app(s, ptm, (q,),
+                                                       bytes_per_app)
+        for pair in [(0, 1), (12, 13), (0, 13), (13, 0), (3, 7), (6, 7),
+                     (1, 12)]:
+            ptm = workloads.noisy_cz(rng, pair, t1, t2)
+            per_target['2q_{}_{}'.format(*pair)] = _time_app(
+                s, ptm, pair, bytes_per_app)
+        dense = rng.standard_normal((4, 4, 4, 4)) * 0.25
+        per_target['2q_dense_3_7'] = _time_app(s, dense, (3, 7), bytes_per_app)
+        per_target['2q_dense_12_13'] = _time_app(s, dense, (12, 13),
+                                                 bytes_per_app)
+
+    # ---- end to end through the public API (host PTMs, trace read back)
+    e2e_steps = [workloads.config1_2q_batch(50000 + 1000 * rank + i,
+                                            N_QUBITS, APPS_PER_STEP)
+                 for i in range(n_steps)]
+    for i in range(args.warmup):
+        step(e2e_steps[i])
+        s.trace()
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.warmup, n_steps):
+        step(e2e_steps[i])
+        s.trace()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = apps * world / e2e_s
+    h2d = APPS_PER_STEP * 16 * 16 * 8
+    qops.check_device_status(dev)
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, dt = cpu_baseline_sample(args.cpu_apps)
+        cpu = {'value': v, 'unit': 'apps/s', 'cores': os.cpu_count(),
+               'kind': 'port',
+               'sample': '{} noisy-CZ applications on the 14-qubit state '
+                         '({:.1f} s; numpy einsum restatement of '
+                         'PauliVectorNumpy)'.format(args.cpu_apps, dt)}
+
+    if rank == 0:
+        line = {
+            'metric': METRIC, 'value': value, 'unit': 'apps/s',
+            'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': ms / args.steps, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'arith': 'float-float (48-bit significand) on FP32 pipes; '
+                     'single-term rows one FP64 multiply',
+            'data': 'synthetic',
+            'config': {'workload': WORKLOAD, 'n_qubits': N_QUBITS,
+                       'entries': n_entries, 'apps_per_step': APPS_PER_STEP,
+                       'l2': 'inputs (2.15 GB) larger than L2, no flush',
+                       'parallelism': 'replicas' if world > 1 else 'single'},
+            'hbm_gbs': bytes_per_app * apps / (ms / 1e3) / 1e9,
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak,
+                         'unit': 'GB/s', 'frac': achieved / peak,
+                         'peak_kind': peak_kind, 'traffic': traffic,
+                         'kernel': 'apply_ptm_kernel<double, DF64> (2q)',
+                         'bytes_per_launch': bytes_per_app,
+                         'launch_ms': launch_ms},
+            'cpu_baseline': cpu,
+            'e2e': {'value': e2e_value, 'unit': 'apps/s',
+                    'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': 8},
+            'gpu_launches': apps,
+            'clocks': clocks,
+            'per_target_gbs': per_target,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def _time_app(s, ptm, qs, bytes_per_app, reps=3):
+    import torch
+    stream = torch.cuda.current_stream()
+    s.apply_ptm(ptm, *qs)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        s.apply_ptm(ptm, *qs)
+    b.record(stream)
+    torch.cuda.synchronize()
+    return round(bytes_per_app * reps / (a.elapsed_time(b) / 1e3) / 1e9, 1)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--cpu-apps', type=int, default=4)
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-sweep', action='store_true')
+    ap.add_argument('--traffic', type=float, default=0.0,
+                    help='dram bytes per launch from an ncu capture')
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == 'gb300':
+        print('warning: fewer than 3 warm-up steps', file=sys.stderr)
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == '__main__':
+    main()

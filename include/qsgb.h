@@ -1,0 +1,196 @@
+/*
+ * qsgb.h -- C ABI of the GB300 density-matrix (Pauli vector) kernels.
+ *
+ * Every entry point takes plain device pointers, 64-bit sizes and a CUDA
+ * stream (as `void*`, NULL = legacy default stream), launches asynchronously
+ * on that stream and returns an int status (QSGB_OK == 0).  Argument errors
+ * are detected on the host before any launch.  No entry point allocates
+ * device memory; the ones that need scratch space take it from the caller
+ * and report the size they need through a *_scratch_bytes() query.
+ *
+ * Data model (quantumsim/pauli_vectors/pauli_vector.py:6-72): a Pauli vector
+ * over n qudits is a dense C-order tensor of shape (d_0, ..., d_{n-1}),
+ * qudit 0 most significant, d_i = dim_pauli of qudit i (1..d_hilbert^2).
+ * Element types: QSGB_F64 (IEEE double) or QSGB_F32 (IEEE float).
+ *
+ * Kernels that take an `unsigned* dev_status` (may be NULL) OR device-side
+ * status bits (QSGB_DEV_*) into it; the host reads it at its next sync.
+ */
+#ifndef QSGB_H_
+#define QSGB_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (host return values) ---- */
+#define QSGB_OK 0
+#define QSGB_ERR_INVALID 1     /* bad argument (shape, pointer, flag) */
+#define QSGB_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define QSGB_ERR_UNSUPPORTED 3 /* valid request this build does not serve */
+#define QSGB_ERR_SCRATCH 4     /* caller scratch buffer too small */
+
+/* ---- device status bits (written into *dev_status) ---- */
+#define QSGB_DEV_RANGE 1u      /* df64 arithmetic saw |x| >= 2^128, inf or nan */
+#define QSGB_DEV_TIMEOUT 2u    /* a bounded device-side wait gave up */
+#define QSGB_DEV_BADITEM 4u    /* batched work queue met a malformed item */
+
+/* ---- storage element types ---- */
+#define QSGB_F64 0
+#define QSGB_F32 1
+
+/* ---- arithmetic of apply_ptm ---- */
+#define QSGB_ARITH_AUTO 0  /* F64 storage -> DF64; F32 storage -> F32 */
+#define QSGB_ARITH_DF64 1  /* float-float (48-bit significand) on the FP32
+                              pipes; single-term rows use one FP64 multiply */
+#define QSGB_ARITH_F64 2   /* native FP64 FMA (exact IEEE, slow on GB300) */
+#define QSGB_ARITH_F32 3   /* FP32 FMA (F32 storage only) */
+
+/* ---- PTM layout flags ---- */
+#define QSGB_PTM_SWAPPED 1    /* 2-qudit PTM given in order (less significant,
+                                 more significant) qudit: the reference's
+                                 `qubit0 > qubit1` case, cuda.py:171-173 */
+#define QSGB_PTM_TRANSPOSED 2 /* apply the transpose of the stored PTM
+                                 (adjoint / gradient w.r.t. the state) */
+#define QSGB_PTM_HOST 4       /* `ptm` is a HOST pointer; its d_out*d_in <=
+                                 256 entries are copied into the launch
+                                 parameters (no device copy, no allocation) */
+
+/* Version of this ABI (bumped on any signature change). */
+int qsgb_abi_version(void);
+
+/* Human-readable text for a status code (static storage). */
+const char* qsgb_status_string(int status);
+
+/*
+ * One-qudit PTM application.
+ * Replaces: quantumsim/pauli_vectors/cuda.py:223-277 (_apply_single_qubit_ptm
+ * launching primitives.cu:15-89 with dim_a_in = 1) and
+ * quantumsim/pauli_vectors/numpy.py:50-64 (np.einsum).
+ *
+ *   out[y, r, z] = sum_k P[r, k] * in[y, k, z]
+ *
+ * in  : tensor viewed as (dim_y, d_in, dim_z), `dtype` elements
+ * out : tensor viewed as (dim_y, d_out, dim_z); must not alias `in`
+ * ptm : FP64 matrix, row-major (d_out, d_in), on the device (or on the host
+ *       with QSGB_PTM_HOST); with QSGB_PTM_TRANSPOSED it is stored as
+ *       (d_in, d_out) and its transpose is applied
+ * max_terms : upper bound on the number of non-zero PTM entries
+ *       (d_out*d_in is always safe; smaller values shrink shared memory)
+ */
+int qsgb_apply_ptm1(const void* in, void* out, const double* ptm,
+                    int64_t d_out, int64_t d_in, int64_t dim_y, int64_t dim_z,
+                    int ptm_flags, int dtype, int arith, int64_t max_terms,
+                    unsigned* dev_status, void* stream);
+
+/*
+ * Two-qudit PTM application on qudits a < b (a more significant).
+ * Replaces: quantumsim/pauli_vectors/cuda.py:151-221 (_apply_two_qubit_ptm,
+ * primitives.cu:15-89 two_qubit_general_ptm) and numpy.py:50-64.
+ *
+ *   out[x, ra, y, rb, z] = sum_{ka,kb} P[ra, rb, ka, kb] * in[x, ka, y, kb, z]
+ *
+ * in  : viewed as (dim_x, d0_in, dim_y, d1_in, dim_z)
+ * out : viewed as (dim_x, d0_out, dim_y, d1_out, dim_z); must not alias `in`
+ * ptm : FP64 (device, or host with QSGB_PTM_HOST), row-major
+ *       (d0_out, d1_out, d0_in, d1_in), index 0 =
+ *       qudit a.  QSGB_PTM_SWAPPED: stored as (d1_out, d0_out, d1_in, d0_in).
+ *       QSGB_PTM_TRANSPOSED: stored as the forward PTM (in/out exchanged).
+ */
+int qsgb_apply_ptm2(const void* in, void* out, const double* ptm,
+                    int64_t d0_out, int64_t d1_out, int64_t d0_in,
+                    int64_t d1_in, int64_t dim_x, int64_t dim_y, int64_t dim_z,
+                    int ptm_flags, int dtype, int arith, int64_t max_terms,
+                    unsigned* dev_status, void* stream);
+
+/*
+ * Multi-axis take ("multitake"): out = in[np.ix_(idx_0, ..., idx_{n-1})].
+ * Replaces: quantumsim/pauli_vectors/primitives.cu:100-130 (multitake, used by
+ * cuda.py:279-345 diagonal()).  Index lists are CSR-like as in cuda.py:307-313
+ * but HOST arrays (copied into the launch): idx_off[ndim+1] offsets into
+ * idx[].  An index of -1 writes 0 (a basis element absent from a subbasis).
+ * in_dtype / out_dtype may differ (F32 -> F64 widening for diagonals).
+ * ndim <= 32, idx_off[ndim] <= 2048.
+ */
+int qsgb_gather(const void* in, void* out, int in_dtype, int out_dtype,
+                int ndim, const int64_t* in_shape, const int32_t* idx_off,
+                const int32_t* idx, void* stream);
+
+/*
+ * Take along one axis: out[o, j, i] = in[o, idx[j], i] for a tensor viewed as
+ * (outer, d_in, inner).  The per-qudit basis reduction (`reduce_basis`, e.g.
+ * 9 -> 3 with the computational subbasis) and `project` (-> 1 element).
+ * Reference semantics: apply_ptm of the selection PTM eye(d_in)[idx]
+ * (quantumsim/operations/operation.py:549-551, bases/pauli_basis.py:70-89).
+ * idx: HOST array of d_out entries (copied into the launch), -1 writes 0.
+ * Bit-exact copy.  d_out <= 2048.
+ */
+int qsgb_take_axis(const void* in, void* out, int dtype, int64_t outer,
+                   int64_t d_in, int64_t inner, const int32_t* idx,
+                   int64_t d_out, void* stream);
+
+/*
+ * Marginal probabilities from an FP64 diagonal (the DM diagonal, shape
+ * `shape[0..ndim)` C order): out[j] = sum of diag entries whose index along
+ * axis `axis` equals j, j < shape[axis]; axis == -1 gives the trace in
+ * out[0].  Deterministic two-stage reduction with FP64 accumulation.
+ * Replaces: cuda.py:355-384 (meas_prob: one ReductionKernel launch per
+ * outcome) and cuda.py:347-349 (trace: D2H + np.sum); numpy.py:82-84,97-107.
+ * scratch: device buffer of qsgb_marginals_scratch_bytes(...) bytes.
+ */
+int64_t qsgb_marginals_scratch_bytes(int64_t n, int64_t n_out);
+int qsgb_marginals(const double* diag, int ndim, const int64_t* shape,
+                   int axis, double* out, void* scratch, int64_t scratch_bytes,
+                   void* stream);
+
+/*
+ * Partial trace: out[kept...] = sum over traced qudits t of
+ *   in[...] * prod_t w_t[k_t]
+ * with w_t[k] = Re tr(P_k) of qudit t's basis (numpy.py:86-95).  Kept
+ * qudits appear in ascending order in `out`.  keep[i] != 0 keeps qudit i.
+ * weights: HOST array, the concatenation of w_t over traced qudits in
+ * ascending order (copied into the launch; zero weights are skipped).
+ * FP64 accumulation for both storage types; out has the `dtype` of in.
+ */
+int qsgb_partial_trace(const void* in, void* out, int dtype, int ndim,
+                       const int64_t* shape, const int32_t* keep,
+                       const double* weights, void* stream);
+
+/* x[i] *= alpha for i < n (renormalize: numpy.py:109-117, cuda.py:386-395) */
+int qsgb_scale(void* x, int dtype, int64_t n, double alpha, void* stream);
+
+/*
+ * x[i] *= 1 / *denom (device scalar) when *denom > threshold, else x is
+ * left unchanged.  Renormalisation without a host round trip.
+ */
+int qsgb_scale_by_inverse(void* x, int dtype, int64_t n, const double* denom,
+                          double threshold, void* stream);
+
+/*
+ * Gradient of apply_ptm with respect to the PTM (reverse mode):
+ *   dP[r, k] = sum_{groups} g_out[..., r, ...] * x_in[..., k, ...]
+ * a tall-skinny reduction over the bystander index, FP64 accumulation.
+ * dptm: device FP64 (d_out, d_in) [1 qudit] or (d0o, d1o, d0i, d1i)
+ * [2 qudits, qudit a first], overwritten.  The state gradient uses
+ * qsgb_apply_ptm* with QSGB_PTM_TRANSPOSED.
+ * scratch: qsgb_ptm_grad_scratch_bytes(n_groups, k_out, k_in) bytes.
+ */
+int64_t qsgb_ptm_grad_scratch_bytes(int64_t n_groups, int64_t k_out,
+                                    int64_t k_in);
+int qsgb_ptm_grad1(const void* x_in, const void* g_out, double* dptm,
+                   int64_t d_out, int64_t d_in, int64_t dim_y, int64_t dim_z,
+                   int dtype, void* scratch, int64_t scratch_bytes,
+                   void* stream);
+int qsgb_ptm_grad2(const void* x_in, const void* g_out, double* dptm,
+                   int64_t d0_out, int64_t d1_out, int64_t d0_in,
+                   int64_t d1_in, int64_t dim_x, int64_t dim_y, int64_t dim_z,
+                   int dtype, void* scratch, int64_t scratch_bytes,
+                   void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QSGB_H_ */

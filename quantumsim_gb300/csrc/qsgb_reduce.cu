@@ -1,0 +1,437 @@
+// Gathers and reductions of the Pauli vector: multitake (diagonal), take
+// along one axis (reduce_basis / project), marginal probabilities and trace,
+// partial trace, and scaling (renormalize).
+//
+// All reductions are deterministic (fixed trees, no floating-point atomics)
+// and accumulate in FP64 for both storage types.
+#include <algorithm>
+
+#include "qsgb_common.cuh"
+
+namespace qsgb {
+namespace {
+
+constexpr int kMaxDim = 32;
+constexpr int kMaxIdx = 2048;
+
+__device__ __forceinline__ double load_f64(const void* p, int64_t i, int dtype) {
+  return dtype == QSGB_F64 ? static_cast<const double*>(p)[i] : (double)static_cast<const float*>(p)[i];
+}
+
+__device__ __forceinline__ void store_from_f64(void* p, int64_t i, int dtype, double v) {
+  if (dtype == QSGB_F64)
+    static_cast<double*>(p)[i] = v;
+  else
+    static_cast<float*>(p)[i] = (float)v;
+}
+
+// ---------------------------------------------------------------- multitake
+struct GatherParams {
+  const void* in;
+  void* out;
+  int in_dtype, out_dtype;
+  int ndim;
+  uint64_t n_out;
+  FastDiv div[kMaxDim];       // out_shape per axis
+  int64_t in_stride[kMaxDim];
+  int idx_off[kMaxDim + 1];
+  int idx[kMaxIdx];
+};
+
+template <typename TI, typename TO>
+__global__ void gather_kernel(const __grid_constant__ GatherParams p) {
+  const TI* __restrict__ in = static_cast<const TI*>(p.in);
+  TO* __restrict__ out = static_cast<TO*>(p.out);
+  for (uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p.n_out;
+       o += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t rem = o;
+    int64_t addr = 0;
+    bool zero = false;
+    for (int a = p.ndim - 1; a >= 0; --a) {
+      const uint64_t q = fdiv(rem, p.div[a]);
+      const int i = (int)(rem - q * p.div[a].d);
+      rem = q;
+      const int j = p.idx[p.idx_off[a] + i];
+      zero |= (j < 0);
+      addr += (int64_t)(j < 0 ? 0 : j) * p.in_stride[a];
+    }
+    out[o] = zero ? (TO)0 : (TO)in[addr];
+  }
+}
+
+// ---------------------------------------------------------------- take axis
+struct TakeParams {
+  const void* in;
+  void* out;
+  uint64_t n_out;
+  FastDiv div_inner, div_dout;
+  int64_t d_in, inner;
+  int idx[kMaxIdx];
+};
+
+template <typename T>
+__global__ void take_kernel(const __grid_constant__ TakeParams p) {
+  const T* __restrict__ in = static_cast<const T*>(p.in);
+  T* __restrict__ out = static_cast<T*>(p.out);
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < p.n_out;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t t = fdiv(e, p.div_inner);
+    const uint64_t i = e - t * p.inner;
+    const uint64_t o = fdiv(t, p.div_dout);
+    const int j = (int)(t - o * p.div_dout.d);
+    const int src = p.idx[j];
+    out[e] = src < 0 ? (T)0 : in[((int64_t)o * p.d_in + src) * p.inner + (int64_t)i];
+  }
+}
+
+// ---------------------------------------------------------------- marginals
+// Stage 1: block (c, j) sums the entries of chunk c whose index along the
+// axis is j.  Entry m of that set (m < n/d) sits at (m / s) * d * s + j*s +
+// m % s, s = product of the dims after the axis.
+constexpr int kRedBlock = 256;
+constexpr int kMaxChunks = 512;
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nw; ++i) r += sh[i];
+  return r;  // valid in thread 0
+}
+
+__global__ void marg_stage1(const double* __restrict__ diag, uint64_t per_j, FastDiv div_s, int64_t d, int64_t s,
+                            uint64_t chunk, double* __restrict__ part) {
+  __shared__ double sh[32];
+  const int j = blockIdx.y;
+  const uint64_t m0 = (uint64_t)blockIdx.x * chunk;
+  const uint64_t m1 = min(per_j, m0 + chunk);
+  double acc = 0.0;
+  for (uint64_t m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+    const uint64_t hi = fdiv(m, div_s);
+    const uint64_t lo = m - hi * (uint64_t)s;
+    acc += diag[(hi * (uint64_t)d + (uint64_t)j) * (uint64_t)s + lo];
+  }
+  const double r = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[(int64_t)j * gridDim.x + blockIdx.x] = r;
+}
+
+__global__ void marg_stage2(const double* __restrict__ part, int nchunks, double* __restrict__ out) {
+  __shared__ double sh[32];
+  const int j = blockIdx.x;
+  double acc = 0.0;
+  for (int c = threadIdx.x; c < nchunks; c += blockDim.x) acc += part[(int64_t)j * nchunks + c];
+  const double r = block_sum(acc, sh);
+  if (threadIdx.x == 0) out[j] = r;
+}
+
+// ---------------------------------------------------------------- partial trace
+constexpr int kMaxPtEntries = 1024;
+
+struct PtParams {
+  const void* in;
+  void* out;
+  int dtype;
+  int nkeep, ntr;
+  uint64_t n_out, n_combos;
+  FastDiv kdiv[kMaxDim];         // kept dims (ascending qudit order)
+  int64_t kstride[kMaxDim];
+  FastDiv tdiv[kMaxDim];         // traced: number of non-zero weights
+  int64_t tstride[kMaxDim];
+  int toff[kMaxDim + 1];
+  int tidx[kMaxPtEntries];
+  double tw[kMaxPtEntries];
+};
+
+__device__ __forceinline__ int64_t pt_base(const PtParams& p, uint64_t o) {
+  int64_t base = 0;
+  for (int a = p.nkeep - 1; a >= 0; --a) {
+    const uint64_t q = fdiv(o, p.kdiv[a]);
+    base += (int64_t)(o - q * p.kdiv[a].d) * p.kstride[a];
+    o = q;
+  }
+  return base;
+}
+
+__device__ __forceinline__ double pt_term(const PtParams& p, int64_t base, uint64_t c) {
+  int64_t addr = base;
+  double w = 1.0;
+  for (int a = p.ntr - 1; a >= 0; --a) {
+    const uint64_t q = fdiv(c, p.tdiv[a]);
+    const int i = p.toff[a] + (int)(c - q * p.tdiv[a].d);
+    c = q;
+    addr += (int64_t)p.tidx[i] * p.tstride[a];
+    w *= p.tw[i];
+  }
+  return w * load_f64(p.in, addr, p.dtype);
+}
+
+// few combos: one thread per output element
+__global__ void pt_thread_kernel(const __grid_constant__ PtParams p) {
+  for (uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p.n_out;
+       o += (uint64_t)gridDim.x * blockDim.x) {
+    const int64_t base = pt_base(p, o);
+    double acc = 0.0;
+    for (uint64_t c = 0; c < p.n_combos; ++c) acc += pt_term(p, base, c);
+    store_from_f64(p.out, (int64_t)o, p.dtype, acc);
+  }
+}
+
+// many combos: one block per output element
+__global__ void pt_block_kernel(const __grid_constant__ PtParams p) {
+  __shared__ double sh[32];
+  for (uint64_t o = blockIdx.x; o < p.n_out; o += gridDim.x) {
+    const int64_t base = pt_base(p, o);
+    double acc = 0.0;
+    for (uint64_t c = threadIdx.x; c < p.n_combos; c += blockDim.x) acc += pt_term(p, base, c);
+    const double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) store_from_f64(p.out, (int64_t)o, p.dtype, r);
+  }
+}
+
+// ---------------------------------------------------------------- scaling
+template <typename T>
+__global__ void scale_kernel(T* __restrict__ x, uint64_t n, double alpha, const double* __restrict__ denom,
+                             double thr) {
+  double a = alpha;
+  if (denom) {
+    const double d = *denom;
+    if (!(d > thr)) return;
+    a = 1.0 / d;
+  }
+  const T ta = (T)a;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    x[i] = x[i] * ta;
+}
+
+unsigned grid_for(uint64_t n, int block, int per_sm = 8) {
+  const uint64_t need = (n + block - 1) / block;
+  const uint64_t cap = (uint64_t)sm_count() * per_sm;
+  return (unsigned)std::max<uint64_t>(1, std::min(need, cap));
+}
+
+}  // namespace
+}  // namespace qsgb
+
+using namespace qsgb;
+
+extern "C" int qsgb_gather(const void* in, void* out, int in_dtype, int out_dtype, int ndim, const int64_t* in_shape,
+                           const int32_t* idx_off, const int32_t* idx, void* stream) {
+  if (!in || !out || !in_shape || !idx_off || (!idx && ndim > 0)) return QSGB_ERR_INVALID;
+  if (ndim < 0 || ndim > kMaxDim) return QSGB_ERR_UNSUPPORTED;
+  if ((in_dtype != QSGB_F64 && in_dtype != QSGB_F32) || (out_dtype != QSGB_F64 && out_dtype != QSGB_F32))
+    return QSGB_ERR_INVALID;
+  if (idx_off[0] != 0 || idx_off[ndim] > kMaxIdx) return QSGB_ERR_UNSUPPORTED;
+  GatherParams p{};  // copied into the launch
+  p.in = in;
+  p.out = out;
+  p.in_dtype = in_dtype;
+  p.out_dtype = out_dtype;
+  p.ndim = ndim;
+  uint64_t n_out = 1;
+  int64_t stride = 1;
+  for (int a = ndim - 1; a >= 0; --a) {
+    const int len = idx_off[a + 1] - idx_off[a];
+    if (len < 1 || in_shape[a] < 1) return QSGB_ERR_INVALID;
+    for (int i = idx_off[a]; i < idx_off[a + 1]; ++i)
+      if (idx[i] >= in_shape[a] || idx[i] < -1) return QSGB_ERR_INVALID;
+    p.div[a] = make_fastdiv((uint64_t)len);
+    p.in_stride[a] = stride;
+    stride *= in_shape[a];
+    n_out *= (uint64_t)len;
+  }
+  for (int a = 0; a <= ndim; ++a) p.idx_off[a] = idx_off[a];
+  for (int i = 0; i < idx_off[ndim]; ++i) p.idx[i] = idx[i];
+  p.n_out = n_out;
+  cudaStream_t s = as_stream(stream);
+  const int block = 256;
+  const unsigned grid = grid_for(n_out, block);
+  if (in_dtype == QSGB_F64 && out_dtype == QSGB_F64)
+    gather_kernel<double, double><<<grid, block, 0, s>>>(p);
+  else if (in_dtype == QSGB_F32 && out_dtype == QSGB_F64)
+    gather_kernel<float, double><<<grid, block, 0, s>>>(p);
+  else if (in_dtype == QSGB_F64 && out_dtype == QSGB_F32)
+    gather_kernel<double, float><<<grid, block, 0, s>>>(p);
+  else
+    gather_kernel<float, float><<<grid, block, 0, s>>>(p);
+  return launch_status();
+}
+
+extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t outer, int64_t d_in, int64_t inner,
+                              const int32_t* idx, int64_t d_out, void* stream) {
+  if (!in || !out || !idx || in == out) return QSGB_ERR_INVALID;
+  if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
+  if (outer < 1 || d_in < 1 || inner < 1 || d_out < 1) return QSGB_ERR_INVALID;
+  if (d_out > kMaxIdx) return QSGB_ERR_UNSUPPORTED;
+  TakeParams p{};
+  p.in = in;
+  p.out = out;
+  p.n_out = (uint64_t)outer * d_out * inner;
+  p.div_inner = make_fastdiv((uint64_t)inner);
+  p.div_dout = make_fastdiv((uint64_t)d_out);
+  p.d_in = d_in;
+  p.inner = inner;
+  for (int64_t j = 0; j < d_out; ++j) {
+    if (idx[j] >= d_in || idx[j] < -1) return QSGB_ERR_INVALID;
+    p.idx[j] = idx[j];
+  }
+  const int block = 256;
+  cudaStream_t s = as_stream(stream);
+  if (dtype == QSGB_F64)
+    take_kernel<double><<<grid_for(p.n_out, block), block, 0, s>>>(p);
+  else
+    take_kernel<float><<<grid_for(p.n_out, block), block, 0, s>>>(p);
+  return launch_status();
+}
+
+static void marg_geometry(int64_t n, int64_t n_out, int* nchunks, uint64_t* chunk) {
+  const uint64_t per_j = (uint64_t)(n / std::max<int64_t>(n_out, 1));
+  uint64_t c = std::max<uint64_t>(4096, (per_j + kMaxChunks - 1) / kMaxChunks);
+  int nc = (int)std::max<uint64_t>(1, (per_j + c - 1) / c);
+  *nchunks = nc;
+  *chunk = c;
+}
+
+extern "C" int64_t qsgb_marginals_scratch_bytes(int64_t n, int64_t n_out) {
+  if (n < 1 || n_out < 1) return 0;
+  int nc;
+  uint64_t c;
+  marg_geometry(n, n_out, &nc, &c);
+  return (int64_t)nc * n_out * (int64_t)sizeof(double);
+}
+
+extern "C" int qsgb_marginals(const double* diag, int ndim, const int64_t* shape, int axis, double* out,
+                              void* scratch, int64_t scratch_bytes, void* stream) {
+  if (!diag || !out || (!shape && ndim > 0)) return QSGB_ERR_INVALID;
+  if (ndim < 0 || axis < -1 || axis >= ndim) return QSGB_ERR_INVALID;
+  int64_t n = 1, s = 1;
+  for (int a = 0; a < ndim; ++a) {
+    if (shape[a] < 1) return QSGB_ERR_INVALID;
+    n *= shape[a];
+    if (a > axis && axis >= 0) s *= shape[a];
+  }
+  const int64_t d = axis < 0 ? 1 : shape[axis];
+  if (axis < 0) s = 1;
+  if (d > 65535) return QSGB_ERR_UNSUPPORTED;
+  int nc;
+  uint64_t chunk;
+  marg_geometry(n, d, &nc, &chunk);
+  if (!scratch || scratch_bytes < (int64_t)nc * d * (int64_t)sizeof(double)) return QSGB_ERR_SCRATCH;
+  double* part = static_cast<double*>(scratch);
+  cudaStream_t st = as_stream(stream);
+  const uint64_t per_j = (uint64_t)(n / d);
+  marg_stage1<<<dim3(nc, (unsigned)d), kRedBlock, 0, st>>>(diag, per_j, make_fastdiv((uint64_t)s), d, s, chunk, part);
+  marg_stage2<<<(unsigned)d, kRedBlock, 0, st>>>(part, nc, out);
+  return launch_status();
+}
+
+extern "C" int qsgb_partial_trace(const void* in, void* out, int dtype, int ndim, const int64_t* shape,
+                                  const int32_t* keep, const double* weights, void* stream) {
+  if (!in || !out || in == out || (ndim > 0 && (!shape || !keep))) return QSGB_ERR_INVALID;
+  if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
+  if (ndim < 0 || ndim > kMaxDim) return QSGB_ERR_UNSUPPORTED;
+  PtParams p{};
+  p.in = in;
+  p.out = out;
+  p.dtype = dtype;
+  int64_t stride = 1;
+  int nent = 0;
+  int nkeep = 0, ntr = 0;
+  for (int a = 0; a < ndim; ++a) (keep[a] ? nkeep : ntr)++;
+  if (ntr > 0 && !weights) return QSGB_ERR_INVALID;
+  // walk from the least significant axis
+  int woffs[kMaxDim];
+  {
+    int off = 0;
+    for (int a = 0; a < ndim; ++a)
+      if (!keep[a]) {
+        woffs[a] = off;
+        off += (int)shape[a];
+      }
+  }
+  uint64_t n_out = 1, n_combos = 1;
+  int kpos = nkeep, tpos = ntr;
+  int toff_rev[kMaxDim];
+  for (int a = ndim - 1; a >= 0; --a) {
+    if (shape[a] < 1) return QSGB_ERR_INVALID;
+    if (keep[a]) {
+      --kpos;
+      p.kdiv[kpos] = make_fastdiv((uint64_t)shape[a]);
+      p.kstride[kpos] = stride;
+      n_out *= (uint64_t)shape[a];
+    } else {
+      --tpos;
+      int cnt = 0;
+      toff_rev[tpos] = nent;
+      for (int64_t k = 0; k < shape[a]; ++k) {
+        const double w = weights[woffs[a] + k];
+        if (w != 0.0) {
+          if (nent >= kMaxPtEntries) return QSGB_ERR_UNSUPPORTED;
+          p.tidx[nent] = (int)k;
+          p.tw[nent] = w;
+          ++nent;
+          ++cnt;
+        }
+      }
+      p.tdiv[tpos] = make_fastdiv((uint64_t)std::max(cnt, 1));
+      p.tstride[tpos] = stride;
+      if (cnt == 0) n_combos = 0;
+      else n_combos *= (uint64_t)cnt;
+    }
+    stride *= shape[a];
+  }
+  // entries were appended from the last traced axis backwards; toff[t] is
+  // the start of traced axis t (ascending)
+  for (int t = 0; t < ntr; ++t) p.toff[t] = toff_rev[t];
+  p.toff[ntr] = nent;
+  p.nkeep = nkeep;
+  p.ntr = ntr;
+  p.n_out = n_out;
+  p.n_combos = n_combos;
+  cudaStream_t s = as_stream(stream);
+  if (n_combos == 0) {
+    QSGB_CUDA_TRY(cudaMemsetAsync(out, 0, n_out * (dtype == QSGB_F64 ? 8 : 4), s));
+    return QSGB_OK;
+  }
+  if (n_combos <= 64) {
+    pt_thread_kernel<<<grid_for(n_out, 256), 256, 0, s>>>(p);
+  } else {
+    const int block = n_combos >= 256 ? 256 : 128;
+    pt_block_kernel<<<(unsigned)std::min<uint64_t>(n_out, (uint64_t)sm_count() * 16), block, 0, s>>>(p);
+  }
+  return launch_status();
+}
+
+extern "C" int qsgb_scale(void* x, int dtype, int64_t n, double alpha, void* stream) {
+  if (!x || n < 0) return QSGB_ERR_INVALID;
+  if (n == 0) return QSGB_OK;
+  cudaStream_t s = as_stream(stream);
+  if (dtype == QSGB_F64)
+    scale_kernel<double><<<grid_for((uint64_t)n, 256), 256, 0, s>>>(static_cast<double*>(x), (uint64_t)n, alpha,
+                                                                   nullptr, 0.0);
+  else if (dtype == QSGB_F32)
+    scale_kernel<float><<<grid_for((uint64_t)n, 256), 256, 0, s>>>(static_cast<float*>(x), (uint64_t)n, alpha,
+                                                                 nullptr, 0.0);
+  else
+    return QSGB_ERR_INVALID;
+  return launch_status();
+}
+
+extern "C" int qsgb_scale_by_inverse(void* x, int dtype, int64_t n, const double* denom, double threshold,
+                                     void* stream) {
+  if (!x || !denom || n < 0) return QSGB_ERR_INVALID;
+  if (n == 0) return QSGB_OK;
+  cudaStream_t s = as_stream(stream);
+  if (dtype == QSGB_F64)
+    scale_kernel<double><<<grid_for((uint64_t)n, 256), 256, 0, s>>>(static_cast<double*>(x), (uint64_t)n, 1.0,
+                                                                   denom, threshold);
+  else if (dtype == QSGB_F32)
+    scale_kernel<float><<<grid_for((uint64_t)n, 256), 256, 0, s>>>(static_cast<float*>(x), (uint64_t)n, 1.0,
+                                                                 denom, threshold);
+  else
+    return QSGB_ERR_INVALID;
+  return launch_status();
+}

@@ -1,0 +1,371 @@
+"""PyTorch custom operators over the C ABI (``torch.ops.qsgb.*``).
+
+Each operator takes torch tensors (device memory and the current CUDA stream
+come from PyTorch), checks arguments on the host, and calls one entry point
+of ``libqsgb.so``.  Shapes follow the Pauli-vector convention: a state is an
+n-dimensional tensor whose axis i has length dim_pauli of qudit i, C order,
+qudit 0 first.
+
+There is no fallback path: on a tensor that is not on a CUDA device the
+operators raise.
+"""
+import ctypes
+import math
+from typing import List
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+_STATUS = {}
+_PTM_HOST_MAX = 256
+
+
+def _stream_handle(t):
+    return ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+
+
+def _dtype_code(t):
+    if t.dtype == torch.float64:
+        return L.F64
+    if t.dtype == torch.float32:
+        return L.F32
+    raise TypeError('Pauli vectors must be float64 or float32 tensors, got '
+                    '{}'.format(t.dtype))
+
+
+def _require_cuda(*tensors):
+    for t in tensors:
+        if not t.is_cuda:
+            raise RuntimeError('qsgb operators run on CUDA tensors only '
+                               '(got a tensor on {})'.format(t.device))
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def status_tensor(device):
+    """Per-device word that kernels OR their QSGB_DEV_* bits into."""
+    device = torch.device(device)
+    key = device.index if device.index is not None else torch.cuda.current_device()
+    st = _STATUS.get(key)
+    if st is None:
+        st = torch.zeros(1, dtype=torch.int32, device=torch.device('cuda', key))
+        _STATUS[key] = st
+    return st
+
+
+def check_device_status(device):
+    """Raise if a kernel reported a device-side problem since the last check
+    (synchronises the device's current stream)."""
+    st = status_tensor(device)
+    val = int(st.item())
+    if val:
+        st.zero_()
+        reasons = []
+        if val & L.DEV_RANGE:
+            reasons.append('a Pauli-vector entry or PTM result left the '
+                           'float-float range (|x| >= 2^128, inf or nan)')
+        if val & L.DEV_TIMEOUT:
+            reasons.append('a bounded device-side wait timed out')
+        if val & L.DEV_BADITEM:
+            reasons.append('a kernel rejected a malformed work item')
+        raise RuntimeError('qsgb device status {}: {}'.format(
+            val, '; '.join(reasons)))
+
+
+def apply_geometry(shape, qudits, ptm_shape, transpose=False):
+    """Sizes of a PTM application.
+
+    Returns (new_shape, (X, Y, Z), dims) where dims = (da_out, db_out, da_in,
+    db_in) for qudits a < b (one qudit: da = 1), plus the swapped flag.
+    ``ptm_shape`` is the stored PTM shape in argument order (out..., in...);
+    with ``transpose`` the stored matrix is the forward PTM whose transpose
+    is applied (its in/out halves are exchanged).
+    """
+    n = len(qudits)
+    half = len(ptm_shape) // 2
+    outs, ins = list(ptm_shape[:half]), list(ptm_shape[half:])
+    if transpose:
+        outs, ins = ins, outs
+    new_shape = list(shape)
+    for q, dout, din in zip(qudits, outs, ins):
+        if shape[q] != din:
+            raise ValueError(
+                'PTM input dimension {} does not match dimension {} of qudit '
+                '{}'.format(din, shape[q], q))
+        new_shape[q] = dout
+    if n == 1:
+        (q,) = qudits
+        X = 1
+        Y = math.prod(shape[:q])
+        Z = math.prod(shape[q + 1:])
+        dims = (1, outs[0], 1, ins[0])
+        swapped = False
+    else:
+        q0, q1 = qudits
+        swapped = q0 > q1
+        a, b = (q1, q0) if swapped else (q0, q1)
+        X = math.prod(shape[:a])
+        Y = math.prod(shape[a + 1:b])
+        Z = math.prod(shape[b + 1:])
+        if swapped:
+            dims = (outs[1], outs[0], ins[1], ins[0])
+        else:
+            dims = (outs[0], outs[1], ins[0], ins[1])
+    return new_shape, (X, Y, Z), dims, swapped
+
+
+# --------------------------------------------------------------- apply_ptm
+@torch.library.custom_op('qsgb::apply_ptm', mutates_args=())
+def apply_ptm(pv: torch.Tensor, ptm: torch.Tensor, qudits: List[int],
+              arith: int, max_terms: int, transpose: bool) -> torch.Tensor:
+    """Apply a 1- or 2-qudit PTM (float64) to a Pauli-vector tensor.
+
+    ``ptm`` may live on the device or (up to 16x16) on the host, in which
+    case it is passed inside the kernel launch."""
+    _require_cuda(pv)
+    if ptm.dtype != torch.float64:
+        raise TypeError('PTM must be float64')
+    new_shape, (X, Y, Z), (dao, dbo, dai, dbi), swapped = apply_geometry(
+        pv.shape, qudits, ptm.shape, transpose)
+    pv = pv.contiguous()
+    ptm = ptm.contiguous()
+    out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
+    flags = (L.PTM_SWAPPED if swapped else 0) | (
+        L.PTM_TRANSPOSED if transpose else 0)
+    if ptm.is_cuda:
+        if ptm.device != pv.device:
+            raise ValueError('PTM and Pauli vector are on different devices')
+    else:
+        if ptm.numel() > _PTM_HOST_MAX:
+            ptm = ptm.to(pv.device, non_blocking=False)
+        else:
+            flags |= L.PTM_HOST
+    lib = L.load()
+    st = status_tensor(pv.device)
+    if out.numel() == 0:
+        return out
+    if len(qudits) == 1:
+        status = lib.qsgb_apply_ptm1(
+            _ptr(pv), _ptr(out), _ptr(ptm), dbo, dbi, Y, Z, flags,
+            _dtype_code(pv), arith, max_terms, _ptr(st), _stream_handle(pv))
+    else:
+        status = lib.qsgb_apply_ptm2(
+            _ptr(pv), _ptr(out), _ptr(ptm), dao, dbo, dai, dbi, X, Y, Z,
+            flags, _dtype_code(pv), arith, max_terms, _ptr(st),
+            _stream_handle(pv))
+    L.check(status, 'qsgb_apply_ptm')
+    return out
+
+
+@apply_ptm.register_fake
+def _(pv, ptm, qudits, arith, max_terms, transpose):
+    new_shape = apply_geometry(pv.shape, qudits, ptm.shape, transpose)[0]
+    return pv.new_empty(new_shape)
+
+
+# --------------------------------------------------------------- ptm_grad
+@torch.library.custom_op('qsgb::ptm_grad', mutates_args=())
+def ptm_grad(x_in: torch.Tensor, g_out: torch.Tensor,
+             qudits: List[int]) -> torch.Tensor:
+    """dL/dPTM for out = apply_ptm(x_in, PTM, qudits), given dL/dout.
+
+    Returned in the PTM's argument-order layout (out..., in...), float64."""
+    _require_cuda(x_in, g_out)
+    if x_in.dtype != g_out.dtype:
+        raise TypeError('x_in and g_out must share a dtype')
+    n = len(qudits)
+    outs = [g_out.shape[q] for q in qudits]
+    ins = [x_in.shape[q] for q in qudits]
+    x_in = x_in.contiguous()
+    g_out = g_out.contiguous()
+    lib = L.load()
+    shape = list(x_in.shape)
+    if n == 1:
+        (q,) = qudits
+        Y, Z = math.prod(shape[:q]), math.prod(shape[q + 1:])
+        groups, kout, kin = Y * Z, outs[0], ins[0]
+    else:
+        a, b = sorted(qudits)
+        X = math.prod(shape[:a])
+        Y = math.prod(shape[a + 1:b])
+        Z = math.prod(shape[b + 1:])
+        groups = X * Y * Z
+        kout, kin = outs[0] * outs[1], ins[0] * ins[1]
+    out_sorted = torch.empty(kout * kin, dtype=torch.float64,
+                             device=x_in.device)
+    nbytes = lib.qsgb_ptm_grad_scratch_bytes(groups, kout, kin)
+    scratch = torch.empty(max(nbytes, 8), dtype=torch.uint8,
+                          device=x_in.device)
+    if n == 1:
+        status = lib.qsgb_ptm_grad1(
+            _ptr(x_in), _ptr(g_out), _ptr(out_sorted), outs[0], ins[0], Y, Z,
+            _dtype_code(x_in), _ptr(scratch), nbytes, _stream_handle(x_in))
+        L.check(status, 'qsgb_ptm_grad1')
+        return out_sorted.view(outs[0], ins[0])
+    a, b = sorted(qudits)
+    da_o, db_o = g_out.shape[a], g_out.shape[b]
+    da_i, db_i = x_in.shape[a], x_in.shape[b]
+    status = lib.qsgb_ptm_grad2(
+        _ptr(x_in), _ptr(g_out), _ptr(out_sorted), da_o, db_o, da_i, db_i, X,
+        Y, Z, _dtype_code(x_in), _ptr(scratch), nbytes, _stream_handle(x_in))
+    L.check(status, 'qsgb_ptm_grad2')
+    res = out_sorted.view(da_o, db_o, da_i, db_i)
+    if qudits[0] > qudits[1]:
+        res = res.permute(1, 0, 3, 2).contiguous()
+    return res
+
+
+@ptm_grad.register_fake
+def _(x_in, g_out, qudits):
+    shape = [g_out.shape[q] for q in qudits] + [x_in.shape[q] for q in qudits]
+    return x_in.new_empty(shape, dtype=torch.float64)
+
+
+# --------------------------------------------------------------- gathers
+@torch.library.custom_op('qsgb::gather', mutates_args=())
+def gather(pv: torch.Tensor, idx_off: List[int], idx: List[int],
+           out_f64: bool) -> torch.Tensor:
+    """Multitake: pv[np.ix_(idx_0, ...)] (flattened); -1 selects a zero."""
+    _require_cuda(pv)
+    pv = pv.contiguous()
+    ndim = pv.dim()
+    n_out = 1
+    for a in range(ndim):
+        n_out *= idx_off[a + 1] - idx_off[a]
+    out = torch.empty(n_out, dtype=torch.float64 if out_f64 else pv.dtype,
+                      device=pv.device)
+    status = L.load().qsgb_gather(
+        _ptr(pv), _ptr(out), _dtype_code(pv), _dtype_code(out), ndim,
+        L.i64_array(pv.shape), L.i32_array(idx_off), L.i32_array(idx),
+        _stream_handle(pv))
+    L.check(status, 'qsgb_gather')
+    return out
+
+
+@gather.register_fake
+def _(pv, idx_off, idx, out_f64):
+    n_out = 1
+    for a in range(pv.dim()):
+        n_out *= idx_off[a + 1] - idx_off[a]
+    return pv.new_empty(n_out, dtype=torch.float64 if out_f64 else pv.dtype)
+
+
+@torch.library.custom_op('qsgb::take_axis', mutates_args=())
+def take_axis(pv: torch.Tensor, axis: int, idx: List[int]) -> torch.Tensor:
+    """pv.index_select(axis, idx) as a bit-exact copy; -1 selects a zero."""
+    _require_cuda(pv)
+    pv = pv.contiguous()
+    shape = list(pv.shape)
+    outer = math.prod(shape[:axis])
+    inner = math.prod(shape[axis + 1:])
+    new_shape = list(shape)
+    new_shape[axis] = len(idx)
+    out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
+    if out.numel() == 0:
+        return out
+    status = L.load().qsgb_take_axis(
+        _ptr(pv), _ptr(out), _dtype_code(pv), outer, shape[axis], inner,
+        L.i32_array(idx), len(idx), _stream_handle(pv))
+    L.check(status, 'qsgb_take_axis')
+    return out
+
+
+@take_axis.register_fake
+def _(pv, axis, idx):
+    shape = list(pv.shape)
+    shape[axis] = len(idx)
+    return pv.new_empty(shape)
+
+
+# --------------------------------------------------------------- reductions
+@torch.library.custom_op('qsgb::marginals', mutates_args=())
+def marginals(diag: torch.Tensor, shape: List[int],
+              axis: int) -> torch.Tensor:
+    """Marginal sums of an FP64 diagonal along `axis` (-1: the trace)."""
+    _require_cuda(diag)
+    if diag.dtype != torch.float64:
+        raise TypeError('diagonal must be float64')
+    diag = diag.contiguous()
+    n_out = 1 if axis < 0 else shape[axis]
+    out = torch.empty(n_out, dtype=torch.float64, device=diag.device)
+    lib = L.load()
+    nbytes = lib.qsgb_marginals_scratch_bytes(max(1, diag.numel()), n_out)
+    scratch = torch.empty(max(8, nbytes), dtype=torch.uint8,
+                          device=diag.device)
+    status = lib.qsgb_marginals(
+        _ptr(diag), len(shape), L.i64_array(shape), axis, _ptr(out),
+        _ptr(scratch), nbytes, _stream_handle(diag))
+    L.check(status, 'qsgb_marginals')
+    return out
+
+
+@marginals.register_fake
+def _(diag, shape, axis):
+    return diag.new_empty(1 if axis < 0 else shape[axis])
+
+
+@torch.library.custom_op('qsgb::partial_trace', mutates_args=())
+def partial_trace(pv: torch.Tensor, keep: List[int],
+                  weights: List[float]) -> torch.Tensor:
+    """Trace out the qudits not flagged in `keep` with per-element weights
+    (concatenated over traced qudits, ascending); kept axes stay in order."""
+    _require_cuda(pv)
+    pv = pv.contiguous()
+    shape = list(pv.shape)
+    new_shape = [d for d, k in zip(shape, keep) if k]
+    out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
+    status = L.load().qsgb_partial_trace(
+        _ptr(pv), _ptr(out), _dtype_code(pv), len(shape), L.i64_array(shape),
+        L.i32_array(keep), L.f64_array(weights), _stream_handle(pv))
+    L.check(status, 'qsgb_partial_trace')
+    return out
+
+
+@partial_trace.register_fake
+def _(pv, keep, weights):
+    return pv.new_empty([d for d, k in zip(pv.shape, keep) if k])
+
+
+@torch.library.custom_op('qsgb::scale_', mutates_args=('pv',))
+def scale_(pv: torch.Tensor, alpha: float) -> None:
+    """pv *= alpha in place."""
+    _require_cuda(pv)
+    if not pv.is_contiguous():
+        raise ValueError('scale_ needs a contiguous tensor')
+    status = L.load().qsgb_scale(_ptr(pv), _dtype_code(pv), pv.numel(),
+                                 float(alpha), _stream_handle(pv))
+    L.check(status, 'qsgb_scale')
+
+
+@torch.library.custom_op('qsgb::scale_by_inverse_', mutates_args=('pv',))
+def scale_by_inverse_(pv: torch.Tensor, denom: torch.Tensor,
+                      threshold: float) -> None:
+    """pv *= 1/denom[0] in place when denom[0] > threshold (device scalar)."""
+    _require_cuda(pv, denom)
+    if not pv.is_contiguous() or denom.dtype != torch.float64:
+        raise ValueError('scale_by_inverse_ needs a contiguous tensor and a '
+                         'float64 denominator')
+    status = L.load().qsgb_scale_by_inverse(
+        _ptr(pv), _dtype_code(pv), pv.numel(), _ptr(denom), float(threshold),
+        _stream_handle(pv))
+    L.check(status, 'qsgb_scale_by_inverse')
+
+
+def nnz_terms(ptm, arith):
+    """Number of PTM entries the kernel keeps (same rule as the device):
+    exact zeros for native FP64, else |p| > 2^-60 max|P| (df64) or
+    2^-40 max|P| (FP32)."""
+    a = np.abs(np.asarray(ptm, dtype=np.float64))
+    if a.size == 0:
+        return 1
+    if arith == L.ARITH_F64:
+        thr = 0.0
+    elif arith == L.ARITH_F32:
+        thr = a.max() * 2.0 ** -40
+    else:
+        thr = a.max() * 2.0 ** -60
+    return max(1, int(np.count_nonzero(a > thr)))

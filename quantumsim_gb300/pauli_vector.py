@@ -1,0 +1,368 @@
+"""``PauliVectorGB300``: the GB300 density-matrix backend.
+
+A drop-in ``PauliVectorBase`` subclass with the surface of the reference
+backends (quantumsim/pauli_vectors/numpy.py:8-121 and
+quantumsim/pauli_vectors/cuda.py:55-425): ``apply_ptm`` for one and two
+qudits on any indices (rectangular PTMs included), ``diagonal``,
+``meas_prob``, ``trace``, ``partial_trace``, ``renormalize`` and ``copy``,
+plus ``reduce_basis`` and ``project``.  All device work goes through the
+``torch.ops.qsgb`` operators over ``libqsgb.so``; there is no CPU path.
+
+Numerical semantics follow ``PauliVectorNumpy`` (the reference oracle):
+
+* the initial state puts 1 at index (0, ..., 0) (numpy.py:39-41);
+* ``diagonal()`` has length prod(dim_hilbert) and contracts each qudit with
+  ``computational_basis_vectors`` (numpy.py:66-80); for bases whose rows are
+  unit vectors (``general(d)`` and its subbases) that is an exact gather;
+* ``meas_prob`` returns an ndarray of length d_hilbert (numpy.py:97-107);
+* ``partial_trace(*qubits)`` keeps ``qubits``: data axes in ascending qudit
+  order, ``bases`` in argument order (numpy.py:86-95);
+* ``renormalize`` warns when the trace is <= 1e-8 and returns the trace
+  before scaling (numpy.py:109-117).
+
+FP64 storage computes PTM products in float-float arithmetic (48-bit
+significand) on the FP32 pipes; ``arith='f64'`` selects native FP64 FMAs.
+``dtype=np.float32`` stores the vector in FP32 while every trace, marginal
+and partial-trace sum still accumulates in FP64.
+"""
+import collections
+import hashlib
+import math
+import warnings
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import ops
+
+try:  # subclass the reference ABC when the quantumsim package is present
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        from quantumsim.pauli_vectors.pauli_vector import \
+            PauliVectorBase as _Base
+    REFERENCE_BASE = True
+except Exception:  # pragma: no cover - depends on the environment
+    from ._base import PauliVectorBase as _Base
+    REFERENCE_BASE = False
+
+_ARITH = {'auto': L.ARITH_AUTO, 'df64': L.ARITH_DF64, 'f64': L.ARITH_F64,
+          'f32': L.ARITH_F32}
+
+
+class _PtmCache:
+    """Device copies of PTMs too large to travel in a kernel launch, keyed
+    by content (the reference keys on hash(bytes), cuda.py:401-420), LRU."""
+
+    def __init__(self, capacity=1024):
+        self.capacity = capacity
+        self._d = collections.OrderedDict()
+
+    def get(self, ptm, device):
+        key = (hashlib.blake2b(ptm.tobytes(), digest_size=16).digest(),
+               ptm.shape, str(device))
+        t = self._d.get(key)
+        if t is None:
+            t = torch.from_numpy(ptm).to(device)
+            self._d[key] = t
+            if len(self._d) > self.capacity:
+                self._d.popitem(last=False)
+        else:
+            self._d.move_to_end(key)
+        return t
+
+
+_PTM_CACHE = _PtmCache()
+
+
+def _diag_plan(bases):
+    """Gather plan for diagonal(): per qudit, for each Hilbert index i the
+    Pauli index x whose computational_basis_vectors row is exactly e_x, or
+    -1 for an all-zero row.  None if some row is neither."""
+    idx_off, idx = [0], []
+    for b in bases:
+        cbv = np.asarray(b.computational_basis_vectors)
+        if np.any(np.imag(cbv) != 0):
+            return None
+        cbv = np.real(cbv)
+        for row in cbv:
+            nz = np.flatnonzero(row)
+            if len(nz) == 0:
+                idx.append(-1)
+            elif len(nz) == 1 and row[nz[0]] == 1.0:
+                idx.append(int(nz[0]))
+            else:
+                return None
+        idx_off.append(len(idx))
+    return idx_off, idx
+
+
+class PauliVectorGB300(_Base):
+    """Density matrix in a Pauli basis, stored on a GB300 (CUDA) device.
+
+    Parameters
+    ----------
+    bases : list of PauliBasis
+        Basis of every qudit.
+    pv : numpy array, torch tensor or None
+        Expansion coefficients, shape ``dim_pauli``; None = |0...0><0...0|
+        (coefficient 1 at index (0, ..., 0)).
+    force : bool
+        Allow more than 2**22 density-matrix elements.
+    dtype : np.float64 (default) or np.float32
+        Storage type of the Pauli vector on the device.
+    device : torch device or None
+        CUDA device (default: the current one).
+    arith : 'auto' | 'df64' | 'f64' | 'f32'
+        Arithmetic of apply_ptm ('auto': df64 for FP64, f32 for FP32).
+    """
+
+    def __init__(self, bases, pv=None, *, force=False, dtype=None,
+                 device=None, arith='auto'):
+        super().__init__(bases, pv, force=force)
+        if not torch.cuda.is_available():
+            raise RuntimeError('PauliVectorGB300 needs a CUDA device')
+        self._device = torch.device(device) if device is not None else \
+            torch.device('cuda', torch.cuda.current_device())
+        if self._device.type != 'cuda':
+            raise ValueError('PauliVectorGB300 lives on a CUDA device')
+        if dtype is None:
+            tdtype = (pv.dtype if isinstance(pv, torch.Tensor) and
+                      pv.dtype == torch.float32 else torch.float64)
+        else:
+            tdtype = torch.float32 if np.dtype(dtype) == np.float32 else \
+                torch.float64
+            if np.dtype(dtype) not in (np.float32, np.float64):
+                raise ValueError('dtype must be float64 or float32')
+        if arith not in _ARITH:
+            raise ValueError('arith must be one of {}'.format(list(_ARITH)))
+        if arith == 'f32' and tdtype != torch.float32 or \
+                arith in ('df64', 'f64') and tdtype != torch.float64:
+            raise ValueError('arith {!r} does not match storage {}'.format(
+                arith, tdtype))
+        self._arith = _ARITH[arith]
+        if self._arith == L.ARITH_AUTO:
+            self._arith = L.ARITH_DF64 if tdtype == torch.float64 else \
+                L.ARITH_F32
+
+        if pv is None:
+            data = torch.zeros(self.dim_pauli, dtype=tdtype,
+                               device=self._device)
+            data[(0,) * self.n_qubits] = 1
+        elif isinstance(pv, np.ndarray):
+            if pv.shape != self.dim_pauli:
+                raise ValueError(
+                    '`bases` Pauli dimensionality should be the same as the '
+                    'shape of `data` array.\n - bases shapes: {}\n - data '
+                    'shape: {}'.format(self.dim_pauli, pv.shape))
+            if pv.dtype not in (np.float16, np.float32, np.float64):
+                raise ValueError('`pv` must have floating point data type, '
+                                 'got {}'.format(pv.dtype))
+            data = torch.from_numpy(np.ascontiguousarray(pv)).to(
+                device=self._device, dtype=tdtype)
+        elif isinstance(pv, torch.Tensor):
+            if tuple(pv.shape) != self.dim_pauli:
+                raise ValueError(
+                    '`bases` Pauli dimensionality should be the same as the '
+                    'shape of `data` array.\n - bases shapes: {}\n - data '
+                    'shape: {}'.format(self.dim_pauli, tuple(pv.shape)))
+            if pv.dtype not in (torch.float16, torch.float32, torch.float64):
+                raise ValueError('`pv` must have floating point data type, '
+                                 'got {}'.format(pv.dtype))
+            data = pv.to(device=self._device, dtype=tdtype).contiguous()
+        else:
+            raise ValueError('`pv` should be a numpy array, a torch tensor or '
+                             'None, got type `{}`'.format(type(pv)))
+        self._data = data
+
+    # ------------------------------------------------------------ accessors
+    @property
+    def data(self):
+        """The device tensor (shape ``dim_pauli``)."""
+        return self._data
+
+    @property
+    def device(self):
+        return self._device
+
+    @property
+    def dtype(self):
+        return np.float64 if self._data.dtype == torch.float64 else np.float32
+
+    def to_pv(self):
+        ops.check_device_status(self._device)
+        return self._data.cpu().numpy()
+
+    def copy(self):
+        return self.__class__(self.bases, self._data.clone(), force=True,
+                              dtype=self.dtype, device=self._device,
+                              arith=self._arith_name())
+
+    def _arith_name(self):
+        for k, v in _ARITH.items():
+            if v == self._arith and k != 'auto':
+                return k
+        return 'auto'
+
+    # ------------------------------------------------------------ apply_ptm
+    def _device_ptm(self, ptm):
+        """Host PTMs up to 16x16 ride in the launch; larger ones are cached
+        on the device by content."""
+        if ptm.size <= 256:
+            return torch.from_numpy(ptm)
+        return _PTM_CACHE.get(ptm, self._device)
+
+    def apply_ptm(self, ptm, *qubits):
+        """Apply a PTM of shape (d_out..., d_in...) to `qubits` (argument
+        order, any position); ``bases`` are left to the caller
+        (quantumsim/operations/operation.py:549-551)."""
+        n = len(qubits)
+        if isinstance(ptm, torch.Tensor):
+            ptm_t = ptm.to(torch.float64)
+            shape = tuple(ptm_t.shape)
+        else:
+            ptm = np.ascontiguousarray(ptm, dtype=np.float64)
+            shape = ptm.shape
+            ptm_t = None
+        if len(shape) != 2 * n:
+            raise ValueError('{}-qubit PTM must have {} dimensions, got {}'
+                             .format(n, 2 * n, len(shape)))
+        if n == 0:
+            raise NotImplementedError('Applying a 0-qubit PTM is not '
+                                      'implemented in this backend.')
+        if n > 2:
+            raise NotImplementedError('Applying {}-qubit PTM is not '
+                                      'implemented in the active backend.'
+                                      .format(n))
+        for i, q in enumerate(qubits):
+            self._validate_qubit(q, 'qubit{}'.format(i))
+        if n == 2 and qubits[0] == qubits[1]:
+            raise ValueError('The two qubits of a 2-qubit PTM must differ')
+        for q, din in zip(qubits, shape[n:]):
+            if self._data.shape[q] != din:
+                raise ValueError(
+                    'PTM acts on a {}-dimensional Pauli space, qubit {} has '
+                    'dim_pauli {}'.format(din, q, self._data.shape[q]))
+        if ptm_t is None:
+            max_terms = ops.nnz_terms(ptm, self._arith)
+            ptm_t = self._device_ptm(ptm)
+        else:
+            max_terms = math.prod(shape)
+        self._data = torch.ops.qsgb.apply_ptm(
+            self._data, ptm_t, list(qubits), self._arith, max_terms, False)
+
+    # ------------------------------------------------------------ diagonal
+    def _diagonal_device(self):
+        """FP64 device tensor of length prod(dim_hilbert)."""
+        plan = _diag_plan(self.bases)
+        if self.n_qubits == 0:
+            return self._data.reshape(1).to(torch.float64)
+        if plan is not None:
+            idx_off, idx = plan
+            return torch.ops.qsgb.gather(self._data, idx_off, idx, True)
+        # general bases: contract each qudit with its (real) computational
+        # basis vectors, d_hilbert x d_pauli, as a rectangular 1-qudit PTM
+        data = self._data if self._data.dtype == torch.float64 else \
+            self._data.to(torch.float64)
+        for q, b in enumerate(self.bases):
+            m = np.ascontiguousarray(
+                np.real(b.computational_basis_vectors), dtype=np.float64)
+            data = torch.ops.qsgb.apply_ptm(
+                data, self._device_ptm(m), [q], L.ARITH_DF64,
+                ops.nnz_terms(m, L.ARITH_DF64), False)
+        return data.reshape(-1)
+
+    def diagonal(self, *, get_data=True):
+        diag = self._diagonal_device()
+        if not get_data:
+            return diag
+        ops.check_device_status(self._device)
+        return diag.cpu().numpy()
+
+    def _trace_device(self):
+        diag = self._diagonal_device()
+        return torch.ops.qsgb.marginals(diag, [diag.numel()], -1)
+
+    def trace(self):
+        tr = self._trace_device()
+        ops.check_device_status(self._device)
+        return float(tr.item())
+
+    def meas_prob(self, qubit):
+        self._validate_qubit(qubit, 'qubit')
+        diag = self._diagonal_device()
+        probs = torch.ops.qsgb.marginals(diag, list(self.dim_hilbert), qubit)
+        ops.check_device_status(self._device)
+        return probs.cpu().numpy()
+
+    def partial_trace(self, *qubits):
+        for q in qubits:
+            self._validate_qubit(q, 'qubit')
+        keep = [1 if i in qubits else 0 for i in range(self.n_qubits)]
+        weights = []
+        for i, b in enumerate(self.bases):
+            if not keep[i]:
+                weights.extend(float(w) for w in
+                               np.real(np.einsum('xkk->x', b.vectors)))
+        data = torch.ops.qsgb.partial_trace(self._data, keep, weights)
+        return self.__class__([self.bases[q] for q in qubits], data,
+                              force=True, dtype=self.dtype,
+                              device=self._device, arith=self._arith_name())
+
+    def renormalize(self):
+        tr = self.trace()
+        if tr > 1e-8:
+            torch.ops.qsgb.scale_(self._data, 1.0 / tr)
+        else:
+            warnings.warn(
+                'Density matrix trace is 0; likely your further computation '
+                'will fail. Have you projected DM on a state with zero '
+                'weight?')
+        return tr
+
+    # ------------------------------------------------------------ new API
+    def reduce_basis(self, qubit, indices):
+        """Keep only the Pauli elements `indices` of `qubit`'s basis
+        (e.g. 9 -> 3 with the computational subbasis of a qutrit) and
+        switch its basis to ``bases[qubit].subbasis(indices)``.  Same result
+        as ``apply_ptm(np.eye(d)[indices], qubit)`` followed by the basis
+        update of quantumsim/operations/operation.py:549-551."""
+        self._validate_qubit(qubit, 'qubit')
+        indices = [int(i) for i in indices]
+        d = self._data.shape[qubit]
+        if not indices or any(i < 0 or i >= d for i in indices):
+            raise ValueError('basis indices must be within [0, {})'.format(d))
+        self._data = torch.ops.qsgb.take_axis(self._data, qubit, indices)
+        self.bases[qubit] = self.bases[qubit].subbasis(indices)
+
+    def project(self, qubit, state):
+        """Project `qubit` onto computational state `state` (its basis shrinks
+        to the single element |state><state|).  The trace afterwards is the
+        outcome's probability; call :meth:`renormalize` to normalise."""
+        self._validate_qubit(qubit, 'qubit')
+        idx = self.bases[qubit].computational_basis_indices.get(state)
+        if idx is None:
+            raise ValueError('state {} of qubit {} has no computational '
+                             'basis element in its basis'.format(state, qubit))
+        self.reduce_basis(qubit, [idx])
+
+
+def register(make_default=False):
+    """Expose the backend as ``quantumsim.pauli_vectors.PauliVectorGB300``
+    (and module ``quantumsim.pauli_vectors.gb300``) when quantumsim is
+    importable.  Returns True if registered."""
+    import sys
+    try:
+        with warnings.catch_warnings():
+            warnings.simplefilter('ignore')
+            import quantumsim.pauli_vectors as qpv
+    except Exception:
+        return False
+    qpv.PauliVectorGB300 = PauliVectorGB300
+    if 'PauliVectorGB300' not in qpv.__all__:
+        qpv.__all__.append('PauliVectorGB300')
+    sys.modules.setdefault('quantumsim.pauli_vectors.gb300',
+                           sys.modules[__name__])
+    if make_default:
+        qpv.Default = PauliVectorGB300
+    return True

@@ -1,0 +1,54 @@
+"""Shared pytest configuration: the `gpu` marker, golden fixtures, helpers."""
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, 'tests', 'golden', 'pauli_vector_golden.npz')
+
+# Agreement with float64 numpy required of the FP64 path (relative per
+# entry, with an absolute floor for entries that cancel to ~0) and on
+# probabilities (absolute).
+RTOL_F64 = 1e-12
+ATOL_F64 = 1e-14
+ATOL_PROB = 1e-12
+
+
+def pytest_configure(config):
+    config.addinivalue_line(
+        'markers', 'gpu: needs a CUDA device (GB300) and libqsgb.so')
+
+
+def has_cuda():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.fixture(scope='session')
+def golden():
+    data = np.load(GOLDEN, allow_pickle=False)
+    return data
+
+
+def golden_cases(data):
+    return json.loads(str(data['manifest']))
+
+
+def golden_bases(data, ids):
+    from quantumsim_gb300.bases import PauliBasis
+    return [PauliBasis(data['basis{}_vectors'.format(i)],
+                       list(data['basis{}_labels'.format(i)])) for i in ids]
+
+
+def assert_close_f64(actual, expected, rtol=RTOL_F64, atol=ATOL_F64):
+    np.testing.assert_allclose(np.asarray(actual), np.asarray(expected),
+                               rtol=rtol, atol=atol)

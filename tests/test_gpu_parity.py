@@ -1,0 +1,389 @@
+"""Parity of the GB300 backend (CUDA kernels through the C ABI) with the
+reference: golden fixtures from quantumsim's PauliVectorNumpy, the
+reference tests' known answers, and the oracle on seeded inputs at every
+target position and stride class.  FP64 agreement: 1e-12 relative per entry
+(1e-14 absolute floor), 1e-12 absolute on probabilities."""
+import itertools
+import math
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import (ATOL_PROB, assert_close_f64, golden_bases, golden_cases)
+from oracle import pauli_vector_np as O
+import quantumsim_gb300 as qg
+from quantumsim_gb300 import bases as B
+from quantumsim_gb300 import ptm as P
+from quantumsim_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+GB = qg.PauliVectorGB300
+
+
+def rand_pv(rng, shape):
+    return rng.standard_normal(shape) / math.sqrt(np.prod(shape))
+
+
+def rand_ptm(rng, shape, density=1.0):
+    p = rng.standard_normal(shape)
+    if density < 1:
+        p *= rng.random(shape) < density
+    return p
+
+
+# ---------------------------------------------------------------- golden
+def test_golden_cases_on_gpu(golden):
+    for i, case in enumerate(golden_cases(golden)):
+        bases = golden_bases(golden, case['bases'])
+        pv_in = golden['c{}_in'.format(i)]
+        s = GB(bases, pv_in.copy())
+        kind = case['kind']
+        if kind == 'apply':
+            s.apply_ptm(golden['c{}_ptm'.format(i)], *case['qubits'])
+            assert_close_f64(s.to_pv(), golden['c{}_out'.format(i)])
+        elif kind == 'reduce':
+            assert_close_f64(s.diagonal(), golden['c{}_diag'.format(i)])
+            assert s.trace() == pytest.approx(
+                float(golden['c{}_trace'.format(i)]), abs=ATOL_PROB)
+            for q in range(len(bases)):
+                np.testing.assert_allclose(
+                    s.meas_prob(q), golden['c{}_prob{}'.format(i, q)],
+                    rtol=0, atol=ATOL_PROB)
+            tr = s.renormalize()
+            assert tr == pytest.approx(
+                float(golden['c{}_renorm_trace'.format(i)]), abs=ATOL_PROB)
+            assert_close_f64(s.to_pv(), golden['c{}_renorm_pv'.format(i)])
+        elif kind == 'partial_trace':
+            pt = s.partial_trace(*case['keep'])
+            assert isinstance(pt, GB)
+            assert_close_f64(pt.to_pv(), golden['c{}_out'.format(i)])
+            assert pt.bases == [bases[q] for q in case['keep']]
+        elif kind == 'reduce_basis':
+            s.reduce_basis(case['qubit'], case['indices'])
+            np.testing.assert_array_equal(s.to_pv(),
+                                          golden['c{}_out'.format(i)])
+            assert s.bases[case['qubit']].dim_pauli == len(case['indices'])
+
+
+def test_circuit0_matches_reference(golden):
+    ops = workloads.config0_circuit(seed=0)
+    s = GB([B.general(2)] * 6)
+    workloads.run(s, ops)
+    assert_close_f64(s.to_pv(), golden['circuit0_pv'])
+    np.testing.assert_allclose(s.diagonal(), golden['circuit0_diag'],
+                               rtol=0, atol=ATOL_PROB)
+
+
+# ---------------------------------------------------------------- strides
+@pytest.mark.parametrize('arith,dtype,rtol,atol', [
+    ('df64', np.float64, 1e-12, 1e-14),
+    ('f64', np.float64, 1e-13, 1e-15),
+    ('f32', np.float32, 2e-5, 2e-6)])
+def test_1q_every_position(arith, dtype, rtol, atol):
+    rng = np.random.default_rng(11)
+    n = 8
+    bases = [B.general(2)] * n
+    for q in range(n):
+        pv = rand_pv(rng, (4,) * n)
+        ptm = rand_ptm(rng, (4, 4))
+        s = GB(bases, pv, dtype=dtype, arith=arith)
+        s.apply_ptm(ptm, q)
+        np.testing.assert_allclose(s.to_pv(), O.apply_ptm(pv, ptm, q),
+                                   rtol=rtol, atol=atol)
+
+
+@pytest.mark.parametrize('density', [1.0, 0.3])
+def test_2q_every_ordered_pair(density):
+    rng = np.random.default_rng(12)
+    n = 6
+    bases = [B.general(2)] * n
+    for q0, q1 in itertools.permutations(range(n), 2):
+        pv = rand_pv(rng, (4,) * n)
+        ptm = rand_ptm(rng, (4, 4, 4, 4), density)
+        s = GB(bases, pv)
+        s.apply_ptm(ptm, q0, q1)
+        assert_close_f64(s.to_pv(), O.apply_ptm(pv, ptm, q0, q1))
+
+
+def test_noisy_cz_on_pairs_native_and_df64():
+    rng = np.random.default_rng(13)
+    n = 7
+    t1, t2 = workloads.coherence_times(rng, n)
+    for q0, q1 in [(0, 6), (6, 0), (2, 3), (5, 1), (4, 6)]:
+        ptm = workloads.noisy_cz(rng, (q0, q1), t1, t2)
+        pv = rand_pv(rng, (4,) * n)
+        ref = O.apply_ptm(pv, ptm, q0, q1)
+        for arith in ('df64', 'f64'):
+            s = GB([B.general(2)] * n, pv, arith=arith)
+            s.apply_ptm(ptm, q0, q1)
+            assert_close_f64(s.to_pv(), ref)
+
+
+def test_rectangular_and_mixed_dims():
+    rng = np.random.default_rng(14)
+    shape = (9, 4, 3, 9, 1)
+    b = [B.general(3), B.general(2), B.general(3).subbasis([0, 1, 2]),
+         B.general(3), B.general(2).subbasis([0])]
+    for qs, pshape in [((0,), (3, 9)), ((2,), (9, 3)), ((4,), (4, 1)),
+                       ((0, 3), (9, 9, 9, 9)), ((3, 0), (3, 1, 9, 9)),
+                       ((1, 2), (1, 9, 4, 3)), ((4, 2), (4, 3, 1, 3)),
+                       ((3, 1), (9, 4, 9, 4))]:
+        pv = rand_pv(rng, shape)
+        ptm = rand_ptm(rng, pshape, 0.5)
+        s = GB(b, pv, force=True)
+        s.apply_ptm(ptm, *qs)
+        assert_close_f64(s.to_pv(), O.apply_ptm(pv, ptm, *qs))
+
+
+def test_two_qutrit_81x81_dense_and_cphase():
+    rng = np.random.default_rng(15)
+    bases = [B.general(3)] * 4
+    for ptm, qs in [(rand_ptm(rng, (9, 9, 9, 9)), (1, 3)),
+                    (P.qutrit_cphase(math.pi + 0.02, 0.005).numpy(), (2, 0)),
+                    (workloads.qutrit_1q(rng), (3,))]:
+        pv = rand_pv(rng, (9,) * 4)
+        s = GB(bases, pv)
+        s.apply_ptm(ptm, *qs)
+        assert_close_f64(s.to_pv(), O.apply_ptm(pv, ptm, *qs))
+
+
+def test_transposed_apply_and_ptm_grad_ops():
+    rng = np.random.default_rng(16)
+    dev = torch.device('cuda')
+    x = rand_pv(rng, (4, 3, 4, 9))
+    ptm = rand_ptm(rng, (2, 4, 4, 4))   # qudits (2, 0), rectangular
+    g = rand_pv(rng, O.apply_ptm(x, ptm, 2, 0).shape)
+    xt = torch.from_numpy(x).to(dev)
+    gt = torch.from_numpy(g).to(dev)
+    pt = torch.from_numpy(ptm)
+    adj = torch.ops.qsgb.apply_ptm(gt, pt, [2, 0], 1, ptm.size, True)
+    assert_close_f64(adj.cpu().numpy(), O.apply_ptm_transposed(g, ptm, 2, 0))
+    dptm = torch.ops.qsgb.ptm_grad(xt, gt, [2, 0])
+    np.testing.assert_allclose(dptm.cpu().numpy(), O.ptm_grad(x, g, 2, 0),
+                               rtol=1e-12, atol=1e-13)
+    p1 = rand_ptm(rng, (3, 3))
+    y1 = O.apply_ptm(x, p1, 1)
+    g1 = rand_pv(rng, y1.shape)
+    d1 = torch.ops.qsgb.ptm_grad(xt, torch.from_numpy(g1).to(dev), [1])
+    np.testing.assert_allclose(d1.cpu().numpy(), O.ptm_grad(x, g1, 1),
+                               rtol=1e-12, atol=1e-13)
+    for dtype, tol in ((torch.float32, 1e-5),):
+        d32 = torch.ops.qsgb.ptm_grad(xt.to(dtype), gt.to(dtype), [2, 0])
+        np.testing.assert_allclose(d32.cpu().numpy(), O.ptm_grad(x, g, 2, 0),
+                                   rtol=tol, atol=tol)
+
+
+# ---------------------------------------------------------------- KATs
+def test_kat_create_trivial():
+    s = GB([])
+    assert s.to_pv() == pytest.approx(1)
+    assert s.diagonal() == pytest.approx(1)
+    assert s.trace() == pytest.approx(1)
+
+
+@pytest.mark.parametrize('dims', [[2] * 9, [3, 2, 2]])
+def test_kat_create(dims):
+    target = [d * d for d in dims]
+    data = np.random.random_sample(target)
+    bases = [B.general(d) for d in dims]
+    for expansion in (None, data):
+        s = GB(bases, expansion)
+        assert s.n_qubits == len(dims)
+        assert s.dim_hilbert == tuple(dims)
+        assert s.dim_pauli == tuple(target)
+        assert s.size == math.prod(np.array(dims) ** 2)
+        if expansion is not None:
+            np.testing.assert_array_equal(s.to_pv(), expansion)
+    wrong = math.prod(dims)
+    with pytest.raises(ValueError):
+        GB(bases, data.reshape(wrong, wrong))
+    for shape in (target, (wrong, wrong)):
+        with pytest.raises(ValueError):
+            GB(bases=bases, pv=np.zeros(shape, dtype=complex))
+    with pytest.raises(ValueError):
+        GB(bases=[B.general(2)] * 16)
+
+
+@pytest.mark.parametrize('bases', [
+    (B.general(2),) * 3,
+    (B.general(2).subbasis([0, 1, 2]), B.general(2).subbasis([0, 1]),
+     B.general(2))])
+def test_kat_create_from_dm(bases):
+    dm = np.zeros((8, 8), dtype=complex)
+    dm[0, 0], dm[1, 1] = 0.25, 0.75
+    dm[0, 1], dm[1, 0] = 0.5 - 0.33j, 0.5 + 0.33j
+    s = GB.from_dm(dm, bases)
+    pv = s.to_pv()
+    assert pv[0, 0, 0] == 0.25 and pv[0, 0, 1] == 0.75
+    assert pv[0, 0, 2] == pytest.approx(0.5 * 2 ** 0.5)
+    assert pv[0, 0, 3] == pytest.approx(0.33 * 2 ** 0.5)
+    assert s.to_dm() == pytest.approx(dm)
+
+
+def _reshuffled():
+    g = B.general(2)
+    order = (0, 2, 1, 3)
+    return B.PauliBasis(np.array([g.vectors[i] for i in order]),
+                        [g.labels[i] for i in order])
+
+
+@pytest.mark.parametrize('bases', [
+    (B.general(2),) * 3, (_reshuffled(),) * 3,
+    (B.general(2), B.general(2).subbasis([0, 1]),
+     B.general(2).subbasis([0, 1, 2]))])
+def test_kat_diagonal_meas_prob(bases):
+    diag = np.array([0.25, 0, 0.75, 0, 0, 0, 0, 0])
+    s = GB.from_dm(np.diag(diag), bases)
+    assert np.allclose(s.diagonal(), diag)
+    assert s.trace() == pytest.approx(1)
+    assert np.allclose(s.meas_prob(0), (1, 0))
+    assert np.allclose(s.meas_prob(1), (0.25, 0.75))
+    diag = np.array([0.25, 0.5, 0, 0, 0, 0, 0, 0])
+    s = GB.from_dm(np.diag(diag), bases)
+    assert np.allclose(s.diagonal(), diag)
+    assert s.trace() == pytest.approx(0.75)
+    assert np.allclose(s.meas_prob(0), (0.75, 0.))
+    assert np.allclose(s.meas_prob(1), (0.75, 0.))
+    assert np.allclose(s.meas_prob(2), (0.25, 0.5))
+
+
+@pytest.mark.parametrize('dims', [(2, 2), (2, 3), (3, 3)])
+def test_kat_default_diagonal(dims):
+    s = GB([B.general(d) for d in dims])
+    ref = np.zeros(dims[0] * dims[1])
+    ref[0] = 1
+    assert s.diagonal() == pytest.approx(ref)
+
+
+def test_kat_apply_random_unitary_each_qubit():
+    from scipy.stats import unitary_group
+    rng = np.random.RandomState(45)
+    b = (B.general(2),)
+    for qubit in range(3):
+        u = unitary_group.rvs(2, random_state=rng)
+        a = rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8))
+        dm = a @ a.conj().T
+        dm /= np.trace(dm)
+        ops3 = [np.eye(2)] * 3
+        ops3[qubit] = u
+        full = ops3[0]
+        for m in ops3[1:]:
+            full = np.kron(full, m)
+        s0 = GB.from_dm(dm, b * 3)
+        s1 = GB.from_dm(full @ dm @ full.conj().T, b * 3)
+        s0.apply_ptm(P.kraus_to_ptm(u, b).numpy(), qubit)
+        assert_close_f64(s0.to_pv(), s1.to_pv(), rtol=1e-12, atol=1e-13)
+
+
+# ---------------------------------------------------------------- API
+def test_errors_match_reference():
+    s = GB([B.general(2)] * 3)
+    with pytest.raises(ValueError):
+        s.apply_ptm(np.eye(4), 0, 1)          # wrong PTM ndim
+    with pytest.raises(ValueError):
+        s.apply_ptm(np.eye(4), 3)             # qubit out of range
+    with pytest.raises(ValueError):
+        s.apply_ptm(np.eye(3), 0)             # dimension mismatch
+    with pytest.raises(NotImplementedError):
+        s.apply_ptm(np.ones((4,) * 6), 0, 1, 2)
+    with pytest.raises(ValueError):
+        s.meas_prob(5)
+    with pytest.raises(ValueError):
+        s.partial_trace(0, 7)
+
+
+def test_renormalize_zero_trace_warns_and_project():
+    s = GB([B.general(2)] * 2)
+    s.project(0, 1)                          # |0><0| projected on 1: trace 0
+    with pytest.warns(UserWarning):
+        assert s.renormalize() == pytest.approx(0)
+    s = GB([B.general(2)] * 2)
+    s.apply_ptm(P.rotate('x', 1.1).numpy(), 1)
+    p1 = s.meas_prob(1)[1]
+    s.project(1, 1)
+    assert s.dim_pauli == (4, 1)
+    assert s.renormalize() == pytest.approx(p1, abs=1e-12)
+    assert s.trace() == pytest.approx(1, abs=1e-12)
+
+
+def test_copy_is_deep():
+    s = GB([B.general(2)] * 2)
+    c = s.copy()
+    s.apply_ptm(P.rotate('y', 0.4).numpy(), 0)
+    assert c.to_pv()[0, 0] == 1 and not np.allclose(c.to_pv(), s.to_pv())
+
+
+def test_qutrit_circuit_with_measurement_matches_oracle():
+    ops = workloads.config2_circuit(seed=2, n_qutrits=4, n_layers=6)
+    s = GB([B.general(3)] * 4)
+    o = O.PauliVectorOracle([B.general(3)] * 4)
+    ts = workloads.run(s, ops)
+    to = workloads.run(o, ops)
+    assert ts == pytest.approx(to, abs=1e-12)
+    assert_close_f64(s.to_pv(), o.to_pv())
+    assert [b.dim_pauli for b in s.bases] == [b.dim_pauli for b in o.bases]
+
+
+def test_float32_storage_probabilities():
+    ops = workloads.config0_circuit(seed=4)
+    s = GB([B.general(2)] * 6, dtype=np.float32)
+    o = O.PauliVectorOracle([B.general(2)] * 6)
+    workloads.run(s, ops)
+    workloads.run(o, ops)
+    assert s.to_pv().dtype == np.float32
+    np.testing.assert_allclose(s.diagonal(), o.diagonal(), rtol=0, atol=1e-6)
+    assert s.trace() == pytest.approx(o.trace(), abs=1e-6)
+
+
+def test_device_status_reports_out_of_range_values():
+    s = GB([B.general(2)] * 2, np.full((4, 4), 1e300))
+    s.apply_ptm(np.full((4, 4), 0.5), 0)   # multi-term rows -> df64 path
+    with pytest.raises(RuntimeError, match='range'):
+        s.to_pv()
+    s2 = GB([B.general(2)] * 2)
+    s2.to_pv()                              # status was cleared
+
+
+# ---------------------------------------------------------------- full size
+def test_12_qubit_apply_matches_oracle():
+    rng = np.random.default_rng(17)
+    n = 12
+    pv = rand_pv(rng, (4,) * n)
+    s = GB([B.general(2)] * n, pv, force=True)
+    ref = pv
+    t1, t2 = workloads.coherence_times(rng, n)
+    for qs in [(0,), (11,), (5,), (0, 11), (11, 0), (6, 7), (3, 9)]:
+        ptm = (workloads.noisy_1q(rng, t1[qs[0]], t2[qs[0]]) if len(qs) == 1
+               else workloads.noisy_cz(rng, qs, t1, t2))
+        s.apply_ptm(ptm, *qs)
+        ref = O.apply_ptm(ref, ptm, *qs)
+    assert_close_f64(s.to_pv(), ref)
+
+
+def test_14_qubit_properties():
+    """At the full 14-qubit size: trace preservation of trace-preserving
+    PTMs, marginals summing to the trace, partial trace keeping the trace,
+    and linearity of apply_ptm."""
+    rng = np.random.default_rng(18)
+    n = 14
+    s = GB([B.general(2)] * n, force=True)
+    ops, keep = workloads.config1_circuit(seed=1, n_qubits=n, n_layers=2)
+    workloads.run(s, ops)
+    tr = s.trace()
+    assert tr == pytest.approx(1.0, abs=1e-12)
+    for q in (0, 7, 13):
+        assert s.meas_prob(q).sum() == pytest.approx(tr, abs=1e-12)
+    pt = s.partial_trace(*keep)
+    assert pt.trace() == pytest.approx(tr, abs=1e-12)
+    # linearity: P(a x) == a P(x) exactly for a power of two
+    x = s.copy()
+    x.apply_ptm(2.0 * np.eye(4), 3)
+    ptm = workloads.noisy_cz(rng, (2, 9), *workloads.coherence_times(rng, n))
+    x.apply_ptm(ptm, 2, 9)
+    s.apply_ptm(ptm, 2, 9)
+    a = x.data
+    b = s.data
+    assert torch.equal(a, 2 * b)
