@@ -262,6 +262,18 @@ def run_gb300(args):
         per_target['2q_dense_3_7'] = _time_app(s, dense, (3, 7), bytes_per_app)
         per_target['2q_dense_12_13'] = _time_app(s, dense, (12, 13),
                                                  bytes_per_app)
+        # the same launches with each arithmetic forced
+        cz = workloads.noisy_cz(rng, (3, 7), t1, t2)
+        r1 = workloads.noisy_1q(rng, t1[5], t2[5])
+        for arith in ('f64', 'df64', 'auto'):
+            s._arith_key, s._arith = arith, qops_arith(arith)
+            per_target['arith_{}_2q_cz_3_7'.format(arith)] = _time_app(
+                s, cz, (3, 7), bytes_per_app)
+            per_target['arith_{}_1q_q5'.format(arith)] = _time_app(
+                s, r1, (5,), bytes_per_app)
+            per_target['arith_{}_2q_dense_3_7'.format(arith)] = _time_app(
+                s, dense, (3, 7), bytes_per_app)
+        s._arith_key, s._arith = 'auto', qops_arith('auto')
 
     # ---- end to end through the public API (host PTMs, trace read back)
     e2e_steps = [workloads.config1_2q_batch(50000 + 1000 * rank + i,
@@ -325,6 +337,11 @@ def run_gb300(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def qops_arith(name):
+    from quantumsim_gb300.pauli_vector import _ARITH
+    return _ARITH[name]
 
 
 def _time_app(s, ptm, qs, bytes_per_app, reps=3):

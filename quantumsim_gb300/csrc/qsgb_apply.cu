@@ -1,5 +1,5 @@
 // PTM application kernels: one- and two-qudit Pauli transfer matrices on any
-// qudit positions, FP64 (df64 or native arithmetic) and FP32 storage.
+// qudit positions, FP64 or FP32 storage.
 //
 // Replaces quantumsim/pauli_vectors/primitives.cu:15-89 (two_qubit_general_ptm,
 // one thread per output element, PTM row re-read from global memory per
@@ -9,17 +9,25 @@
 //  * The state tensor is viewed as (X, Da, Y, Db, Z) with targets a < b; a
 //    one-qudit PTM is the case X = Da = 1.  A "group" is one bystander index
 //    (x, y, z); it owns Kin = Da_in*Db_in inputs and Kout outputs.
-//  * Each block compacts the PTM into a per-row term list in shared memory
-//    once (exact zeros and entries below 2^-60 of the largest one dropped),
-//    then loops grid-stride over groups.  Consecutive threads take
-//    consecutive z, so every one of the Kin loads and Kout stores of a warp
-//    is a contiguous run whenever Z >= 32.
+//  * Each block compacts the PTM into per-row term lists in shared memory
+//    once, then loops grid-stride over groups.  Consecutive threads take
+//    consecutive z; when Z is even a thread takes the pair (z, z+1), so every
+//    load and store is a 16-byte access and a warp covers contiguous runs.
 //  * Inputs are parked in a per-thread shared-memory column so that the term
-//    loop can index them at run time.
-//  * df64: rows with one term use a single FP64 multiply (exact, as numpy);
-//    rows with more terms accumulate in float-float on the FP32 pipes.
+//    loops can index them at run time.
+//  * FP64 storage, per-row arithmetic.  GB300 issues ~1.9 FP64 FMAs per SM
+//    clock, about 1.4 per streamed element at full HBM bandwidth, against
+//    ~58x that on the FP32 pipes.  A row is computed either with native FP64
+//    FMAs ("dp": exact IEEE products and sums) or in float-float on the FP32
+//    pipes ("df", 48-bit significand).  QSGB_ARITH_F64 makes every row dp;
+//    QSGB_ARITH_DF64 makes every row with >= 2 terms df; QSGB_ARITH_AUTO
+//    (default) picks, per PTM, the split of rows that minimises the larger of
+//    the DP-pipe, integer-pipe, FMA-pipe and HBM times (rows in ascending term
+//    count go to dp first).
+//  * Entries with |P| <= 2^-52 max|P| (the round-off residue of PTM
+//    construction) are skipped except in QSGB_ARITH_F64 mode, which skips
+//    exact zeros only.
 #include <algorithm>
-#include <cstdio>
 
 #include "qsgb_common.cuh"
 
@@ -30,6 +38,19 @@ namespace {
 constexpr int kMaxK = 256;        // Kin, Kout limit
 constexpr int kMaxEntries = 6561; // Kout*Kin limit (two qutrits)
 constexpr int kMaxInline = 256;   // host PTMs up to 16x16 travel in the launch
+constexpr int kBlock = 128;
+
+enum RowMode { kZero = 0, kDP = 1, kDF = 2, kF32 = 3 };
+
+struct __align__(16) Term {
+  double p;  // dp / f32 rows: the value; df rows: (hi, lo) floats
+  int k;
+  int pad;
+};
+
+struct __align__(16) RowInfo {
+  int beg, end, mode, pad;
+};
 
 struct ApplyParams {
   const void* in;
@@ -38,9 +59,10 @@ struct ApplyParams {
   int kin, kout;
   int da_in, db_in, da_out, db_out;
   int flags;
+  int arith;
   int max_terms;
-  uint64_t n_groups;
-  FastDiv div_z, div_y;
+  uint64_t n_items;   // groups, or group pairs when PAIR
+  FastDiv div_z, div_y;  // Z (or Z/2 when PAIR), Y
   int64_t sxi, syi, sai, sbi;  // input strides (z stride 1)
   int64_t sxo, syo, sao, sbo;  // output strides
   unsigned* status;
@@ -64,66 +86,134 @@ __device__ __forceinline__ int ptm_index(const ApplyParams& p, int r, int k) {
 }
 
 struct SmemLayout {
-  // region 0: max(PTM staging, per-thread input columns)
-  size_t xs_off, xs_bytes;
-  size_t terms_off;   // float2[max_terms]
-  size_t tk_off;      // uint16[max_terms]
-  size_t rowptr_off;  // int[kout + 1]
-  size_t rowone_off;  // double[kout]
-  size_t offin_off;   // int64[kin]
-  size_t offout_off;  // int64[kout]
-  size_t red_off;     // double[32] reduction scratch + int flag
+  size_t xs_off, xs_bytes;  // region 0: max(PTM staging, input columns)
+  size_t terms_off;         // Term[max_terms]
+  size_t rows_off;          // RowInfo[kout]
+  size_t offin_off;         // int64[kin]
+  size_t offout_off;        // int64[kout]
+  size_t cnt_off;           // int[kout] term counts
+  size_t red_off;           // double[34] reduction scratch + flag
   size_t total;
 };
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-SmemLayout make_layout(int kin, int kout, int max_terms, int block, size_t elem) {
+SmemLayout make_layout(int kin, int kout, int max_terms, int block, size_t item_bytes) {
   SmemLayout L;
-  size_t xs = (size_t)kin * block * elem;
-  size_t stage = (size_t)kin * kout * sizeof(double);
+  const size_t xs = (size_t)kin * block * item_bytes;
+  const size_t stage = (size_t)kin * kout * sizeof(double);
   L.xs_off = 0;
   L.xs_bytes = std::max(xs, stage);
   size_t o = align_up(L.xs_bytes, 16);
   L.terms_off = o;
-  o = align_up(o + (size_t)max_terms * sizeof(float2), 16);
-  L.tk_off = o;
-  o = align_up(o + (size_t)max_terms * sizeof(uint16_t), 16);
-  L.rowptr_off = o;
-  o = align_up(o + (size_t)(kout + 1) * sizeof(int), 16);
-  L.rowone_off = o;
-  o = align_up(o + (size_t)kout * sizeof(double), 16);
+  o = align_up(o + (size_t)max_terms * sizeof(Term), 16);
+  L.rows_off = o;
+  o = align_up(o + (size_t)kout * sizeof(RowInfo), 16);
   L.offin_off = o;
   o = align_up(o + (size_t)kin * sizeof(int64_t), 16);
   L.offout_off = o;
   o = align_up(o + (size_t)kout * sizeof(int64_t), 16);
+  L.cnt_off = o;
+  o = align_up(o + (size_t)kout * sizeof(int), 16);
   L.red_off = o;
   o = align_up(o + 34 * sizeof(double), 16);
   L.total = o;
   return L;
 }
 
-// ARITH: QSGB_ARITH_DF64 / QSGB_ARITH_F64 (T = double) or QSGB_ARITH_F32 (T = float)
-template <typename T, int ARITH>
-__global__ void apply_ptm_kernel(const __grid_constant__ ApplyParams p, const SmemLayout L) {
+// Cost model (SM clock cycles per group) of a row split, used by
+// QSGB_ARITH_AUTO.  Rates per SM per clock on GB300: FP64 ~1.9 ops, the
+// integer pipe 64 lanes, the FP32 FMA pipe 128 lanes, issue 128 lanes, HBM
+// ~23 bytes.  A dp row of n terms costs n FP64 ops and ~2n+4 issue slots; a
+// df row costs 12n FMA-pipe and 12n+25 integer ops (splits, rounding) and
+// ~24n+30 issue slots.
+struct SplitCost {
+  float dp, alu, fma, issue, hbm;
+  __device__ float time() const {
+    float t = hbm;
+    t = fmaxf(t, dp / 1.9f);
+    t = fmaxf(t, alu / 64.f);
+    t = fmaxf(t, fma / 128.f);
+    t = fmaxf(t, issue / 128.f);
+    return t;
+  }
+  __device__ void add_dp(int n, float sgn) {
+    dp += sgn * n;
+    issue += sgn * (2.f * n + 4.f);
+  }
+  __device__ void add_df(int n, float sgn) {
+    fma += sgn * 12.f * n;
+    alu += sgn * (12.f * n + 25.f);
+    issue += sgn * (24.f * n + 30.f);
+  }
+};
+
+template <typename T, bool PAIR>
+struct Vec;
+template <>
+struct Vec<double, false> {
+  using type = double;
+};
+template <>
+struct Vec<double, true> {
+  using type = double2;
+};
+template <>
+struct Vec<float, false> {
+  using type = float;
+};
+template <>
+struct Vec<float, true> {
+  using type = float2;
+};
+
+__device__ __forceinline__ double lane(const double v, int) { return v; }
+__device__ __forceinline__ double lane(const double2 v, int i) { return i ? v.y : v.x; }
+__device__ __forceinline__ float lane(const float v, int) { return v; }
+__device__ __forceinline__ float lane(const float2 v, int i) { return i ? v.y : v.x; }
+
+template <typename V>
+__device__ __forceinline__ V make_vec(double a, double b);
+template <>
+__device__ __forceinline__ double make_vec<double>(double a, double) {
+  return a;
+}
+template <>
+__device__ __forceinline__ double2 make_vec<double2>(double a, double b) {
+  return make_double2(a, b);
+}
+template <>
+__device__ __forceinline__ float make_vec<float>(double a, double) {
+  return (float)a;
+}
+template <>
+__device__ __forceinline__ float2 make_vec<float2>(double a, double b) {
+  return make_float2((float)a, (float)b);
+}
+
+// PAIR: each item is two adjacent groups (z, z+1); requires Z even.
+template <typename T, bool PAIR>
+__global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant__ ApplyParams p,
+                                                           const SmemLayout L) {
+  using V = typename Vec<T, PAIR>::type;
+  constexpr int NL = PAIR ? 2 : 1;
   extern __shared__ __align__(16) unsigned char smem[];
   double* stage = reinterpret_cast<double*>(smem + L.xs_off);
-  T* xs = reinterpret_cast<T*>(smem + L.xs_off);
-  float2* terms = reinterpret_cast<float2*>(smem + L.terms_off);
-  uint16_t* tk = reinterpret_cast<uint16_t*>(smem + L.tk_off);
-  int* rowptr = reinterpret_cast<int*>(smem + L.rowptr_off);
-  double* rowone = reinterpret_cast<double*>(smem + L.rowone_off);
+  V* xs = reinterpret_cast<V*>(smem + L.xs_off);
+  Term* terms = reinterpret_cast<Term*>(smem + L.terms_off);
+  RowInfo* rows = reinterpret_cast<RowInfo*>(smem + L.rows_off);
   int64_t* offin = reinterpret_cast<int64_t*>(smem + L.offin_off);
   int64_t* offout = reinterpret_cast<int64_t*>(smem + L.offout_off);
+  int* cnt = reinterpret_cast<int*>(smem + L.cnt_off);
   double* red = reinterpret_cast<double*>(smem + L.red_off);
-  int* overflow = reinterpret_cast<int*>(red + 33);
+  int* flag = reinterpret_cast<int*>(red + 33);
 
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
   const int ne = p.kin * p.kout;
   const double* __restrict__ src = p.ptm ? p.ptm : p.ptm_inline;
 
-  // ---- 1. stage the op matrix M[r][k] and find max |M| ----
+  // ---- 1. stage the op matrix M[r][k], max |M|, offsets ----
   double amax = 0.0;
   for (int i = tid; i < ne; i += nthr) {
     const int r = i / p.kin, k = i - r * p.kin;
@@ -133,7 +223,6 @@ __global__ void apply_ptm_kernel(const __grid_constant__ ApplyParams p, const Sm
   }
   for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
   if ((tid & 31) == 0) red[tid >> 5] = amax;
-  if (tid == 0) *overflow = 0;
   for (int k = tid; k < p.kin; k += nthr) {
     const int ka = k / p.db_in, kb = k - ka * p.db_in;
     offin[k] = ka * p.sai + kb * p.sbi;
@@ -149,102 +238,209 @@ __global__ void apply_ptm_kernel(const __grid_constant__ ApplyParams p, const Sm
     red[32] = m;
   }
   __syncthreads();
-  // drop threshold: exact zeros for native FP64, else far below precision
-  const double thr = (ARITH == QSGB_ARITH_F64) ? 0.0 : red[32] * ((ARITH == QSGB_ARITH_F32) ? 0x1p-40 : 0x1p-60);
+  const double thr = (p.arith == QSGB_ARITH_F64) ? 0.0 : red[32] * ((p.arith == QSGB_ARITH_F32) ? 0x1p-30 : 0x1p-52);
 
-  // ---- 2. per-row term counts and prefix sum ----
+  // ---- 2. term counts, row modes, prefix sums ----
   for (int r = tid; r < p.kout; r += nthr) {
     int c = 0;
     for (int k = 0; k < p.kin; ++k) c += fabs(stage[r * p.kin + k]) > thr;
-    rowptr[r + 1] = c;
+    cnt[r] = c;
   }
   __syncthreads();
   if (tid == 0) {
-    rowptr[0] = 0;
-    for (int r = 0; r < p.kout; ++r) rowptr[r + 1] += rowptr[r];
-    if (rowptr[p.kout] > p.max_terms) *overflow = 1;
+    // modes
+    int n_dp_best = p.kout;
+    if (p.arith == QSGB_ARITH_AUTO) {
+      int sorted[kMaxK];
+      for (int r = 0; r < p.kout; ++r) {
+        int v = cnt[r], j = r;
+        while (j > 0 && sorted[j - 1] > v) {
+          sorted[j] = sorted[j - 1];
+          --j;
+        }
+        sorted[j] = v;
+      }
+      // n_dp = number of rows (ascending count) computed in FP64; rows with
+      // one term are always dp.  Evaluate every n_dp incrementally.
+      SplitCost sc{0.f, 0.f, 0.f, 5.f * (p.kin + p.kout), (float)(p.kin + p.kout) * (float)sizeof(T) / 23.f};
+      for (int i = 0; i < p.kout; ++i) {
+        if (sorted[i] == 1) sc.add_dp(1, 1.f);
+        else if (sorted[i] > 1) sc.add_df(sorted[i], 1.f);
+      }
+      float best = sc.time();
+      n_dp_best = 0;
+      for (int i = 0; i < p.kout; ++i) {
+        if (sorted[i] > 1) {
+          sc.add_df(sorted[i], -1.f);
+          sc.add_dp(sorted[i], 1.f);
+        }
+        const float c = sc.time();
+        if (c < best * 0.999f) {
+          best = c;
+          n_dp_best = i + 1;
+        }
+      }
+      // rows with the n_dp_best smallest counts are dp: threshold on counts
+      // (ties broken by row index)
+      int cut = n_dp_best > 0 ? sorted[n_dp_best - 1] : -1;
+      int ties = 0;
+      for (int i = 0; i < n_dp_best; ++i) ties += sorted[i] == cut;
+      int t = 0;
+      for (int r = 0; r < p.kout; ++r) {
+        const int c = cnt[r];
+        int mode;
+        if (c == 0)
+          mode = kZero;
+        else if (c == 1 || c < cut)
+          mode = kDP;
+        else if (c == cut && ties > 0) {
+          mode = kDP;
+          --ties;
+        } else
+          mode = kDF;
+        rows[r].beg = t;
+        rows[r].end = t + c;
+        rows[r].mode = mode;
+        t += c;
+      }
+      if (t > p.max_terms) *flag = 1; else *flag = 0;
+    } else {
+      int t = 0;
+      for (int r = 0; r < p.kout; ++r) {
+        const int c = cnt[r];
+        int mode;
+        if (c == 0)
+          mode = kZero;
+        else if (p.arith == QSGB_ARITH_F32)
+          mode = kF32;
+        else if (p.arith == QSGB_ARITH_F64 || c == 1)
+          mode = kDP;
+        else
+          mode = kDF;
+        rows[r].beg = t;
+        rows[r].end = t + c;
+        rows[r].mode = mode;
+        t += c;
+      }
+      *flag = (t > p.max_terms) ? 1 : 0;
+    }
   }
   __syncthreads();
-  if (*overflow) {
+  if (*flag) {
     if (tid == 0 && p.status) atomicOr(p.status, QSGB_DEV_BADITEM);
     return;
   }
   for (int r = tid; r < p.kout; r += nthr) {
-    int t = rowptr[r];
-    double one = 0.0;
+    const RowInfo ri = rows[r];
+    int t = ri.beg;
     for (int k = 0; k < p.kin; ++k) {
       const double v = stage[r * p.kin + k];
       if (fabs(v) > thr) {
-        if (ARITH == QSGB_ARITH_F64) {
-          terms[t] = make_float2(__int_as_float(__double2loint(v)), __int_as_float(__double2hiint(v)));
+        Term tm;
+        if (ri.mode == kDF) {
+          const float h = __double2float_rn(v);
+          const float l = __double2float_rn(v - (double)h);
+          tm.p = __hiloint2double(__float_as_int(h), __float_as_int(l));  // (hi, lo) words
+        } else if (ri.mode == kF32) {
+          tm.p = __hiloint2double(0, __float_as_int(__double2float_rn(v)));
         } else {
-          const float h = (float)v;
-          const float l = (float)(v - (double)h);
-          terms[t] = make_float2(h, l);
+          tm.p = v;
         }
-        tk[t] = (uint16_t)k;
-        one = v;
-        ++t;
+        tm.k = k;
+        tm.pad = 0;
+        terms[t++] = tm;
       }
     }
-    rowone[r] = one;
   }
   __syncthreads();  // stage[] is reused as xs[] below
 
   // ---- 3. stream the groups ----
-  const T* __restrict__ in = static_cast<const T*>(p.in);
-  T* __restrict__ out = static_cast<T*>(p.out);
+  const V* __restrict__ in = static_cast<const V*>(p.in);
+  V* __restrict__ out = static_cast<V*>(p.out);
   unsigned bad = 0;
   const uint64_t stride = (uint64_t)gridDim.x * nthr;
-  for (uint64_t g = (uint64_t)blockIdx.x * nthr + tid; g < p.n_groups; g += stride) {
-    const uint64_t t1 = fdiv(g, p.div_z);
-    const uint64_t z = g - t1 * p.div_z.d;
+  for (uint64_t it = (uint64_t)blockIdx.x * nthr + tid; it < p.n_items; it += stride) {
+    const uint64_t t1 = fdiv(it, p.div_z);
+    const uint64_t zi = it - t1 * p.div_z.d;
     const uint64_t x = fdiv(t1, p.div_y);
     const uint64_t y = t1 - x * p.div_y.d;
-    const int64_t bi = (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
-    const int64_t bo = (int64_t)x * p.sxo + (int64_t)y * p.syo + (int64_t)z;
-    for (int k = 0; k < p.kin; ++k) xs[k * nthr + tid] = in[bi + offin[k]];
+    // element offsets; with PAIR all strides are even, divide by 2 for V
+    const int64_t bi = ((int64_t)x * p.sxi + (int64_t)y * p.syi) / NL + (int64_t)zi;
+    const int64_t bo = ((int64_t)x * p.sxo + (int64_t)y * p.syo) / NL + (int64_t)zi;
+    for (int k = 0; k < p.kin; ++k) xs[k * nthr + tid] = in[bi + offin[k] / NL];
     for (int r = 0; r < p.kout; ++r) {
-      const int beg = rowptr[r], end = rowptr[r + 1];
-      T yv;
-      if (ARITH == QSGB_ARITH_F32) {
-        float acc = 0.f;
-        for (int t = beg; t < end; ++t) acc = fmaf(terms[t].x, (float)xs[tk[t] * nthr + tid], acc);
-        yv = (T)acc;
-      } else if (ARITH == QSGB_ARITH_F64) {
-        double acc = 0.0;
-        for (int t = beg; t < end; ++t) {
-          const double pv = __hiloint2double(__float_as_int(terms[t].y), __float_as_int(terms[t].x));
-          acc = fma(pv, (double)xs[tk[t] * nthr + tid], acc);
+      const RowInfo ri = rows[r];
+      if constexpr (sizeof(T) == 4) {  // FP32 storage and arithmetic
+        float facc[NL];
+#pragma unroll
+        for (int l = 0; l < NL; ++l) facc[l] = 0.f;
+        for (int t = ri.beg; t < ri.end; ++t) {
+          const Term tm = terms[t];
+          const float pf = __int_as_float(__double2loint(tm.p));
+          const V xv = xs[tm.k * nthr + tid];
+#pragma unroll
+          for (int l = 0; l < NL; ++l) facc[l] = fmaf(pf, lane(xv, l), facc[l]);
         }
-        yv = (T)acc;
-      } else {  // DF64
-        if (end - beg == 0) {
-          yv = (T)0;
-        } else if (end - beg == 1) {
-          yv = (T)(rowone[r] * (double)xs[tk[beg] * nthr + tid]);
+        V o;
+        if constexpr (PAIR) {
+          o = make_float2(facc[0], facc[NL - 1]);
         } else {
-          float xh, xl, s, c;
-          split_f64((double)xs[tk[beg] * nthr + tid], xh, xl, bad);
-          df_mul(s, c, terms[beg].x, terms[beg].y, xh, xl);
-          for (int t = beg + 1; t < end; ++t) {
-            split_f64((double)xs[tk[t] * nthr + tid], xh, xl, bad);
-            df_fma(s, c, terms[t].x, terms[t].y, xh, xl);
-          }
-          yv = (T)df_to_double(s, c);
+          o = facc[0];
         }
+        out[bo + offout[r] / NL] = o;
+        continue;
       }
-      out[bo + offout[r]] = yv;
+      double acc[NL];
+#pragma unroll
+      for (int l = 0; l < NL; ++l) acc[l] = 0.0;
+      if (ri.mode == kDP) {
+        for (int t = ri.beg; t < ri.end; ++t) {
+          const Term tm = terms[t];
+          const V xv = xs[tm.k * nthr + tid];
+#pragma unroll
+          for (int l = 0; l < NL; ++l) acc[l] = fma(tm.p, (double)lane(xv, l), acc[l]);
+        }
+      } else if (ri.mode == kDF) {
+        float s[NL], c[NL];
+        {
+          const Term tm = terms[ri.beg];
+          const float ph = __int_as_float(__double2hiint(tm.p));
+          const float pl = __int_as_float(__double2loint(tm.p));
+          const V xv = xs[tm.k * nthr + tid];
+#pragma unroll
+          for (int l = 0; l < NL; ++l) {
+            float xh, xl;
+            split_f64((double)lane(xv, l), xh, xl, bad);
+            df_mul(s[l], c[l], ph, pl, xh, xl);
+          }
+        }
+        for (int t = ri.beg + 1; t < ri.end; ++t) {
+          const Term tm = terms[t];
+          const float ph = __int_as_float(__double2hiint(tm.p));
+          const float pl = __int_as_float(__double2loint(tm.p));
+          const V xv = xs[tm.k * nthr + tid];
+#pragma unroll
+          for (int l = 0; l < NL; ++l) {
+            float xh, xl;
+            split_f64((double)lane(xv, l), xh, xl, bad);
+            df_fma(s[l], c[l], ph, pl, xh, xl);
+          }
+        }
+#pragma unroll
+        for (int l = 0; l < NL; ++l) acc[l] = df_to_double(s[l], c[l]);
+      }
+      out[bo + offout[r] / NL] = make_vec<V>(acc[0], acc[NL - 1]);
     }
   }
   if (bad && p.status) atomicOr(p.status, QSGB_DEV_RANGE);
 }
 
-template <typename T, int ARITH>
+template <typename T, bool PAIR>
 int launch_apply(const ApplyParams& p, cudaStream_t stream) {
-  const int block = (p.kin <= 16) ? 128 : (p.kin <= 81 ? 64 : 32);
-  SmemLayout L = make_layout(p.kin, p.kout, p.max_terms, block, sizeof(T));
-  auto kern = apply_ptm_kernel<T, ARITH>;
+  using V = typename Vec<T, PAIR>::type;
+  const int block = kBlock;
+  SmemLayout L = make_layout(p.kin, p.kout, p.max_terms, block, sizeof(V));
+  auto kern = apply_ptm_kernel<T, PAIR>;
   if (L.total > 48 * 1024) {
     if (L.total > 227 * 1024) return QSGB_ERR_UNSUPPORTED;
     QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
@@ -252,7 +448,7 @@ int launch_apply(const ApplyParams& p, cudaStream_t stream) {
   int occ = 0;
   QSGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, L.total));
   if (occ < 1) return QSGB_ERR_UNSUPPORTED;
-  const uint64_t need = (p.n_groups + block - 1) / block;
+  const uint64_t need = (p.n_items + block - 1) / block;
   const uint64_t cap = (uint64_t)sm_count() * occ;
   const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(need, cap));
   kern<<<grid, block, L.total, stream>>>(p, L);
@@ -271,10 +467,10 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   if (kin > kMaxK || kout > kMaxK || kin * kout > kMaxEntries) return QSGB_ERR_UNSUPPORTED;
   if (max_terms < 1 || max_terms > kin * kout) max_terms = kin * kout;
   if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
-  if (arith == QSGB_ARITH_AUTO) arith = (dtype == QSGB_F64) ? QSGB_ARITH_DF64 : QSGB_ARITH_F32;
+  if (arith < QSGB_ARITH_AUTO || arith > QSGB_ARITH_F32) return QSGB_ERR_INVALID;
+  if (dtype == QSGB_F32 && arith == QSGB_ARITH_AUTO) arith = QSGB_ARITH_F32;
   if (dtype == QSGB_F32 && arith != QSGB_ARITH_F32) return QSGB_ERR_INVALID;
   if (dtype == QSGB_F64 && arith == QSGB_ARITH_F32) return QSGB_ERR_INVALID;
-  if (arith < QSGB_ARITH_DF64 || arith > QSGB_ARITH_F32) return QSGB_ERR_INVALID;
 
   ApplyParams p;
   p.in = in;
@@ -292,10 +488,8 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.da_out = (int)da_out;
   p.db_out = (int)db_out;
   p.flags = flags & 3;
+  p.arith = arith;
   p.max_terms = (int)max_terms;
-  p.n_groups = (uint64_t)X * Y * Z;
-  p.div_z = make_fastdiv((uint64_t)Z);
-  p.div_y = make_fastdiv((uint64_t)Y);
   p.sbi = Z;
   p.syi = db_in * Z;
   p.sai = Y * db_in * Z;
@@ -305,10 +499,14 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.sao = Y * db_out * Z;
   p.sxo = da_out * Y * db_out * Z;
   p.status = status;
+  const size_t esz = dtype == QSGB_F64 ? 8 : 4;
+  const bool pair = (Z % 2 == 0) && ((uintptr_t)in % (2 * esz) == 0) && ((uintptr_t)out % (2 * esz) == 0);
+  p.div_y = make_fastdiv((uint64_t)Y);
+  p.div_z = make_fastdiv((uint64_t)(pair ? Z / 2 : Z));
+  p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
-  if (dtype == QSGB_F32) return launch_apply<float, QSGB_ARITH_F32>(p, s);
-  if (arith == QSGB_ARITH_F64) return launch_apply<double, QSGB_ARITH_F64>(p, s);
-  return launch_apply<double, QSGB_ARITH_DF64>(p, s);
+  if (dtype == QSGB_F32) return pair ? launch_apply<float, true>(p, s) : launch_apply<float, false>(p, s);
+  return pair ? launch_apply<double, true>(p, s) : launch_apply<double, false>(p, s);
 }
 
 }  // namespace

@@ -357,15 +357,15 @@ def scale_by_inverse_(pv: torch.Tensor, denom: torch.Tensor,
 
 def nnz_terms(ptm, arith):
     """Number of PTM entries the kernel keeps (same rule as the device):
-    exact zeros for native FP64, else |p| > 2^-60 max|P| (df64) or
-    2^-40 max|P| (FP32)."""
+    exact zeros are dropped for native FP64, otherwise entries with
+    |p| <= 2^-52 max|P| (FP64 storage) or 2^-30 max|P| (FP32)."""
     a = np.abs(np.asarray(ptm, dtype=np.float64))
     if a.size == 0:
         return 1
     if arith == L.ARITH_F64:
         thr = 0.0
     elif arith == L.ARITH_F32:
-        thr = a.max() * 2.0 ** -40
+        thr = a.max() * 2.0 ** -30
     else:
-        thr = a.max() * 2.0 ** -60
+        thr = a.max() * 2.0 ** -52
     return max(1, int(np.count_nonzero(a > thr)))

@@ -20,8 +20,11 @@ Numerical semantics follow ``PauliVectorNumpy`` (the reference oracle):
 * ``renormalize`` warns when the trace is <= 1e-8 and returns the trace
   before scaling (numpy.py:109-117).
 
-FP64 storage computes PTM products in float-float arithmetic (48-bit
-significand) on the FP32 pipes; ``arith='f64'`` selects native FP64 FMAs.
+FP64 storage: by default (``arith='auto'``) the kernel computes each PTM
+row either with native FP64 FMAs or in float-float arithmetic (48-bit
+significand) on the FP32 pipes, whichever keeps the launch closest to the
+HBM bound; ``arith='f64'`` forces native FP64 everywhere and
+``arith='df64'`` float-float for every row with more than one term.
 ``dtype=np.float32`` stores the vector in FP32 while every trace, marginal
 and partial-trace sum still accumulates in FP64.
 """
@@ -140,10 +143,10 @@ class PauliVectorGB300(_Base):
                 arith in ('df64', 'f64') and tdtype != torch.float64:
             raise ValueError('arith {!r} does not match storage {}'.format(
                 arith, tdtype))
+        if arith == 'auto' and tdtype == torch.float32:
+            arith = 'f32'
+        self._arith_key = arith
         self._arith = _ARITH[arith]
-        if self._arith == L.ARITH_AUTO:
-            self._arith = L.ARITH_DF64 if tdtype == torch.float64 else \
-                L.ARITH_F32
 
         if pv is None:
             data = torch.zeros(self.dim_pauli, dtype=tdtype,
@@ -199,10 +202,7 @@ class PauliVectorGB300(_Base):
                               arith=self._arith_name())
 
     def _arith_name(self):
-        for k, v in _ARITH.items():
-            if v == self._arith and k != 'auto':
-                return k
-        return 'auto'
+        return self._arith_key
 
     # ------------------------------------------------------------ apply_ptm
     def _device_ptm(self, ptm):

@@ -49,6 +49,17 @@ def golden_bases(data, ids):
                        list(data['basis{}_labels'.format(i)])) for i in ids]
 
 
+def assert_close_dot(actual, expected, absref, rtol=RTOL_F64):
+    """Per-entry forward-error check of a contraction: |a - e| <= rtol *
+    (sum_k |P_rk| |x_k|), the natural scale of a dot product whose terms may
+    cancel (`absref` = the same contraction applied to |P| and |x|)."""
+    actual, expected = np.asarray(actual), np.asarray(expected)
+    bound = rtol * np.asarray(absref) + 1e-300
+    err = np.abs(actual - expected)
+    worst = np.max(err / bound) if err.size else 0.0
+    assert worst <= 1.0, 'max error / bound = {:.3g}'.format(worst)
+
+
 def assert_close_f64(actual, expected, rtol=RTOL_F64, atol=ATOL_F64):
     np.testing.assert_allclose(np.asarray(actual), np.asarray(expected),
                                rtol=rtol, atol=atol)

@@ -127,9 +127,10 @@ def test_apply_geometry_transposed_and_mismatch():
 
 
 def test_nnz_terms_rule():
-    p = np.array([[1.0, 0.0, 1e-20, 0.5], [0, 0, 0, 0]])
-    assert ops.nnz_terms(p, L.ARITH_F64) == 3
+    p = np.array([[1.0, 0.0, 1e-20, 0.5], [0, 0, 1e-16, 0]])
+    assert ops.nnz_terms(p, L.ARITH_F64) == 4
     assert ops.nnz_terms(p, L.ARITH_DF64) == 2
+    assert ops.nnz_terms(p, L.ARITH_AUTO) == 2
     assert ops.nnz_terms(np.zeros((2, 2)), L.ARITH_DF64) == 1
 
 

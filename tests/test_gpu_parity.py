@@ -11,7 +11,8 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import (ATOL_PROB, assert_close_f64, golden_bases, golden_cases)
+from conftest import (ATOL_PROB, assert_close_dot, assert_close_f64,
+                      golden_bases, golden_cases)
 from oracle import pauli_vector_np as O
 import quantumsim_gb300 as qg
 from quantumsim_gb300 import bases as B
@@ -79,6 +80,7 @@ def test_circuit0_matches_reference(golden):
 
 # ---------------------------------------------------------------- strides
 @pytest.mark.parametrize('arith,dtype,rtol,atol', [
+    ('auto', np.float64, 1e-12, 1e-14),
     ('df64', np.float64, 1e-12, 1e-14),
     ('f64', np.float64, 1e-13, 1e-15),
     ('f32', np.float32, 2e-5, 2e-6)])
@@ -105,7 +107,8 @@ def test_2q_every_ordered_pair(density):
         ptm = rand_ptm(rng, (4, 4, 4, 4), density)
         s = GB(bases, pv)
         s.apply_ptm(ptm, q0, q1)
-        assert_close_f64(s.to_pv(), O.apply_ptm(pv, ptm, q0, q1))
+        assert_close_dot(s.to_pv(), O.apply_ptm(pv, ptm, q0, q1),
+                         O.apply_ptm(np.abs(pv), np.abs(ptm), q0, q1))
 
 
 def test_noisy_cz_on_pairs_native_and_df64():
@@ -116,7 +119,7 @@ def test_noisy_cz_on_pairs_native_and_df64():
         ptm = workloads.noisy_cz(rng, (q0, q1), t1, t2)
         pv = rand_pv(rng, (4,) * n)
         ref = O.apply_ptm(pv, ptm, q0, q1)
-        for arith in ('df64', 'f64'):
+        for arith in ('auto', 'df64', 'f64'):
             s = GB([B.general(2)] * n, pv, arith=arith)
             s.apply_ptm(ptm, q0, q1)
             assert_close_f64(s.to_pv(), ref)
@@ -135,7 +138,8 @@ def test_rectangular_and_mixed_dims():
         ptm = rand_ptm(rng, pshape, 0.5)
         s = GB(b, pv, force=True)
         s.apply_ptm(ptm, *qs)
-        assert_close_f64(s.to_pv(), O.apply_ptm(pv, ptm, *qs))
+        assert_close_dot(s.to_pv(), O.apply_ptm(pv, ptm, *qs),
+                         O.apply_ptm(np.abs(pv), np.abs(ptm), *qs))
 
 
 def test_two_qutrit_81x81_dense_and_cphase():
@@ -147,7 +151,8 @@ def test_two_qutrit_81x81_dense_and_cphase():
         pv = rand_pv(rng, (9,) * 4)
         s = GB(bases, pv)
         s.apply_ptm(ptm, *qs)
-        assert_close_f64(s.to_pv(), O.apply_ptm(pv, ptm, *qs))
+        assert_close_dot(s.to_pv(), O.apply_ptm(pv, ptm, *qs),
+                         O.apply_ptm(np.abs(pv), np.abs(ptm), *qs))
 
 
 def test_transposed_apply_and_ptm_grad_ops():
