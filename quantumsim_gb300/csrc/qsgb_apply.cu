@@ -86,7 +86,7 @@ __device__ __forceinline__ int ptm_index(const ApplyParams& p, int r, int k) {
 }
 
 struct SmemLayout {
-  size_t xs_off, xs_bytes;  // region 0: max(PTM staging, input columns)
+  size_t xs_off, xs_bytes;  // region 0: max(PTM staging, 2 x input columns)
   size_t terms_off;         // Term[max_terms]
   size_t rows_off;          // RowInfo[kout]
   size_t offin_off;         // int64[kin]
@@ -100,7 +100,7 @@ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 SmemLayout make_layout(int kin, int kout, int max_terms, int block, size_t item_bytes) {
   SmemLayout L;
-  const size_t xs = (size_t)kin * block * item_bytes;
+  const size_t xs = 2 * (size_t)kin * block * item_bytes;  // double buffer
   const size_t stage = (size_t)kin * kout * sizeof(double);
   L.xs_off = 0;
   L.xs_bytes = std::max(xs, stage);
@@ -147,6 +147,22 @@ struct SplitCost {
     issue += sgn * (24.f * n + 30.f);
   }
 };
+
+// Per-thread asynchronous global->shared copies (no register staging).
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  if constexpr (BYTES == 16) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gsrc), "n"(BYTES) : "memory");
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 template <typename T, bool PAIR>
 struct Vec;
@@ -359,15 +375,41 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
   V* __restrict__ out = static_cast<V*>(p.out);
   unsigned bad = 0;
   const uint64_t stride = (uint64_t)gridDim.x * nthr;
-  for (uint64_t it = (uint64_t)blockIdx.x * nthr + tid; it < p.n_items; it += stride) {
+  const int buf_len = p.kin * nthr;  // V elements per buffer
+  // Decode item -> (input offset, output offset) in V units; with PAIR all
+  // strides are even and the offsets are halved.
+  auto offsets = [&](uint64_t it, int64_t& bi, int64_t& bo) {
     const uint64_t t1 = fdiv(it, p.div_z);
     const uint64_t zi = it - t1 * p.div_z.d;
     const uint64_t x = fdiv(t1, p.div_y);
     const uint64_t y = t1 - x * p.div_y.d;
-    // element offsets; with PAIR all strides are even, divide by 2 for V
-    const int64_t bi = ((int64_t)x * p.sxi + (int64_t)y * p.syi) / NL + (int64_t)zi;
-    const int64_t bo = ((int64_t)x * p.sxo + (int64_t)y * p.syo) / NL + (int64_t)zi;
-    for (int k = 0; k < p.kin; ++k) xs[k * nthr + tid] = in[bi + offin[k] / NL];
+    bi = ((int64_t)x * p.sxi + (int64_t)y * p.syi) / NL + (int64_t)zi;
+    bo = ((int64_t)x * p.sxo + (int64_t)y * p.syo) / NL + (int64_t)zi;
+  };
+  auto prefetch = [&](int64_t bi, int b) {
+    V* dst = xs + b * buf_len + tid;
+    for (int k = 0; k < p.kin; ++k) cp_async<(int)sizeof(V)>(dst + k * nthr, in + bi + offin[k] / NL);
+  };
+  uint64_t it = (uint64_t)blockIdx.x * nthr + tid;
+  int64_t bi_cur = 0, bo_cur = 0;
+  if (it < p.n_items) {
+    offsets(it, bi_cur, bo_cur);
+    prefetch(bi_cur, 0);
+  }
+  cp_async_commit();
+  int b = 0;
+  for (; it < p.n_items; it += stride) {
+    // prefetch the next item into the other buffer, then wait for this one
+    const uint64_t nx = it + stride;
+    int64_t bi_nx = 0, bo_nx = 0;
+    if (nx < p.n_items) {
+      offsets(nx, bi_nx, bo_nx);
+      prefetch(bi_nx, b ^ 1);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();
+    const V* xb = xs + b * buf_len;
+    const int64_t bo = bo_cur;
     for (int r = 0; r < p.kout; ++r) {
       const RowInfo ri = rows[r];
       if constexpr (sizeof(T) == 4) {  // FP32 storage and arithmetic
@@ -377,7 +419,7 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
         for (int t = ri.beg; t < ri.end; ++t) {
           const Term tm = terms[t];
           const float pf = __int_as_float(__double2loint(tm.p));
-          const V xv = xs[tm.k * nthr + tid];
+          const V xv = xb[tm.k * nthr + tid];
 #pragma unroll
           for (int l = 0; l < NL; ++l) facc[l] = fmaf(pf, lane(xv, l), facc[l]);
         }
@@ -388,15 +430,14 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
           o = facc[0];
         }
         out[bo + offout[r] / NL] = o;
-        continue;
-      }
+      } else {
       double acc[NL];
 #pragma unroll
       for (int l = 0; l < NL; ++l) acc[l] = 0.0;
       if (ri.mode == kDP) {
         for (int t = ri.beg; t < ri.end; ++t) {
           const Term tm = terms[t];
-          const V xv = xs[tm.k * nthr + tid];
+          const V xv = xb[tm.k * nthr + tid];
 #pragma unroll
           for (int l = 0; l < NL; ++l) acc[l] = fma(tm.p, (double)lane(xv, l), acc[l]);
         }
@@ -406,7 +447,7 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
           const Term tm = terms[ri.beg];
           const float ph = __int_as_float(__double2hiint(tm.p));
           const float pl = __int_as_float(__double2loint(tm.p));
-          const V xv = xs[tm.k * nthr + tid];
+          const V xv = xb[tm.k * nthr + tid];
 #pragma unroll
           for (int l = 0; l < NL; ++l) {
             float xh, xl;
@@ -418,7 +459,7 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
           const Term tm = terms[t];
           const float ph = __int_as_float(__double2hiint(tm.p));
           const float pl = __int_as_float(__double2loint(tm.p));
-          const V xv = xs[tm.k * nthr + tid];
+          const V xv = xb[tm.k * nthr + tid];
 #pragma unroll
           for (int l = 0; l < NL; ++l) {
             float xh, xl;
@@ -430,21 +471,29 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
         for (int l = 0; l < NL; ++l) acc[l] = df_to_double(s[l], c[l]);
       }
       out[bo + offout[r] / NL] = make_vec<V>(acc[0], acc[NL - 1]);
+      }  // FP64 storage
     }
+    bo_cur = bo_nx;
+    b ^= 1;
   }
+  cp_async_wait<0>();
   if (bad && p.status) atomicOr(p.status, QSGB_DEV_RANGE);
 }
 
 template <typename T, bool PAIR>
 int launch_apply(const ApplyParams& p, cudaStream_t stream) {
   using V = typename Vec<T, PAIR>::type;
-  const int block = kBlock;
-  SmemLayout L = make_layout(p.kin, p.kout, p.max_terms, block, sizeof(V));
   auto kern = apply_ptm_kernel<T, PAIR>;
-  if (L.total > 48 * 1024) {
-    if (L.total > 227 * 1024) return QSGB_ERR_UNSUPPORTED;
-    QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
+  // largest block (<= 128 threads) whose shared memory fits
+  int block = kBlock;
+  SmemLayout L = make_layout(p.kin, p.kout, p.max_terms, block, sizeof(V));
+  while (L.total > 227 * 1024 && block > 32) {
+    block /= 2;
+    L = make_layout(p.kin, p.kout, p.max_terms, block, sizeof(V));
   }
+  if (L.total > 227 * 1024) return QSGB_ERR_UNSUPPORTED;
+  if (L.total > 48 * 1024)
+    QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
   int occ = 0;
   QSGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, L.total));
   if (occ < 1) return QSGB_ERR_UNSUPPORTED;
@@ -505,8 +554,15 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.div_z = make_fastdiv((uint64_t)(pair ? Z / 2 : Z));
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
-  if (dtype == QSGB_F32) return pair ? launch_apply<float, true>(p, s) : launch_apply<float, false>(p, s);
-  return pair ? launch_apply<double, true>(p, s) : launch_apply<double, false>(p, s);
+  int st;
+  if (pair) {
+    st = dtype == QSGB_F32 ? launch_apply<float, true>(p, s) : launch_apply<double, true>(p, s);
+    if (st != QSGB_ERR_UNSUPPORTED) return st;
+    // pairs do not fit in shared memory: single groups
+    p.div_z = make_fastdiv((uint64_t)Z);
+    p.n_items = (uint64_t)X * Y * Z;
+  }
+  return dtype == QSGB_F32 ? launch_apply<float, false>(p, s) : launch_apply<double, false>(p, s);
 }
 
 }  // namespace
