@@ -8,13 +8,20 @@
 // Design:
 //  * The state tensor is viewed as (X, Da, Y, Db, Z) with targets a < b; a
 //    one-qudit PTM is the case X = Da = 1.  A "group" is one bystander index
-//    (x, y, z); it owns Kin = Da_in*Db_in inputs and Kout outputs.
-//  * Each block compacts the PTM into per-row term lists in shared memory
-//    once, then loops grid-stride over groups.  Consecutive threads take
-//    consecutive z; when Z is even a thread takes the pair (z, z+1), so every
-//    load and store is a 16-byte access and a warp covers contiguous runs.
-//  * Inputs are parked in a per-thread shared-memory column so that the term
-//    loops can index them at run time.
+//    (x, y, z); it owns Kin = Da_in*Db_in inputs and Kout outputs.  When Z is
+//    even an "item" is the pair of groups (z, z+1) and every access is 16
+//    bytes wide; otherwise an item is one group.
+//  * Persistent blocks of 256 threads (8 warps).  Each block compacts the PTM
+//    once into per-row term lists in shared memory, then walks tiles of
+//    T = 32*IW items: the whole block copies a tile's Kin x T inputs into
+//    shared memory with cp.async (double-buffered: tile i+1 streams in while
+//    tile i is computed), and the 8 warps split the work as IW "item warps"
+//    x RG = 8/IW "row groups": warp (iw, rg) computes the rows assigned to
+//    row group rg (balanced by cost) for items iw*32 .. iw*32+31.  Shared
+//    memory therefore scales with the tile, not with the thread count.
+//  * Every access pattern is warp-uniform: all lanes of a warp walk the same
+//    row and term lists, term data are shared-memory broadcasts, and input
+//    reads are consecutive 8/16-byte words (conflict free).
 //  * FP64 storage, per-row arithmetic.  GB300 issues ~1.9 FP64 FMAs per SM
 //    clock, about 1.4 per streamed element at full HBM bandwidth, against
 //    ~58x that on the FP32 pipes.  A row is computed either with native FP64
@@ -35,10 +42,11 @@ namespace qsgb {
 
 namespace {
 
-constexpr int kMaxK = 256;        // Kin, Kout limit
-constexpr int kMaxEntries = 6561; // Kout*Kin limit (two qutrits)
-constexpr int kMaxInline = 256;   // host PTMs up to 16x16 travel in the launch
-constexpr int kBlock = 128;
+constexpr int kMaxK = 256;         // Kin, Kout limit
+constexpr int kMaxEntries = 6561;  // Kout*Kin limit (two qutrits)
+constexpr int kMaxInline = 256;    // host PTMs up to 16x16 travel in the launch
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
 
 enum RowMode { kZero = 0, kDP = 1, kDF = 2, kF32 = 3 };
 
@@ -61,8 +69,9 @@ struct ApplyParams {
   int flags;
   int arith;
   int max_terms;
-  uint64_t n_items;   // groups, or group pairs when PAIR
-  FastDiv div_z, div_y;  // Z (or Z/2 when PAIR), Y
+  int iw;             // item warps per tile (tile = 32*iw items)
+  uint64_t n_items;   // groups, or group pairs
+  FastDiv div_z, div_y;  // Z (or Z/2 for pairs), Y
   int64_t sxi, syi, sai, sbi;  // input strides (z stride 1)
   int64_t sxo, syo, sao, sbo;  // output strides
   unsigned* status;
@@ -86,9 +95,12 @@ __device__ __forceinline__ int ptm_index(const ApplyParams& p, int r, int k) {
 }
 
 struct SmemLayout {
-  size_t xs_off, xs_bytes;  // region 0: max(PTM staging, 2 x input columns)
+  size_t xs_off, xs_bytes;  // region 0: max(PTM staging, 2 input tiles)
+  size_t bo_off;            // int64[2][T] output offsets of the tile items
   size_t terms_off;         // Term[max_terms]
   size_t rows_off;          // RowInfo[kout]
+  size_t rg_off;            // int[kWarps][kout] rows of each row group
+  size_t rgn_off;           // int[kWarps] row counts
   size_t offin_off;         // int64[kin]
   size_t offout_off;        // int64[kout]
   size_t cnt_off;           // int[kout] term counts
@@ -98,17 +110,23 @@ struct SmemLayout {
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-SmemLayout make_layout(int kin, int kout, int max_terms, int block, size_t item_bytes) {
+SmemLayout make_layout(int kin, int kout, int max_terms, int tile, size_t item_bytes) {
   SmemLayout L;
-  const size_t xs = 2 * (size_t)kin * block * item_bytes;  // double buffer
+  const size_t xs = 2 * (size_t)kin * tile * item_bytes;
   const size_t stage = (size_t)kin * kout * sizeof(double);
   L.xs_off = 0;
   L.xs_bytes = std::max(xs, stage);
   size_t o = align_up(L.xs_bytes, 16);
+  L.bo_off = o;
+  o = align_up(o + 2 * (size_t)tile * sizeof(int64_t), 16);
   L.terms_off = o;
   o = align_up(o + (size_t)max_terms * sizeof(Term), 16);
   L.rows_off = o;
   o = align_up(o + (size_t)kout * sizeof(RowInfo), 16);
+  L.rg_off = o;
+  o = align_up(o + (size_t)kWarps * kout * sizeof(int), 16);
+  L.rgn_off = o;
+  o = align_up(o + (size_t)kWarps * sizeof(int), 16);
   L.offin_off = o;
   o = align_up(o + (size_t)kin * sizeof(int64_t), 16);
   L.offout_off = o;
@@ -148,6 +166,11 @@ struct SplitCost {
   }
 };
 
+// relative cost of a row, for balancing rows over warps
+__device__ __forceinline__ int row_weight(int mode, int n) {
+  return mode == kDF ? 24 * n + 30 : (mode == kZero ? 3 : 2 * n + 4);
+}
+
 // Per-thread asynchronous global->shared copies (no register staging).
 template <int BYTES>
 __device__ __forceinline__ void cp_async(void* smem_dst, const void* gsrc) {
@@ -183,53 +206,35 @@ struct Vec<float, true> {
   using type = float2;
 };
 
-__device__ __forceinline__ double lane(const double v, int) { return v; }
-__device__ __forceinline__ double lane(const double2 v, int i) { return i ? v.y : v.x; }
-__device__ __forceinline__ float lane(const float v, int) { return v; }
-__device__ __forceinline__ float lane(const float2 v, int i) { return i ? v.y : v.x; }
+__device__ __forceinline__ double lane_of(const double v, int) { return v; }
+__device__ __forceinline__ double lane_of(const double2 v, int i) { return i ? v.y : v.x; }
+__device__ __forceinline__ float lane_of(const float v, int) { return v; }
+__device__ __forceinline__ float lane_of(const float2 v, int i) { return i ? v.y : v.x; }
 
-template <typename V>
-__device__ __forceinline__ V make_vec(double a, double b);
-template <>
-__device__ __forceinline__ double make_vec<double>(double a, double) {
-  return a;
-}
-template <>
-__device__ __forceinline__ double2 make_vec<double2>(double a, double b) {
-  return make_double2(a, b);
-}
-template <>
-__device__ __forceinline__ float make_vec<float>(double a, double) {
-  return (float)a;
-}
-template <>
-__device__ __forceinline__ float2 make_vec<float2>(double a, double b) {
-  return make_float2((float)a, (float)b);
-}
+__device__ __forceinline__ void put(double* o, const double* a) { *o = a[0]; }
+__device__ __forceinline__ void put(double2* o, const double* a) { *o = make_double2(a[0], a[1]); }
+__device__ __forceinline__ void put(float* o, const float* a) { *o = a[0]; }
+__device__ __forceinline__ void put(float2* o, const float* a) { *o = make_float2(a[0], a[1]); }
 
-// PAIR: each item is two adjacent groups (z, z+1); requires Z even.
-template <typename T, bool PAIR>
-__global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant__ ApplyParams p,
-                                                           const SmemLayout L) {
-  using V = typename Vec<T, PAIR>::type;
-  constexpr int NL = PAIR ? 2 : 1;
-  extern __shared__ __align__(16) unsigned char smem[];
+// ---------------------------------------------------------------------------
+// setup: PTM -> term lists, row modes, row groups (once per block)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ bool build_terms(const ApplyParams& p, const SmemLayout& L, unsigned char* smem) {
   double* stage = reinterpret_cast<double*>(smem + L.xs_off);
-  V* xs = reinterpret_cast<V*>(smem + L.xs_off);
   Term* terms = reinterpret_cast<Term*>(smem + L.terms_off);
   RowInfo* rows = reinterpret_cast<RowInfo*>(smem + L.rows_off);
+  int* rg_rows = reinterpret_cast<int*>(smem + L.rg_off);
+  int* rg_n = reinterpret_cast<int*>(smem + L.rgn_off);
   int64_t* offin = reinterpret_cast<int64_t*>(smem + L.offin_off);
   int64_t* offout = reinterpret_cast<int64_t*>(smem + L.offout_off);
   int* cnt = reinterpret_cast<int*>(smem + L.cnt_off);
   double* red = reinterpret_cast<double*>(smem + L.red_off);
   int* flag = reinterpret_cast<int*>(red + 33);
-
-  const int tid = threadIdx.x;
-  const int nthr = blockDim.x;
+  const int tid = threadIdx.x, nthr = blockDim.x;
   const int ne = p.kin * p.kout;
   const double* __restrict__ src = p.ptm ? p.ptm : p.ptm_inline;
 
-  // ---- 1. stage the op matrix M[r][k], max |M|, offsets ----
   double amax = 0.0;
   for (int i = tid; i < ne; i += nthr) {
     const int r = i / p.kin, k = i - r * p.kin;
@@ -254,9 +259,8 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
     red[32] = m;
   }
   __syncthreads();
-  const double thr = (p.arith == QSGB_ARITH_F64) ? 0.0 : red[32] * ((p.arith == QSGB_ARITH_F32) ? 0x1p-30 : 0x1p-52);
-
-  // ---- 2. term counts, row modes, prefix sums ----
+  const double thr =
+      (p.arith == QSGB_ARITH_F64) ? 0.0 : red[32] * ((p.arith == QSGB_ARITH_F32) ? 0x1p-30 : 0x1p-52);
   for (int r = tid; r < p.kout; r += nthr) {
     int c = 0;
     for (int k = 0; k < p.kin; ++k) c += fabs(stage[r * p.kin + k]) > thr;
@@ -264,8 +268,7 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
   }
   __syncthreads();
   if (tid == 0) {
-    // modes
-    int n_dp_best = p.kout;
+    int cut = 1 << 30, ties = 0;
     if (p.arith == QSGB_ARITH_AUTO) {
       int sorted[kMaxK];
       for (int r = 0; r < p.kout; ++r) {
@@ -280,11 +283,13 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
       // one term are always dp.  Evaluate every n_dp incrementally.
       SplitCost sc{0.f, 0.f, 0.f, 5.f * (p.kin + p.kout), (float)(p.kin + p.kout) * (float)sizeof(T) / 23.f};
       for (int i = 0; i < p.kout; ++i) {
-        if (sorted[i] == 1) sc.add_dp(1, 1.f);
-        else if (sorted[i] > 1) sc.add_df(sorted[i], 1.f);
+        if (sorted[i] == 1)
+          sc.add_dp(1, 1.f);
+        else if (sorted[i] > 1)
+          sc.add_df(sorted[i], 1.f);
       }
       float best = sc.time();
-      n_dp_best = 0;
+      int n_dp_best = 0;
       for (int i = 0; i < p.kout; ++i) {
         if (sorted[i] > 1) {
           sc.add_df(sorted[i], -1.f);
@@ -296,55 +301,66 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
           n_dp_best = i + 1;
         }
       }
-      // rows with the n_dp_best smallest counts are dp: threshold on counts
-      // (ties broken by row index)
-      int cut = n_dp_best > 0 ? sorted[n_dp_best - 1] : -1;
-      int ties = 0;
+      cut = n_dp_best > 0 ? sorted[n_dp_best - 1] : -1;
       for (int i = 0; i < n_dp_best; ++i) ties += sorted[i] == cut;
-      int t = 0;
+    }
+    int t = 0;
+    for (int r = 0; r < p.kout; ++r) {
+      const int c = cnt[r];
+      int mode;
+      if (c == 0)
+        mode = kZero;
+      else if (p.arith == QSGB_ARITH_F32)
+        mode = kF32;
+      else if (p.arith == QSGB_ARITH_F64 || c == 1)
+        mode = kDP;
+      else if (p.arith == QSGB_ARITH_DF64)
+        mode = kDF;
+      else if (c < cut)
+        mode = kDP;
+      else if (c == cut && ties > 0) {
+        mode = kDP;
+        --ties;
+      } else
+        mode = kDF;
+      rows[r].beg = t;
+      rows[r].end = t + c;
+      rows[r].mode = mode;
+      rows[r].pad = 0;
+      t += c;
+    }
+    *flag = (t > p.max_terms) ? 1 : 0;
+    // balance rows over the row groups (longest processing time first)
+    const int rg_count = kWarps / p.iw;
+    int load[kWarps];
+    for (int g = 0; g < rg_count; ++g) {
+      load[g] = 0;
+      rg_n[g] = 0;
+    }
+    bool used[kMaxK];
+    for (int r = 0; r < p.kout; ++r) used[r] = false;
+    for (int step = 0; step < p.kout; ++step) {
+      int rbest = -1, wbest = -1;
       for (int r = 0; r < p.kout; ++r) {
-        const int c = cnt[r];
-        int mode;
-        if (c == 0)
-          mode = kZero;
-        else if (c == 1 || c < cut)
-          mode = kDP;
-        else if (c == cut && ties > 0) {
-          mode = kDP;
-          --ties;
-        } else
-          mode = kDF;
-        rows[r].beg = t;
-        rows[r].end = t + c;
-        rows[r].mode = mode;
-        t += c;
+        if (used[r]) continue;
+        const int w = row_weight(rows[r].mode, cnt[r]);
+        if (w > wbest) {
+          wbest = w;
+          rbest = r;
+        }
       }
-      if (t > p.max_terms) *flag = 1; else *flag = 0;
-    } else {
-      int t = 0;
-      for (int r = 0; r < p.kout; ++r) {
-        const int c = cnt[r];
-        int mode;
-        if (c == 0)
-          mode = kZero;
-        else if (p.arith == QSGB_ARITH_F32)
-          mode = kF32;
-        else if (p.arith == QSGB_ARITH_F64 || c == 1)
-          mode = kDP;
-        else
-          mode = kDF;
-        rows[r].beg = t;
-        rows[r].end = t + c;
-        rows[r].mode = mode;
-        t += c;
-      }
-      *flag = (t > p.max_terms) ? 1 : 0;
+      used[rbest] = true;
+      int g = 0;
+      for (int h = 1; h < rg_count; ++h)
+        if (load[h] < load[g]) g = h;
+      load[g] += wbest;
+      rg_rows[g * p.kout + rg_n[g]++] = rbest;
     }
   }
   __syncthreads();
   if (*flag) {
     if (tid == 0 && p.status) atomicOr(p.status, QSGB_DEV_BADITEM);
-    return;
+    return false;
   }
   for (int r = tid; r < p.kout; r += nthr) {
     const RowInfo ri = rows[r];
@@ -368,145 +384,184 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
       }
     }
   }
-  __syncthreads();  // stage[] is reused as xs[] below
+  __syncthreads();  // stage[] is reused for the input tiles
+  return true;
+}
 
-  // ---- 3. stream the groups ----
+// ---------------------------------------------------------------------------
+// main kernel
+// ---------------------------------------------------------------------------
+template <typename T, bool PAIR>
+__global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant__ ApplyParams p,
+                                                           const SmemLayout L) {
+  using V = typename Vec<T, PAIR>::type;
+  constexpr int NL = PAIR ? 2 : 1;
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (!build_terms<T>(p, L, smem)) return;
+
+  V* xs = reinterpret_cast<V*>(smem + L.xs_off);
+  int64_t* bo_tile = reinterpret_cast<int64_t*>(smem + L.bo_off);
+  const Term* terms = reinterpret_cast<const Term*>(smem + L.terms_off);
+  const RowInfo* rows = reinterpret_cast<const RowInfo*>(smem + L.rows_off);
+  const int* rg_rows = reinterpret_cast<const int*>(smem + L.rg_off);
+  const int* rg_n = reinterpret_cast<const int*>(smem + L.rgn_off);
+  const int64_t* offin = reinterpret_cast<const int64_t*>(smem + L.offin_off);
+  const int64_t* offout = reinterpret_cast<const int64_t*>(smem + L.offout_off);
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int tile = 32 * p.iw;
+  const int buf_len = p.kin * tile;  // V elements per buffer
+  const uint64_t n_tiles = (p.n_items + tile - 1) / tile;
   const V* __restrict__ in = static_cast<const V*>(p.in);
   V* __restrict__ out = static_cast<V*>(p.out);
-  unsigned bad = 0;
-  const uint64_t stride = (uint64_t)gridDim.x * nthr;
-  const int buf_len = p.kin * nthr;  // V elements per buffer
-  // Decode item -> (input offset, output offset) in V units; with PAIR all
-  // strides are even and the offsets are halved.
-  auto offsets = [&](uint64_t it, int64_t& bi, int64_t& bo) {
-    const uint64_t t1 = fdiv(it, p.div_z);
-    const uint64_t zi = it - t1 * p.div_z.d;
-    const uint64_t x = fdiv(t1, p.div_y);
-    const uint64_t y = t1 - x * p.div_y.d;
-    bi = ((int64_t)x * p.sxi + (int64_t)y * p.syi) / NL + (int64_t)zi;
-    bo = ((int64_t)x * p.sxo + (int64_t)y * p.syo) / NL + (int64_t)zi;
-  };
-  auto prefetch = [&](int64_t bi, int b) {
-    V* dst = xs + b * buf_len + tid;
-    for (int k = 0; k < p.kin; ++k) cp_async<(int)sizeof(V)>(dst + k * nthr, in + bi + offin[k] / NL);
-  };
-  uint64_t it = (uint64_t)blockIdx.x * nthr + tid;
-  int64_t bi_cur = 0, bo_cur = 0;
-  if (it < p.n_items) {
-    offsets(it, bi_cur, bo_cur);
-    prefetch(bi_cur, 0);
-  }
-  cp_async_commit();
-  int b = 0;
-  for (; it < p.n_items; it += stride) {
-    // prefetch the next item into the other buffer, then wait for this one
-    const uint64_t nx = it + stride;
-    int64_t bi_nx = 0, bo_nx = 0;
-    if (nx < p.n_items) {
-      offsets(nx, bi_nx, bo_nx);
-      prefetch(bi_nx, b ^ 1);
+
+  // loader role: thread -> (item of the tile, first input row)
+  const int ld_item = tid % tile;
+  const int ld_k0 = tid / tile;
+  const int ld_kstep = kBlock / tile;
+  // compute role: warp -> (item warp, row group)
+  const int iw = warp % p.iw;
+  const int rg = warp / p.iw;
+  const int my_item = iw * 32 + lane;
+  const int n_my_rows = rg_n[rg];
+  const int* my_rows = rg_rows + rg * p.kout;
+
+  auto load_tile = [&](uint64_t t, int b) {
+    const uint64_t it = t * tile + ld_item;
+    if (it < p.n_items) {
+      const uint64_t t1 = fdiv(it, p.div_z);
+      const uint64_t zi = it - t1 * p.div_z.d;
+      const uint64_t x = fdiv(t1, p.div_y);
+      const uint64_t y = t1 - x * p.div_y.d;
+      // with pairs all strides are even: offsets are halved (V units)
+      const int64_t bi = ((int64_t)x * p.sxi + (int64_t)y * p.syi) / NL + (int64_t)zi;
+      if (ld_k0 == 0) bo_tile[b * tile + ld_item] = ((int64_t)x * p.sxo + (int64_t)y * p.syo) / NL + (int64_t)zi;
+      V* dst = xs + b * buf_len + ld_item;
+      for (int k = ld_k0; k < p.kin; k += ld_kstep)
+        cp_async<(int)sizeof(V)>(dst + k * tile, in + bi + offin[k] / NL);
     }
+  };
+
+  unsigned bad = 0;
+  uint64_t t = blockIdx.x;
+  int b = 0;
+  if (t < n_tiles) load_tile(t, 0);
+  cp_async_commit();
+  for (; t < n_tiles; t += gridDim.x) {
+    const uint64_t tn = t + gridDim.x;
+    if (tn < n_tiles) load_tile(tn, b ^ 1);
     cp_async_commit();
     cp_async_wait<1>();
-    const V* xb = xs + b * buf_len;
-    const int64_t bo = bo_cur;
-    for (int r = 0; r < p.kout; ++r) {
-      const RowInfo ri = rows[r];
-      if constexpr (sizeof(T) == 4) {  // FP32 storage and arithmetic
-        float facc[NL];
+    __syncthreads();  // tile t is in shared memory
+
+    const uint64_t item = t * tile + my_item;
+    if (item < p.n_items) {
+      const V* xb = xs + b * buf_len + my_item;
+      const int64_t bo = bo_tile[b * tile + my_item];
+      for (int j = 0; j < n_my_rows; ++j) {
+        const int r = my_rows[j];
+        const RowInfo ri = rows[r];
+        V* dst = out + bo + offout[r] / NL;
+        if constexpr (sizeof(T) == 4) {  // FP32 storage and arithmetic
+          float acc[NL];
 #pragma unroll
-        for (int l = 0; l < NL; ++l) facc[l] = 0.f;
-        for (int t = ri.beg; t < ri.end; ++t) {
-          const Term tm = terms[t];
-          const float pf = __int_as_float(__double2loint(tm.p));
-          const V xv = xb[tm.k * nthr + tid];
+          for (int l = 0; l < NL; ++l) acc[l] = 0.f;
+          for (int q = ri.beg; q < ri.end; ++q) {
+            const Term tm = terms[q];
+            const float pf = __int_as_float(__double2loint(tm.p));
+            const V xv = xb[tm.k * tile];
 #pragma unroll
-          for (int l = 0; l < NL; ++l) facc[l] = fmaf(pf, lane(xv, l), facc[l]);
-        }
-        V o;
-        if constexpr (PAIR) {
-          o = make_float2(facc[0], facc[NL - 1]);
+            for (int l = 0; l < NL; ++l) acc[l] = fmaf(pf, lane_of(xv, l), acc[l]);
+          }
+          put(dst, acc);
         } else {
-          o = facc[0];
-        }
-        out[bo + offout[r] / NL] = o;
-      } else {
-      double acc[NL];
+          double acc[NL];
 #pragma unroll
-      for (int l = 0; l < NL; ++l) acc[l] = 0.0;
-      if (ri.mode == kDP) {
-        for (int t = ri.beg; t < ri.end; ++t) {
-          const Term tm = terms[t];
-          const V xv = xb[tm.k * nthr + tid];
+          for (int l = 0; l < NL; ++l) acc[l] = 0.0;
+          if (ri.mode == kDP) {
+            for (int q = ri.beg; q < ri.end; ++q) {
+              const Term tm = terms[q];
+              const V xv = xb[tm.k * tile];
 #pragma unroll
-          for (int l = 0; l < NL; ++l) acc[l] = fma(tm.p, (double)lane(xv, l), acc[l]);
-        }
-      } else if (ri.mode == kDF) {
-        float s[NL], c[NL];
-        {
-          const Term tm = terms[ri.beg];
-          const float ph = __int_as_float(__double2hiint(tm.p));
-          const float pl = __int_as_float(__double2loint(tm.p));
-          const V xv = xb[tm.k * nthr + tid];
+              for (int l = 0; l < NL; ++l) acc[l] = fma(tm.p, (double)lane_of(xv, l), acc[l]);
+            }
+          } else if (ri.mode == kDF) {
+            float s[NL], c[NL];
+            {
+              const Term tm = terms[ri.beg];
+              const float ph = __int_as_float(__double2hiint(tm.p));
+              const float pl = __int_as_float(__double2loint(tm.p));
+              const V xv = xb[tm.k * tile];
 #pragma unroll
-          for (int l = 0; l < NL; ++l) {
-            float xh, xl;
-            split_f64((double)lane(xv, l), xh, xl, bad);
-            df_mul(s[l], c[l], ph, pl, xh, xl);
+              for (int l = 0; l < NL; ++l) {
+                float xh, xl;
+                split_f64((double)lane_of(xv, l), xh, xl, bad);
+                df_mul(s[l], c[l], ph, pl, xh, xl);
+              }
+            }
+            for (int q = ri.beg + 1; q < ri.end; ++q) {
+              const Term tm = terms[q];
+              const float ph = __int_as_float(__double2hiint(tm.p));
+              const float pl = __int_as_float(__double2loint(tm.p));
+              const V xv = xb[tm.k * tile];
+#pragma unroll
+              for (int l = 0; l < NL; ++l) {
+                float xh, xl;
+                split_f64((double)lane_of(xv, l), xh, xl, bad);
+                df_fma(s[l], c[l], ph, pl, xh, xl);
+              }
+            }
+#pragma unroll
+            for (int l = 0; l < NL; ++l) acc[l] = df_to_double(s[l], c[l]);
           }
+          put(dst, acc);
         }
-        for (int t = ri.beg + 1; t < ri.end; ++t) {
-          const Term tm = terms[t];
-          const float ph = __int_as_float(__double2hiint(tm.p));
-          const float pl = __int_as_float(__double2loint(tm.p));
-          const V xv = xb[tm.k * nthr + tid];
-#pragma unroll
-          for (int l = 0; l < NL; ++l) {
-            float xh, xl;
-            split_f64((double)lane(xv, l), xh, xl, bad);
-            df_fma(s[l], c[l], ph, pl, xh, xl);
-          }
-        }
-#pragma unroll
-        for (int l = 0; l < NL; ++l) acc[l] = df_to_double(s[l], c[l]);
       }
-      out[bo + offout[r] / NL] = make_vec<V>(acc[0], acc[NL - 1]);
-      }  // FP64 storage
     }
-    bo_cur = bo_nx;
+    __syncthreads();  // buffer b is free for the tile after next
     b ^= 1;
   }
   cp_async_wait<0>();
   if (bad && p.status) atomicOr(p.status, QSGB_DEV_RANGE);
 }
 
+// row groups = min(Kout, 4) rounded down to a power of two; the remaining
+// warps of the 8 are item warps (tile = 32 * 8 / row groups items)
+int pick_iw(int kout) {
+  int rg = 1;
+  while (rg * 2 <= std::min(kout, 4)) rg *= 2;
+  return kWarps / rg;
+}
+
 template <typename T, bool PAIR>
-int launch_apply(const ApplyParams& p, cudaStream_t stream) {
+int launch_apply(ApplyParams& p, cudaStream_t stream) {
   using V = typename Vec<T, PAIR>::type;
   auto kern = apply_ptm_kernel<T, PAIR>;
-  // largest block (<= 128 threads) whose shared memory fits
-  int block = kBlock;
-  SmemLayout L = make_layout(p.kin, p.kout, p.max_terms, block, sizeof(V));
-  while (L.total > 227 * 1024 && block > 32) {
-    block /= 2;
-    L = make_layout(p.kin, p.kout, p.max_terms, block, sizeof(V));
+  // shrink the tile (more row groups) if shared memory is short
+  int iw = p.iw;
+  SmemLayout L = make_layout(p.kin, p.kout, p.max_terms, 32 * iw, sizeof(V));
+  while (L.total > 227 * 1024 && iw > 1) {
+    iw /= 2;
+    L = make_layout(p.kin, p.kout, p.max_terms, 32 * iw, sizeof(V));
   }
   if (L.total > 227 * 1024) return QSGB_ERR_UNSUPPORTED;
+  p.iw = iw;
   if (L.total > 48 * 1024)
     QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
   int occ = 0;
-  QSGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, L.total));
+  QSGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlock, L.total));
   if (occ < 1) return QSGB_ERR_UNSUPPORTED;
-  const uint64_t need = (p.n_items + block - 1) / block;
+  const uint64_t tiles = (p.n_items + 32 * iw - 1) / (32 * iw);
   const uint64_t cap = (uint64_t)sm_count() * occ;
-  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(need, cap));
-  kern<<<grid, block, L.total, stream>>>(p, L);
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(tiles, cap));
+  kern<<<grid, kBlock, L.total, stream>>>(p, L);
   return launch_status();
 }
 
-int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, int64_t db_out,
-                 int64_t da_in, int64_t db_in, int64_t X, int64_t Y, int64_t Z, int flags,
-                 int dtype, int arith, int64_t max_terms, unsigned* status, void* stream) {
+int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, int64_t db_out, int64_t da_in,
+                 int64_t db_in, int64_t X, int64_t Y, int64_t Z, int flags, int dtype, int arith,
+                 int64_t max_terms, unsigned* status, void* stream) {
   if (!in || !out || !ptm) return QSGB_ERR_INVALID;
   if (in == out) return QSGB_ERR_INVALID;
   if (da_out < 1 || db_out < 1 || da_in < 1 || db_in < 1 || X < 1 || Y < 1 || Z < 1) return QSGB_ERR_INVALID;
@@ -539,6 +594,7 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.flags = flags & 3;
   p.arith = arith;
   p.max_terms = (int)max_terms;
+  p.iw = pick_iw((int)kout);
   p.sbi = Z;
   p.syi = db_in * Z;
   p.sai = Y * db_in * Z;
@@ -554,11 +610,11 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.div_z = make_fastdiv((uint64_t)(pair ? Z / 2 : Z));
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
-  int st;
   if (pair) {
-    st = dtype == QSGB_F32 ? launch_apply<float, true>(p, s) : launch_apply<double, true>(p, s);
+    const int st = dtype == QSGB_F32 ? launch_apply<float, true>(p, s) : launch_apply<double, true>(p, s);
     if (st != QSGB_ERR_UNSUPPORTED) return st;
     // pairs do not fit in shared memory: single groups
+    p.iw = pick_iw((int)kout);
     p.div_z = make_fastdiv((uint64_t)Z);
     p.n_items = (uint64_t)X * Y * Z;
   }
