@@ -54,15 +54,24 @@ extern "C" {
                                  `qubit0 > qubit1` case, cuda.py:171-173 */
 #define QSGB_PTM_TRANSPOSED 2 /* apply the transpose of the stored PTM
                                  (adjoint / gradient w.r.t. the state) */
-#define QSGB_PTM_HOST 4       /* `ptm` is a HOST pointer; its d_out*d_in <=
-                                 256 entries are copied into the launch
-                                 parameters (no device copy, no allocation) */
+#define QSGB_PTM_HOST 4       /* `ptm` is a HOST pointer, read during the
+                                 call (no device copy, no allocation).  Its
+                                 sparsity pattern selects a kernel compiled
+                                 for that pattern at run time (NVRTC, cached);
+                                 without NVRTC, PTMs of <= 256 entries run in
+                                 the generic kernel, larger ones return
+                                 QSGB_ERR_UNSUPPORTED */
+#define QSGB_PTM_NOJIT 8      /* never use the run-time specialised kernel */
 
 /* Version of this ABI (bumped on any signature change). */
 int qsgb_abi_version(void);
 
 /* Human-readable text for a status code (static storage). */
 const char* qsgb_status_string(int status);
+
+/* 1 if run-time specialisation of apply kernels (NVRTC) is available (and
+ * not disabled by the environment variable QSGB_NO_JIT), else 0. */
+int qsgb_jit_available(void);
 
 /*
  * One-qudit PTM application.

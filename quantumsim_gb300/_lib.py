@@ -30,6 +30,7 @@ ARITH_F32 = 3
 PTM_SWAPPED = 1
 PTM_TRANSPOSED = 2
 PTM_HOST = 4
+PTM_NOJIT = 8
 
 _c_void_p = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -42,6 +43,7 @@ _p_i32 = ctypes.POINTER(ctypes.c_int32)
 SIGNATURES = {
     'qsgb_abi_version': (_int, []),
     'qsgb_status_string': (ctypes.c_char_p, [_int]),
+    'qsgb_jit_available': (_int, []),
     'qsgb_apply_ptm1': (_int, [_c_void_p, _c_void_p, _c_void_p, _i64, _i64,
                                _i64, _i64, _int, _int, _int, _i64, _c_void_p,
                                _c_void_p]),

@@ -19,7 +19,10 @@ LIB_PATH = os.path.join(PKG_DIR, 'libqsgb.so')
 
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC',
-              '--expt-relaxed-constexpr', '-I', INCLUDE]
+              '--expt-relaxed-constexpr', '-I', INCLUDE, '-I', BUILD_DIR]
+LINK_FLAGS = ['-ldl']
+# device helpers embedded as text for the run-time specialised kernels
+EMBED = [('qsgb_device.cuh', 'qsgb_device_src.inc', 'kQsgbDeviceSrc')]
 
 
 def _nvcc():
@@ -39,6 +42,7 @@ def sources():
 
 def _deps():
     return (sources() + glob.glob(os.path.join(CSRC, '*.cuh')) +
+            glob.glob(os.path.join(CSRC, '*.h')) +
             glob.glob(os.path.join(INCLUDE, '*.h')))
 
 
@@ -49,12 +53,25 @@ def is_stale():
     return any(os.path.getmtime(f) > t for f in _deps())
 
 
+def _embed():
+    """Write each embedded header as a C++ raw string literal."""
+    for src, dst, name in EMBED:
+        with open(os.path.join(CSRC, src)) as f:
+            text = f.read()
+        if ')QSGB"' in text:
+            raise RuntimeError('embedded source contains the delimiter')
+        with open(os.path.join(BUILD_DIR, dst), 'w') as f:
+            f.write('static const char {}[] = R"QSGB({})QSGB";\n'.format(
+                name, text))
+
+
 def build(force=False, verbose=False, jobs=None):
     """Compile and link ``libqsgb.so``; returns its path."""
     if not force and not is_stale():
         return LIB_PATH
     nvcc = _nvcc()
     os.makedirs(BUILD_DIR, exist_ok=True)
+    _embed()
     srcs = sources()
     objs = [os.path.join(BUILD_DIR, os.path.basename(s)[:-3] + '.o')
             for s in srcs]
@@ -73,7 +90,7 @@ def build(force=False, verbose=False, jobs=None):
     with _cf.ThreadPoolExecutor(max_workers=jobs or len(srcs)) as ex:
         list(ex.map(compile_one, zip(srcs, objs)))
     tmp = LIB_PATH + '.tmp'
-    cmd = [nvcc] + ARCH_FLAGS + ['-shared', '-o', tmp] + objs
+    cmd = [nvcc] + ARCH_FLAGS + ['-shared', '-o', tmp] + objs + LINK_FLAGS
     if verbose:
         print(' '.join(cmd))
     res = subprocess.run(cmd, capture_output=True, text=True)

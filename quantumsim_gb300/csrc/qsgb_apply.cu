@@ -37,6 +37,9 @@
 #include <algorithm>
 
 #include "qsgb_common.cuh"
+#include "qsgb_jit.h"
+#include <cmath>
+#include <vector>
 
 namespace qsgb {
 
@@ -559,15 +562,156 @@ int launch_apply(ApplyParams& p, cudaStream_t stream) {
   return launch_status();
 }
 
+
+// ---------------------------------------------------------------------------
+// host-side planning of the run-time specialised kernel (see qsgb_jit.cu)
+// ---------------------------------------------------------------------------
+// Row modes for the specialised kernel under QSGB_ARITH_AUTO: rows in
+// ascending term count are computed in FP64 while that lowers the larger of
+// the estimated times per group (SM clock cycles) of HBM traffic, the FP64
+// pipe (~1.9 ops/clk), the integer pipe (64 lanes/clk: ~16 ops per split
+// input, ~30 per float-float row result) and instruction issue (128/clk;
+// ~12 per float-float term).
+void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, size_t esz, std::vector<int>& mode) {
+  const int kout = (int)cols.size();
+  mode.assign(kout, jit::kModeZero);
+  for (int r = 0; r < kout; ++r) {
+    const int n = (int)cols[r].size();
+    if (n == 0) continue;
+    if (arith == QSGB_ARITH_F32) mode[r] = jit::kModeF32;
+    else if (arith == QSGB_ARITH_F64 || n == 1) mode[r] = jit::kModeDP;
+    else mode[r] = jit::kModeDF;
+  }
+  if (arith != QSGB_ARITH_AUTO) return;
+  std::vector<int> order;
+  for (int r = 0; r < kout; ++r)
+    if (cols[r].size() > 1) order.push_back(r);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cols[a].size() < cols[b].size(); });
+  auto cost = [&](const std::vector<int>& m) {
+    double dp = 0, alu = 0, issue = 0;
+    std::vector<char> split(kin, 0);
+    int n_used = 0;
+    std::vector<char> used(kin, 0);
+    for (int r = 0; r < kout; ++r) {
+      for (int k : cols[r]) {
+        if (!used[k]) {
+          used[k] = 1;
+          ++n_used;
+        }
+        if (m[r] == jit::kModeDF) split[k] = 1;
+      }
+      if (m[r] == jit::kModeDP) {
+        dp += (double)cols[r].size();
+        issue += (double)cols[r].size();
+      } else if (m[r] == jit::kModeDF) {
+        issue += 12.0 * cols[r].size() + 30.0;
+        alu += 30.0;
+      }
+    }
+    for (int k = 0; k < kin; ++k)
+      if (split[k]) {
+        alu += 16.0;
+        issue += 16.0;
+      }
+    issue += 2.0 * (n_used + kout);
+    const double hbm = (double)(kin + kout) * (double)esz / 23.0;
+    return std::max(std::max(hbm, dp / 1.9), std::max(alu / 64.0, issue / 128.0));
+  };
+  std::vector<int> m = mode;
+  double best = cost(m);
+  std::vector<int> best_m = m;
+  for (int r : order) {
+    m[r] = jit::kModeDP;
+    const double c = cost(m);
+    if (c < best * 0.999) {
+      best = c;
+      best_m = m;
+    }
+  }
+  mode = best_m;
+}
+
+// Returns QSGB_ERR_UNSUPPORTED when the specialised path does not apply.
+int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_in, int64_t db_in, int flags,
+            int dtype, int arith, bool pair, ApplyParams& p, cudaStream_t stream) {
+  if (!(flags & QSGB_PTM_HOST) || (flags & QSGB_PTM_NOJIT) || !jit::available()) return QSGB_ERR_UNSUPPORTED;
+  const int kin = (int)(da_in * db_in), kout = (int)(da_out * db_out);
+  if (kin > 81 || kout > 81) return QSGB_ERR_UNSUPPORTED;
+  // op matrix M[r][k] from the stored layout (same mapping as ptm_index)
+  std::vector<double> M((size_t)kin * kout);
+  double amax = 0.0;
+  for (int r = 0; r < kout; ++r)
+    for (int k = 0; k < kin; ++k) {
+      const int ra = r / (int)db_out, rb = r % (int)db_out;
+      const int ka = k / (int)db_in, kb = k % (int)db_in;
+      int idx;
+      switch (flags & 3) {
+        case 0: idx = r * kin + k; break;
+        case QSGB_PTM_SWAPPED: idx = ((rb * (int)da_out + ra) * (int)db_in + kb) * (int)da_in + ka; break;
+        case QSGB_PTM_TRANSPOSED: idx = k * kout + r; break;
+        default: idx = ((kb * (int)da_in + ka) * (int)db_out + rb) * (int)da_out + ra; break;
+      }
+      const double v = ptm_host[idx];
+      M[(size_t)r * kin + k] = v;
+      amax = std::max(amax, std::fabs(v));
+    }
+  const double thr = arith == QSGB_ARITH_F64 ? 0.0 : amax * (arith == QSGB_ARITH_F32 ? 0x1p-30 : 0x1p-52);
+  jit::Spec spec;
+  spec.kin = kin;
+  spec.kout = kout;
+  spec.db_in = (int)db_in;
+  spec.db_out = (int)db_out;
+  spec.pair = pair;
+  spec.f32 = dtype == QSGB_F32;
+  spec.cols.assign(kout, {});
+  for (int r = 0; r < kout; ++r)
+    for (int k = 0; k < kin; ++k)
+      if (std::fabs(M[(size_t)r * kin + k]) > thr) spec.cols[r].push_back(k);
+  plan_modes(spec.cols, kin, arith, dtype == QSGB_F64 ? 8 : 4, spec.mode);
+  std::vector<double> coef;
+  coef.reserve(spec.n_coef());
+  for (int r = 0; r < kout; ++r)
+    for (int k : spec.cols[r]) {
+      const double v = M[(size_t)r * kin + k];
+      if (spec.mode[r] == jit::kModeDF) {
+        const float h = (float)v;
+        const float l = (float)(v - (double)h);
+        uint64_t bits = ((uint64_t)__builtin_bit_cast(uint32_t, h) << 32) | __builtin_bit_cast(uint32_t, l);
+        coef.push_back(__builtin_bit_cast(double, bits));
+      } else if (spec.mode[r] == jit::kModeF32) {
+        uint64_t bits = __builtin_bit_cast(uint32_t, (float)v);
+        coef.push_back(__builtin_bit_cast(double, bits));
+      } else {
+        coef.push_back(v);
+      }
+    }
+  const int NL = pair ? 2 : 1;
+  jit::Geometry g;
+  g.in = p.in;
+  g.out = p.out;
+  g.status = p.status;
+  g.n_items = p.n_items;
+  g.div_z = p.div_z;
+  g.div_y = p.div_y;
+  g.sxi = p.sxi / NL;
+  g.syi = p.syi / NL;
+  g.sai = p.sai / NL;
+  g.sbi = p.sbi / NL;
+  g.sxo = p.sxo / NL;
+  g.syo = p.syo / NL;
+  g.sao = p.sao / NL;
+  g.sbo = p.sbo / NL;
+  return jit::launch(spec, g, coef.data(), stream);
+}
+
 int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, int64_t db_out, int64_t da_in,
                  int64_t db_in, int64_t X, int64_t Y, int64_t Z, int flags, int dtype, int arith,
                  int64_t max_terms, unsigned* status, void* stream) {
   if (!in || !out || !ptm) return QSGB_ERR_INVALID;
   if (in == out) return QSGB_ERR_INVALID;
   if (da_out < 1 || db_out < 1 || da_in < 1 || db_in < 1 || X < 1 || Y < 1 || Z < 1) return QSGB_ERR_INVALID;
-  if (flags & ~(QSGB_PTM_SWAPPED | QSGB_PTM_TRANSPOSED | QSGB_PTM_HOST)) return QSGB_ERR_INVALID;
+  if (flags & ~(QSGB_PTM_SWAPPED | QSGB_PTM_TRANSPOSED | QSGB_PTM_HOST | QSGB_PTM_NOJIT)) return QSGB_ERR_INVALID;
   const int64_t kin = da_in * db_in, kout = da_out * db_out;
-  if ((flags & QSGB_PTM_HOST) && kin * kout > kMaxInline) return QSGB_ERR_UNSUPPORTED;
   if (kin > kMaxK || kout > kMaxK || kin * kout > kMaxEntries) return QSGB_ERR_UNSUPPORTED;
   if (max_terms < 1 || max_terms > kin * kout) max_terms = kin * kout;
   if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
@@ -579,12 +723,7 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   ApplyParams p;
   p.in = in;
   p.out = out;
-  if (flags & QSGB_PTM_HOST) {
-    for (int64_t i = 0; i < kin * kout; ++i) p.ptm_inline[i] = ptm[i];
-    p.ptm = nullptr;
-  } else {
-    p.ptm = ptm;
-  }
+  p.ptm = ptm;
   p.kin = (int)kin;
   p.kout = (int)kout;
   p.da_in = (int)da_in;
@@ -610,6 +749,15 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.div_z = make_fastdiv((uint64_t)(pair ? Z / 2 : Z));
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
+  // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)
+  const int js = try_jit(ptm, da_out, db_out, da_in, db_in, flags, dtype, arith, pair, p, s);
+  if (js != QSGB_ERR_UNSUPPORTED) return js;
+  // 2. generic kernel; a host PTM travels inside its launch parameters
+  if (flags & QSGB_PTM_HOST) {
+    if (kin * kout > kMaxInline) return QSGB_ERR_UNSUPPORTED;
+    for (int64_t i = 0; i < kin * kout; ++i) p.ptm_inline[i] = ptm[i];
+    p.ptm = nullptr;
+  }
   if (pair) {
     const int st = dtype == QSGB_F32 ? launch_apply<float, true>(p, s) : launch_apply<double, true>(p, s);
     if (st != QSGB_ERR_UNSUPPORTED) return st;

@@ -19,7 +19,6 @@ import torch
 from . import _lib as L
 
 _STATUS = {}
-_PTM_HOST_MAX = 256
 
 
 def _stream_handle(t):
@@ -121,7 +120,8 @@ def apply_geometry(shape, qudits, ptm_shape, transpose=False):
 # --------------------------------------------------------------- apply_ptm
 @torch.library.custom_op('qsgb::apply_ptm', mutates_args=())
 def apply_ptm(pv: torch.Tensor, ptm: torch.Tensor, qudits: List[int],
-              arith: int, max_terms: int, transpose: bool) -> torch.Tensor:
+              arith: int, max_terms: int, transpose: bool,
+              jit: bool = True) -> torch.Tensor:
     """Apply a 1- or 2-qudit PTM (float64) to a Pauli-vector tensor.
 
     ``ptm`` may live on the device or (up to 16x16) on the host, in which
@@ -140,29 +140,41 @@ def apply_ptm(pv: torch.Tensor, ptm: torch.Tensor, qudits: List[int],
         if ptm.device != pv.device:
             raise ValueError('PTM and Pauli vector are on different devices')
     else:
-        if ptm.numel() > _PTM_HOST_MAX:
-            ptm = ptm.to(pv.device, non_blocking=False)
-        else:
-            flags |= L.PTM_HOST
+        # host PTM: read by the library during the call (its sparsity
+        # pattern selects a specialised kernel); no device copy
+        flags |= L.PTM_HOST
+    if jit is False:
+        flags |= L.PTM_NOJIT
     lib = L.load()
     st = status_tensor(pv.device)
     if out.numel() == 0:
         return out
-    if len(qudits) == 1:
-        status = lib.qsgb_apply_ptm1(
-            _ptr(pv), _ptr(out), _ptr(ptm), dbo, dbi, Y, Z, flags,
-            _dtype_code(pv), arith, max_terms, _ptr(st), _stream_handle(pv))
-    else:
-        status = lib.qsgb_apply_ptm2(
-            _ptr(pv), _ptr(out), _ptr(ptm), dao, dbo, dai, dbi, X, Y, Z,
-            flags, _dtype_code(pv), arith, max_terms, _ptr(st),
+
+    def call(ptm_, flags_):
+        if len(qudits) == 1:
+            return lib.qsgb_apply_ptm1(
+                _ptr(pv), _ptr(out), _ptr(ptm_), dbo, dbi, Y, Z, flags_,
+                _dtype_code(pv), arith, max_terms, _ptr(st),
+                _stream_handle(pv))
+        return lib.qsgb_apply_ptm2(
+            _ptr(pv), _ptr(out), _ptr(ptm_), dao, dbo, dai, dbi, X, Y, Z,
+            flags_, _dtype_code(pv), arith, max_terms, _ptr(st),
             _stream_handle(pv))
+
+    status = call(ptm, flags)
+    if status == L.ERR_UNSUPPORTED and (flags & L.PTM_HOST):
+        # no specialised kernel and too large to travel in the launch:
+        # the generic kernel reads it from device memory
+        # (stream-ordered allocator: freeing dev_ptm after the enqueue is
+        # safe for work on this stream)
+        dev_ptm = ptm.to(pv.device)
+        status = call(dev_ptm, flags & ~L.PTM_HOST)
     L.check(status, 'qsgb_apply_ptm')
     return out
 
 
 @apply_ptm.register_fake
-def _(pv, ptm, qudits, arith, max_terms, transpose):
+def _(pv, ptm, qudits, arith, max_terms, transpose, jit=True):
     new_shape = apply_geometry(pv.shape, qudits, ptm.shape, transpose)[0]
     return pv.new_empty(new_shape)
 

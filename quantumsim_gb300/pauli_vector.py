@@ -206,11 +206,10 @@ class PauliVectorGB300(_Base):
 
     # ------------------------------------------------------------ apply_ptm
     def _device_ptm(self, ptm):
-        """Host PTMs up to 16x16 ride in the launch; larger ones are cached
-        on the device by content."""
-        if ptm.size <= 256:
-            return torch.from_numpy(ptm)
-        return _PTM_CACHE.get(ptm, self._device)
+        """PTMs stay on the host: the library reads them during the call
+        (their sparsity pattern picks a kernel specialised at run time) and
+        passes the values inside the kernel launch."""
+        return torch.from_numpy(ptm)
 
     def apply_ptm(self, ptm, *qubits):
         """Apply a PTM of shape (d_out..., d_in...) to `qubits` (argument

@@ -44,6 +44,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 def test_abi_version_and_status_strings(lib):
     assert lib.qsgb_abi_version() >= 1
+    assert lib.qsgb_jit_available() in (0, 1)
     assert lib.qsgb_status_string(0) == b'ok'
     assert b'invalid' in lib.qsgb_status_string(1)
 
@@ -72,8 +73,11 @@ def test_argument_errors_rejected_on_host(lib):
     # too large PTMs are unsupported, host PTMs limited to 256 entries
     assert lib.qsgb_apply_ptm2(one, two, two, 81, 81, 81, 81, 1, 1, 1, 0,
                                L.F64, 0, 0, null, null) == L.ERR_UNSUPPORTED
-    assert lib.qsgb_apply_ptm2(one, two, two, 9, 9, 9, 9, 1, 1, 1,
+    assert lib.qsgb_apply_ptm2(one, two, two, 81, 81, 81, 81, 1, 1, 1,
                                L.PTM_HOST, L.F64, 0, 0, null,
+                               null) == L.ERR_UNSUPPORTED
+    assert lib.qsgb_apply_ptm2(one, two, two, 9, 9, 9, 9, 1, 1, 1,
+                               L.PTM_HOST | L.PTM_NOJIT, L.F64, 0, 0, null,
                                null) == L.ERR_UNSUPPORTED
     # gathers
     assert lib.qsgb_take_axis(one, one, L.F64, 1, 4, 1, L.i32_array([0]), 1,

@@ -102,9 +102,10 @@ def test_2q_every_ordered_pair(density):
     rng = np.random.default_rng(12)
     n = 6
     bases = [B.general(2)] * n
+    mask = rng.random((4, 4, 4, 4)) < density  # one sparsity pattern
     for q0, q1 in itertools.permutations(range(n), 2):
         pv = rand_pv(rng, (4,) * n)
-        ptm = rand_ptm(rng, (4, 4, 4, 4), density)
+        ptm = rand_ptm(rng, (4, 4, 4, 4)) * mask
         s = GB(bases, pv)
         s.apply_ptm(ptm, q0, q1)
         assert_close_dot(s.to_pv(), O.apply_ptm(pv, ptm, q0, q1),
@@ -153,6 +154,39 @@ def test_two_qutrit_81x81_dense_and_cphase():
         s.apply_ptm(ptm, *qs)
         assert_close_dot(s.to_pv(), O.apply_ptm(pv, ptm, *qs),
                          O.apply_ptm(np.abs(pv), np.abs(ptm), *qs))
+
+
+@pytest.mark.parametrize('arith', [0, 1, 2])
+def test_specialised_and_generic_kernels_agree(arith):
+    """The run-time specialised kernel and the generic one give the same
+    result (and match the oracle) on rectangular, swapped and transposed
+    applications, pairs and single groups, FP64 and FP32."""
+    rng = np.random.default_rng(21)
+    dev = torch.device('cuda')
+    cases = [((4, 4, 4, 4, 4), (1, 3), (4, 4, 4, 4), False),
+             ((4, 4, 4, 4, 4), (4, 0), (4, 4, 4, 4), False),
+             ((4, 3, 4, 9), (3, 1), (9, 3, 9, 3), False),
+             ((4, 3, 4, 9), (2,), (1, 4), False),
+             ((9, 9, 9), (0, 2), (9, 9, 9, 9), False),
+             ((4, 4, 4, 4), (2, 0), (4, 4, 4, 4), True)]
+    for shape, qs, pshape, tr in cases:
+        x = rand_pv(rng, shape)
+        ptm = rand_ptm(rng, pshape, 0.4)
+        ref = (O.apply_ptm_transposed(x, ptm, *qs) if tr
+               else O.apply_ptm(x, ptm, *qs))
+        absref = (O.apply_ptm_transposed(np.abs(x), np.abs(ptm), *qs) if tr
+                  else O.apply_ptm(np.abs(x), np.abs(ptm), *qs))
+        xt = torch.from_numpy(x).to(dev)
+        outs = []
+        for jit in (True, False):
+            y = torch.ops.qsgb.apply_ptm(xt, torch.from_numpy(ptm), list(qs),
+                                         arith, ptm.size, tr, jit)
+            outs.append(y.cpu().numpy())
+            assert_close_dot(outs[-1], ref, absref)
+        y32 = torch.ops.qsgb.apply_ptm(xt.float(), torch.from_numpy(ptm),
+                                       list(qs), 3, ptm.size, tr, True)
+        np.testing.assert_allclose(y32.cpu().numpy(), ref, rtol=1e-4,
+                                   atol=1e-5)
 
 
 def test_transposed_apply_and_ptm_grad_ops():
