@@ -313,8 +313,10 @@ def run_gb300(args):
             'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': ms / args.steps, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
-            'arith': 'float-float (48-bit significand) on FP32 pipes; '
-                     'single-term rows one FP64 multiply',
+            'arith': 'per PTM row: native FP64 FMA or float-float (48-bit '
+                     'significand) on the FP32 pipes, chosen by a pipe cost '
+                     'model; kernel specialised to the PTM sparsity pattern '
+                     'at run time (NVRTC, cached)',
             'data': 'synthetic',
             'config': {'workload': WORKLOAD, 'n_qubits': N_QUBITS,
                        'entries': n_entries, 'apps_per_step': APPS_PER_STEP,
@@ -324,7 +326,8 @@ def run_gb300(args):
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak,
                          'unit': 'GB/s', 'frac': achieved / peak,
                          'peak_kind': peak_kind, 'traffic': traffic,
-                         'kernel': 'apply_ptm_kernel<double, DF64> (2q)',
+                         'kernel': 'qsgb_jit (apply kernel specialised to '
+                                   'the noisy-CZ sparsity pattern, 2q)',
                          'bytes_per_launch': bytes_per_app,
                          'launch_ms': launch_ms},
             'cpu_baseline': cpu,

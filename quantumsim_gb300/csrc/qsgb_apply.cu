@@ -569,7 +569,7 @@ int launch_apply(ApplyParams& p, cudaStream_t stream) {
 // Row modes for the specialised kernel under QSGB_ARITH_AUTO: rows in
 // ascending term count are computed in FP64 while that lowers the larger of
 // the estimated times per group (SM clock cycles) of HBM traffic, the FP64
-// pipe (~1.9 ops/clk), the integer pipe (64 lanes/clk: ~16 ops per split
+// pipe (~1.6 ops/clk sustained in these kernels), the integer pipe (64 lanes/clk: ~16 ops per split
 // input, ~30 per float-float row result) and instruction issue (128/clk;
 // ~12 per float-float term).
 void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, size_t esz, std::vector<int>& mode) {
@@ -615,7 +615,7 @@ void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, s
       }
     issue += 2.0 * (n_used + kout);
     const double hbm = (double)(kin + kout) * (double)esz / 23.0;
-    return std::max(std::max(hbm, dp / 1.9), std::max(alu / 64.0, issue / 128.0));
+    return std::max(std::max(hbm, dp / 1.6), std::max(alu / 64.0, issue / 128.0));
   };
   std::vector<int> m = mode;
   double best = cost(m);
@@ -632,8 +632,8 @@ void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, s
 }
 
 // Returns QSGB_ERR_UNSUPPORTED when the specialised path does not apply.
-int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_in, int64_t db_in, int flags,
-            int dtype, int arith, bool pair, ApplyParams& p, cudaStream_t stream) {
+int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_in, int64_t db_in, int64_t Z,
+            int flags, int dtype, int arith, bool pair, ApplyParams& p, cudaStream_t stream) {
   if (!(flags & QSGB_PTM_HOST) || (flags & QSGB_PTM_NOJIT) || !jit::available()) return QSGB_ERR_UNSUPPORTED;
   const int kin = (int)(da_in * db_in), kout = (int)(da_out * db_out);
   if (kin > 81 || kout > 81) return QSGB_ERR_UNSUPPORTED;
@@ -663,6 +663,17 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
   spec.db_out = (int)db_out;
   spec.pair = pair;
   spec.f32 = dtype == QSGB_F32;
+  // Z == 1: the db inputs (outputs) of a group along the less significant
+  // target are contiguous; move them with 2- or 4-wide vector accesses
+  auto vwidth = [&](int64_t db, const void* ptr) {
+    const size_t esz = dtype == QSGB_F64 ? 8 : 4;
+    if (Z != 1) return 1;
+    for (int w : {4, 2})
+      if (db % w == 0 && (uintptr_t)ptr % (w * esz) == 0) return w;
+    return 1;
+  };
+  spec.vin = vwidth(db_in, p.in);
+  spec.vout = vwidth(db_out, p.out);
   spec.cols.assign(kout, {});
   for (int r = 0; r < kout; ++r)
     for (int k = 0; k < kin; ++k)
@@ -750,7 +761,7 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
   // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)
-  const int js = try_jit(ptm, da_out, db_out, da_in, db_in, flags, dtype, arith, pair, p, s);
+  const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s);
   if (js != QSGB_ERR_UNSUPPORTED) return js;
   // 2. generic kernel; a host PTM travels inside its launch parameters
   if (flags & QSGB_PTM_HOST) {

@@ -106,6 +106,25 @@ std::string gen_source(const Spec& s) {
   src += buf;
   const char* V = s.pair ? (f32 ? "qv2f" : "qv2d") : scal;
   src += "#define QH(v) __int_as_float(__double2hiint(v))\n#define QL(v) __int_as_float(__double2loint(v))\n";
+  // vector loads / stores along the less significant target when Z == 1
+  {
+    const char* ty = f32 ? "f32" : "f64";
+    const char* cs = f32 ? "f" : "d";
+    std::snprintf(buf, sizeof buf,
+                  "__device__ __forceinline__ void qld2(const %s* q, %s& a, %s& b) {\n"
+                  "  asm(\"ld.global.nc.v2.%s {%%0,%%1}, [%%2];\" : \"=%s\"(a), \"=%s\"(b) : \"l\"(q)); }\n"
+                  "__device__ __forceinline__ void qld4(const %s* q, %s& a, %s& b, %s& c, %s& d) {\n"
+                  "  asm(\"ld.global.nc.v4.%s {%%0,%%1,%%2,%%3}, [%%4];\" : \"=%s\"(a), \"=%s\"(b), \"=%s\"(c), "
+                  "\"=%s\"(d) : \"l\"(q)); }\n"
+                  "__device__ __forceinline__ void qst2(%s* q, %s a, %s b) {\n"
+                  "  asm volatile(\"st.global.v2.%s [%%0], {%%1,%%2};\" :: \"l\"(q), \"%s\"(a), \"%s\"(b) : \"memory\"); }\n"
+                  "__device__ __forceinline__ void qst4(%s* q, %s a, %s b, %s c, %s d) {\n"
+                  "  asm volatile(\"st.global.v4.%s [%%0], {%%1,%%2,%%3,%%4};\" :: \"l\"(q), \"%s\"(a), \"%s\"(b), "
+                  "\"%s\"(c), \"%s\"(d) : \"memory\"); }\n",
+                  scal, scal, scal, ty, cs, cs, scal, scal, scal, scal, scal, ty, cs, cs, cs, cs, scal, scal, scal, ty, cs,
+                  cs, scal, scal, scal, scal, scal, ty, cs, cs, cs, cs);
+    src += buf;
+  }
   std::snprintf(buf, sizeof buf,
                 "extern \"C\" __global__ void __launch_bounds__(128) qsgb_jit(const __grid_constant__ P p) {\n"
                 "  typedef %s V;\n"
@@ -131,11 +150,29 @@ std::string gen_source(const Spec& s) {
       if (s.mode[r] == kModeDF) split[k] = 1;
     }
   const char* lanes[2] = {s.pair ? ".x" : "", ".y"};
-  for (int k = 0; k < s.kin; ++k) {
-    if (!used[k]) continue;
-    const int ka = k / s.db_in, kb = k % s.db_in;
-    std::snprintf(buf, sizeof buf, "    const V x%d = in[bi + %dLL * p.h.sai + %dLL * p.h.sbi];\n", k, ka, kb);
-    src += buf;
+  if (s.vin > 1) {  // Z == 1: runs of vin inputs along kb are contiguous
+    for (int k0 = 0; k0 < s.kin; k0 += s.vin) {
+      bool any = false;
+      for (int j = 0; j < s.vin; ++j) any |= used[k0 + j] != 0;
+      if (!any) continue;
+      const int ka = k0 / s.db_in, kb = k0 % s.db_in;
+      std::string vars;
+      for (int j = 0; j < s.vin; ++j) {
+        std::snprintf(buf, sizeof buf, "    V x%d;\n", k0 + j);
+        src += buf;
+        vars += ", x" + std::to_string(k0 + j);
+      }
+      std::snprintf(buf, sizeof buf, "    qld%d((const V*)p.h.in + bi + %dLL * p.h.sai + %d%s);\n", s.vin, ka, kb,
+                    vars.c_str());
+      src += buf;
+    }
+  } else {
+    for (int k = 0; k < s.kin; ++k) {
+      if (!used[k]) continue;
+      const int ka = k / s.db_in, kb = k % s.db_in;
+      std::snprintf(buf, sizeof buf, "    const V x%d = in[bi + %dLL * p.h.sai + %dLL * p.h.sbi];\n", k, ka, kb);
+      src += buf;
+    }
   }
   for (int k = 0; k < s.kin; ++k) {
     if (!split[k]) continue;
@@ -144,6 +181,10 @@ std::string gen_source(const Spec& s) {
                     l, k, lanes[l], k, l, k, l);
       src += buf;
     }
+  }
+  for (int r = 0; r < s.kout; ++r) {
+    std::snprintf(buf, sizeof buf, "    V y%d;\n", r);
+    src += buf;
   }
   int ci = 0;
   for (int r = 0; r < s.kout; ++r) {
@@ -188,16 +229,27 @@ std::string gen_source(const Spec& s) {
         vals[l] = "qsgb_df_to_double(s" + std::to_string(l) + ", c" + std::to_string(l) + ")";
       }
     }
-    std::snprintf(buf, sizeof buf, "      V y; ");
-    src += buf;
     if (s.pair) {
-      src += "y.x = " + vals[0] + "; y.y = " + vals[1] + ";\n";
+      src += "      y" + std::to_string(r) + ".x = " + vals[0] + "; y" + std::to_string(r) + ".y = " + vals[1] + ";\n";
     } else {
-      src += "y = " + vals[0] + ";\n";
+      src += "      y" + std::to_string(r) + " = " + vals[0] + ";\n";
     }
-    std::snprintf(buf, sizeof buf, "      out[bo + %dLL * p.h.sao + %dLL * p.h.sbo] = y;\n    }\n", ra, rb);
-    src += buf;
+    src += "    }\n";
     ci += (int)cols.size();
+    // store as soon as a row (or a vector of vout rows) is complete
+    if (s.vout > 1) {
+      if ((r + 1) % s.vout == 0) {
+        const int r0 = r + 1 - s.vout;
+        std::string vars;
+        for (int j = 0; j < s.vout; ++j) vars += ", y" + std::to_string(r0 + j);
+        std::snprintf(buf, sizeof buf, "    qst%d((V*)p.h.out + bo + %dLL * p.h.sao + %d%s);\n", s.vout,
+                      r0 / s.db_out, r0 % s.db_out, vars.c_str());
+        src += buf;
+      }
+    } else {
+      std::snprintf(buf, sizeof buf, "    out[bo + %dLL * p.h.sao + %dLL * p.h.sbo] = y%d;\n", ra, rb, r);
+      src += buf;
+    }
   }
   src += "  }\n  if (bad && p.h.status) atomicOr(p.h.status, 1u);\n}\n";
   return src;

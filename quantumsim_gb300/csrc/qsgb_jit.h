@@ -19,6 +19,8 @@ struct Spec {
   int db_in, db_out;   // less significant target dims (index split k = ka*db + kb)
   bool pair;           // items are (z, z+1) pairs (16-byte accesses)
   bool f32;            // FP32 storage
+  int vin, vout;       // 1, or 2 / 4: vector width of loads / stores along
+                       // the less significant target (only when Z == 1)
   std::vector<int> mode;               // per output row
   std::vector<std::vector<int>> cols;  // per output row: input indices of its terms
   int n_coef() const;
