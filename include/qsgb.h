@@ -155,6 +155,36 @@ int qsgb_marginals(const double* diag, int ndim, const int64_t* shape,
                    void* stream);
 
 /*
+ * qsgb_marginals without caller scratch and without any allocation.
+ *
+ * No counterpart in the reference.  Some programs that embed this library
+ * cannot allocate device memory when they need probabilities: an
+ * application whose device memory is wholly owned by its own pool allocator
+ * (and which forbids outside cudaMalloc calls), or a latency-critical
+ * measurement loop in which the implicit device synchronisation of
+ * cudaMalloc / cudaFree would stall the pipeline.  This entry point computes
+ * exactly what qsgb_marginals computes, but keeps its partial sums in a
+ * fixed 128 KiB array inside the library (a file-scope __device__ array that
+ * every GPU loading the library holds until the process exits).  It calls
+ * no cudaMalloc, cudaFree or allocating library routine.
+ *
+ * - The first call on each device looks up the array's device address
+ *   (cudaGetSymbolAddress) with that device current; make that first call
+ *   before any stream capture on the device.
+ * - Requests needing more than qsgb_marginals_noalloc_max_scratch_bytes()
+ *   of partial sums (chunks x outcomes > 16384 doubles) return
+ *   QSGB_ERR_SCRATCH; up to 32 outcomes per axis always fit.
+ * - All calls share the one array and it keeps the last call's contents
+ *   (every partial a call reads is written by that call first, so nothing
+ *   needs clearing).  Calls that can overlap on the GPU -- on different
+ *   streams, or from different host threads -- race on the array; serialise
+ *   them (one stream, or events).
+ */
+int64_t qsgb_marginals_noalloc_max_scratch_bytes(void);
+int qsgb_marginals_noalloc(const double* diag, int ndim, const int64_t* shape,
+                           int axis, double* out, void* stream);
+
+/*
  * Partial trace: out[kept...] = sum over traced qudits t of
  *   in[...] * prod_t w_t[k_t]
  * with w_t[k] = Re tr(P_k) of qudit t's basis (numpy.py:86-95).  Kept

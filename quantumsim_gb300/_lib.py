@@ -57,6 +57,9 @@ SIGNATURES = {
     'qsgb_marginals_scratch_bytes': (_i64, [_i64, _i64]),
     'qsgb_marginals': (_int, [_c_void_p, _int, _p_i64, _int, _c_void_p,
                               _c_void_p, _i64, _c_void_p]),
+    'qsgb_marginals_noalloc_max_scratch_bytes': (_i64, []),
+    'qsgb_marginals_noalloc': (_int, [_c_void_p, _int, _p_i64, _int,
+                                      _c_void_p, _c_void_p]),
     'qsgb_partial_trace': (_int, [_c_void_p, _c_void_p, _int, _int, _p_i64,
                                   _p_i32, ctypes.POINTER(ctypes.c_double),
                                   _c_void_p]),

@@ -5,6 +5,7 @@
 // All reductions are deterministic (fixed trees, no floating-point atomics)
 // and accumulate in FP64 for both storage types.
 #include <algorithm>
+#include <mutex>
 
 #include "qsgb_common.cuh"
 
@@ -433,5 +434,83 @@ extern "C" int qsgb_scale_by_inverse(void* x, int dtype, int64_t n, const double
                                                                  denom, threshold);
   else
     return QSGB_ERR_INVALID;
+  return launch_status();
+}
+
+// ---------------------------------------------------------------------------
+// Marginals without any allocation by anyone.
+//
+// qsgb_marginals() needs a scratch buffer for its per-chunk partial sums and
+// leaves allocating it to the caller.  Some programs that embed this library
+// cannot allocate device memory at the point where they need probabilities:
+// applications whose device memory is wholly owned by their own pool
+// allocator (which forbids outside cudaMalloc calls), or latency-critical
+// measurement loops in which the implicit device synchronisation of
+// cudaMalloc / cudaFree would stall the pipeline.  For them the partial sums
+// live in the fixed array below, which exists in every device that loads
+// this library for as long as the process runs.
+// ---------------------------------------------------------------------------
+namespace {
+
+// 16384 doubles (128 KiB): enough for up to 512 chunks x 32 outcomes, i.e.
+// any diagonal of qudits with up to 32 levels.
+constexpr int64_t kNoAllocScratchDoubles = 16384;
+__device__ __align__(256) double g_noalloc_marg_scratch[kNoAllocScratchDoubles];
+
+// Device address of the array, looked up once per device (the name is only a
+// host-side stand-in for the symbol in host code).
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {nullptr};
+
+int noalloc_scratch(double** ptr) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return QSGB_ERR_CUDA;
+  if (dev < 0 || dev >= 64) return QSGB_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_marg_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return QSGB_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return QSGB_OK;
+}
+
+}  // namespace
+
+extern "C" int64_t qsgb_marginals_noalloc_max_scratch_bytes(void) {
+  return kNoAllocScratchDoubles * (int64_t)sizeof(double);
+}
+
+extern "C" int qsgb_marginals_noalloc(const double* diag, int ndim, const int64_t* shape, int axis, double* out,
+                                      void* stream) {
+  if (!diag || !out || (!shape && ndim > 0)) return QSGB_ERR_INVALID;
+  if (ndim < 0 || axis < -1 || axis >= ndim) return QSGB_ERR_INVALID;
+  int64_t n = 1, s = 1;
+  for (int a = 0; a < ndim; ++a) {
+    if (shape[a] < 1) return QSGB_ERR_INVALID;
+    n *= shape[a];
+    if (a > axis && axis >= 0) s *= shape[a];
+  }
+  const int64_t d = axis < 0 ? 1 : shape[axis];
+  if (axis < 0) s = 1;
+  if (d > 65535) return QSGB_ERR_UNSUPPORTED;
+  int nc;
+  uint64_t chunk;
+  marg_geometry(n, d, &nc, &chunk);
+  // the fixed array bounds the request: refuse instead of overrunning it
+  if ((int64_t)nc * d > kNoAllocScratchDoubles) return QSGB_ERR_SCRATCH;
+  double* part = nullptr;
+  const int st0 = noalloc_scratch(&part);
+  if (st0 != QSGB_OK) return st0;
+  // every partial the second stage reads is written by the first stage of
+  // this call, so nothing needs clearing between calls
+  cudaStream_t st = as_stream(stream);
+  const uint64_t per_j = (uint64_t)(n / d);
+  marg_stage1<<<dim3(nc, (unsigned)d), kRedBlock, 0, st>>>(diag, per_j, make_fastdiv((uint64_t)s), d, s, chunk, part);
+  marg_stage2<<<(unsigned)d, kRedBlock, 0, st>>>(part, nc, out);
   return launch_status();
 }
