@@ -361,6 +361,37 @@ def _time_app(s, ptm, qs, bytes_per_app, reps=3):
     return round(bytes_per_app * reps / (a.elapsed_time(b) / 1e3) / 1e9, 1)
 
 
+def run_profile_case(args):
+    """Small workload for ncu captures: a 12-qubit FP64 state (134 MB, larger
+    than L2); one circuit layer (12 noisy rotations + 3 noisy CZs), then 3x
+    [noisy CZ on (3, 7), noisy rotation on qubit 5, dense 16x16 PTM on
+    (3, 7), noisy CZ on the last two qubits].
+    Launch order: 15 setup launches, then 4 per repetition."""
+    import numpy as np
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads
+    n = args.profile_qubits
+    s = qg.PauliVectorGB300([bases.general(2)] * n, force=True)
+    rng = np.random.default_rng(3)
+    t1, t2 = workloads.coherence_times(rng, n)
+    for op in workloads.config1_layer(rng, n, t1, t2, 3):
+        s.apply_ptm(op[1], *op[2])
+    cz = workloads.noisy_cz(rng, (3, 7), t1, t2)
+    r1 = workloads.noisy_1q(rng, t1[5], t2[5])
+    dense = rng.standard_normal((4, 4, 4, 4)) * 0.25
+    last = workloads.noisy_cz(rng, (n - 2, n - 1), t1, t2)
+    for _ in range(3):
+        s.apply_ptm(cz, 3, 7)
+        s.apply_ptm(r1, 5)
+        s.apply_ptm(dense, 3, 7)
+        s.apply_ptm(last, n - 2, n - 1)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_case': n, 'trace': s.trace()}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
     ap.add_argument('--gpus', type=int, default=1)
@@ -372,7 +403,13 @@ def main():
     ap.add_argument('--no-sweep', action='store_true')
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
+    ap.add_argument('--profile-case', action='store_true',
+                    help='run the small ncu profiling workload and exit')
+    ap.add_argument('--profile-qubits', type=int, default=12)
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.warmup < 3 and args.impl == 'gb300':
         print('warning: fewer than 3 warm-up steps', file=sys.stderr)
     if args.impl == 'reference':
