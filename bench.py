@@ -398,7 +398,7 @@ def main():
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--cpu-apps', type=int, default=4)
+    ap.add_argument('--cpu-apps', type=int, default=16)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-sweep', action='store_true')
     ap.add_argument('--traffic', type=float, default=0.0,
