@@ -37,6 +37,11 @@ sys.path.insert(0, ROOT)
 
 N_QUBITS = 14
 APPS_PER_STEP = 7
+# DRAM bytes (read + write) of one 14-qubit noisy-CZ launch, from the ncu
+# capture summarised in profiles/apply_jit_traffic_13q.md (13-qubit launch:
+# 536.9 MB read, 486.8 MB written; reads scale 4x, writes 4x minus the ~50 MB
+# still in L2 at kernel end)
+TRAFFIC_14Q = 4 * 536.9e6 + 4 * 536.9e6 - 50e6
 METRIC = ('2q-PTM apps/s & HBM GB/s (14q fp64); batched fp32 fwd+adjoint vs '
           'plain, err<1e-6')
 WORKLOAD = ('14-qubit FP64 Pauli vector (4^14 entries, 2.15 GB); step = 7 '
@@ -244,7 +249,7 @@ def run_gb300(args):
     launch_ms = sum(a.elapsed_time(b) for a, b in per) / len(per)
     peak, peak_kind = _peaks()
     achieved = bytes_per_app / (launch_ms / 1e3) / 1e9
-    traffic = args.traffic if args.traffic else None
+    traffic = args.traffic if args.traffic else TRAFFIC_14Q
 
     # ---- per-target breakdown (1q positions, 2q stride classes)
     per_target = {}
