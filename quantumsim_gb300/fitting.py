@@ -1,0 +1,148 @@
+"""Differentiable noisy-circuit model: gradients of a measurement loss with
+respect to physical gate parameters, through the GB300 adjoint kernels.
+
+The circuit is the CPU-runnable workload family (per layer a rotation on
+every qubit followed by amplitude + phase damping over the 20 ns gate time,
+then CZs on line neighbours), with trainable physical parameters:
+
+* ``angle_offset`` (n_groups, n): added to the seeded rotation angle of the
+  gate on qubit q in every layer l with l % n_groups == g;
+* ``t1``, ``t2`` (n,): coherence times in microseconds, setting the damping
+  rates (:func:`quantumsim_gb300.ptm.damping_rates`);
+* ``cz_phase`` (n - 1,): conditional-phase error of the CZ on edge (i, i+1).
+
+With n = 10 and 22 offset groups this is 220 + 10 + 10 + 9 = 249
+parameters.  The loss is KL(target || model) over the diagonal (computational
+basis probabilities); the target is the same circuit at perturbed
+parameters.  ``loss(..., backend='gb300')`` runs the state through the
+``ApplyPTM`` autograd function (adjoint kernels, checkpoints every
+`checkpoint_every` layers); ``backend='einsum'`` is the float64
+``torch.einsum`` autograd reference used by the tests.
+"""
+import math
+
+import numpy as np
+import torch
+
+from . import bases as _bases
+from . import ptm as P
+from .autograd import apply_ptm_diff, checkpointed, diagonal_diff
+
+T_GATE = 20e-9
+
+
+class NoisyCircuitModel:
+    def __init__(self, n_qubits=10, n_layers=40, n_groups=22, seed=3):
+        self.n = n_qubits
+        self.n_layers = n_layers
+        self.n_groups = n_groups
+        rng = np.random.default_rng(seed)
+        self.axes = [['xyz'[i] for i in rng.integers(3, size=n_qubits)]
+                     for _ in range(n_layers)]
+        self.base_angles = torch.from_numpy(
+            rng.uniform(0, 2 * math.pi, (n_layers, n_qubits)))
+        t1 = rng.uniform(20, 60, n_qubits)
+        t2 = rng.uniform(10, t1)
+        self.init = {
+            'angle_offset': torch.zeros(n_groups, n_qubits,
+                                        dtype=torch.float64),
+            't1': torch.from_numpy(t1),
+            't2': torch.from_numpy(t2),
+            'cz_phase': torch.zeros(n_qubits - 1, dtype=torch.float64),
+        }
+        self.basis = _bases.general(2)
+
+    @property
+    def n_params(self):
+        return sum(v.numel() for v in self.init.values())
+
+    def params(self, requires_grad=True):
+        return {k: v.clone().requires_grad_(requires_grad)
+                for k, v in self.init.items()}
+
+    def perturbed(self, scale=0.05, seed=11):
+        rng = np.random.default_rng(seed)
+        out = {}
+        for k, v in self.init.items():
+            noise = torch.from_numpy(rng.normal(0, scale, v.shape))
+            out[k] = v + (noise * v.abs().clamp(min=1.0) if k in ('t1', 't2')
+                          else noise)
+        return out
+
+    def pairs(self, layer):
+        off = layer % 2
+        return [(i, i + 1) for i in range(off, self.n - 1, 2)]
+
+    def build_ptms(self, p):
+        """All PTMs of the circuit (float64 CPU tensors, differentiable)."""
+        n, nl = self.n, self.n_layers
+        groups = torch.arange(nl) % self.n_groups
+        angles = self.base_angles + p['angle_offset'][groups]
+        axes = [ax for row in self.axes for ax in row]
+        rot = P.rotations_batched(axes, angles.reshape(-1), self.basis)
+        gamma, lam = P.damping_rates(p['t1'] * 1e-6, p['t2'] * 1e-6, T_GATE)
+        damp = P.amp_phase_damping_batched(gamma, lam, self.basis)
+        one_q = (damp[None] @ rot.reshape(nl, n, 4, 4))
+        cz = P.cphase_batched(math.pi + p['cz_phase'], self.basis)
+        return one_q, cz
+
+    def layers(self, p, apply_fn):
+        one_q, cz = self.build_ptms(p)
+        fns = []
+        for l in range(self.n_layers):
+            ptms1 = [one_q[l, q] for q in range(self.n)]
+            ptms2 = [(cz[i], (i, i + 1)) for i, _ in self.pairs(l)]
+
+            def layer(x, ptms1=ptms1, ptms2=ptms2):
+                for q, pt in enumerate(ptms1):
+                    x = apply_fn(x, pt, (q,))
+                for pt, qs in ptms2:
+                    x = apply_fn(x, pt, qs)
+                return x
+            fns.append(layer)
+        return fns
+
+    def initial_state(self, device, dtype):
+        x = torch.zeros((4,) * self.n, dtype=dtype, device=device)
+        x[(0,) * self.n] = 1
+        return x
+
+    def probabilities(self, p, backend='gb300', dtype=torch.float64,
+                      checkpoint_every=8, device=None):
+        if backend == 'gb300':
+            device = device or torch.device('cuda')
+            x = self.initial_state(device, dtype)
+            x = checkpointed(
+                self.layers(p, lambda s, pt, qs: apply_ptm_diff(s, pt, *qs)),
+                x, checkpoint_every)
+            return diagonal_diff(x, [self.basis] * self.n)
+        device = device or torch.device('cpu')
+        x = self.initial_state(device, torch.float64)
+        for f in self.layers(p, _einsum_apply):
+            x = f(x)
+        idx = [self.basis.computational_basis_indices[i] for i in range(2)]
+        d = x
+        for q in range(self.n):
+            d = d.index_select(q, torch.tensor(idx, device=device))
+        return d.reshape(-1)
+
+    def loss(self, p, target, **kw):
+        prob = self.probabilities(p, **kw)
+        t = target.to(prob.device)
+        return torch.sum(t * (torch.log(t) - torch.log(prob)))
+
+
+def _einsum_apply(x, ptm, qs):
+    """Float64 torch.einsum reference of apply_ptm (autograd-capable)."""
+    ptm = ptm.to(x.device)
+    n = x.dim()
+    k = len(qs)
+    letters = 'abcdefghijklmnopqrstuvwxyz'
+    xi = list(letters[:n])
+    outs = [letters[n + i] for i in range(k)]
+    yi = list(xi)
+    for q, o in zip(qs, outs):
+        yi[q] = o
+    spec = '{},{}->{}'.format(''.join(outs + [xi[q] for q in qs]),
+                              ''.join(xi), ''.join(yi))
+    return torch.einsum(spec, ptm, x)

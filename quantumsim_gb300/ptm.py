@@ -221,3 +221,77 @@ def selection_ptm(d_in, indices):
     """Rectangular PTM keeping the Pauli elements `indices` (the oracle form
     of reduce_basis / project)."""
     return np.eye(d_in)[list(indices)]
+
+
+# ----------------------------------------------------------------- batched
+def kraus_to_ptm_batched(kraus, bases_in, bases_out=None):
+    """PTMs of a batch of channels: kraus (G, n_kraus, D, D) complex ->
+    (G, d_out..., d_in...) float64."""
+    bases_out = bases_out or bases_in
+    k = torch.as_tensor(kraus).to(_CDTYPE)
+    p_out = _basis_tensor(bases_out, k.device)
+    p_in = _basis_tensor(bases_in, k.device)
+    ptm = torch.einsum('xij,gkjl,ylm,gkim->gxy', p_out, k, p_in, k.conj()).real
+    shape = ([k.shape[0]] + [b.dim_pauli for b in bases_out] +
+             [b.dim_pauli for b in bases_in])
+    return ptm.reshape(shape)
+
+
+def rotations_batched(axes, angles, basis=None):
+    """Rotation PTMs for many gates at once: axes is a sequence of 'x', 'y',
+    'z' and angles a (G,) tensor; returns (G, d, d)."""
+    basis = basis or _bases.general(2)
+    a = angles.to(torch.float64)
+    c = torch.cos(a / 2).to(_CDTYPE)
+    s = torch.sin(a / 2).to(_CDTYPE)
+    j = torch.tensor(1j, dtype=_CDTYPE, device=a.device)
+    e = torch.exp(-j * a.to(_CDTYPE) / 2)
+    zero = torch.zeros_like(c)
+    kx = torch.stack([torch.stack([c, -j * s], -1),
+                      torch.stack([-j * s, c], -1)], -2)
+    ky = torch.stack([torch.stack([c, -s], -1), torch.stack([s, c], -1)], -2)
+    kz = torch.stack([torch.stack([e, zero], -1),
+                      torch.stack([zero, e.conj()], -1)], -2)
+    code = torch.tensor([{'x': 0, 'y': 1, 'z': 2}[ax] for ax in axes],
+                        device=a.device)
+    k = torch.where((code == 0)[:, None, None], kx,
+                    torch.where((code == 1)[:, None, None], ky, kz))
+    d = basis.dim_hilbert
+    if d > 2:  # act in the 0-1 subspace
+        full = torch.eye(d, dtype=_CDTYPE, device=a.device).repeat(
+            len(axes), 1, 1)
+        full[:, :2, :2] = k
+        k = full
+    return kraus_to_ptm_batched(k[:, None], (basis,))
+
+
+def amp_phase_damping_batched(gamma, lam, basis=None):
+    """(Q,) rates -> (Q, 4, 4): amplitude then phase damping per qubit."""
+    basis = basis or _bases.general(2)
+    g = gamma.to(torch.float64)
+    lm = lam.to(torch.float64)
+    z = torch.zeros_like(g)
+    one = torch.ones_like(g)
+
+    def mat(a, b, c, d):
+        return torch.stack([torch.stack([a, b], -1), torch.stack([c, d], -1)],
+                           -2)
+
+    amp = torch.stack([mat(one, z, z, torch.sqrt(1 - g)),
+                       mat(z, torch.sqrt(g), z, z)], 1)
+    ph = torch.stack([mat(one, z, z, torch.sqrt(1 - lm)),
+                      mat(z, z, z, torch.sqrt(lm))], 1)
+    pa = kraus_to_ptm_batched(amp, (basis,))
+    pp = kraus_to_ptm_batched(ph, (basis,))
+    return pp @ pa
+
+
+def cphase_batched(angles, basis=None):
+    """(E,) conditional phases -> (E, 4, 4, 4, 4) cphase PTMs."""
+    basis = basis or _bases.general(2)
+    a = angles.to(torch.float64)
+    j = torch.tensor(1j, dtype=_CDTYPE, device=a.device)
+    one = torch.ones_like(a).to(_CDTYPE)
+    diag = torch.stack([one, one, one, torch.exp(j * a.to(_CDTYPE))], -1)
+    return kraus_to_ptm_batched(torch.diag_embed(diag)[:, None],
+                                (basis, basis))
