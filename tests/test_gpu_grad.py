@@ -73,7 +73,7 @@ def test_model_gradients_small_match_reference_and_fd():
         p = m.params()
         loss = m.loss(p, target, backend=backend, checkpoint_every=3)
         loss.backward()
-        out[backend] = (float(loss), _flat([p[k].grad for k in names]))
+        out[backend] = (loss.item(), _flat([p[k].grad for k in names]))
     assert out['gb300'][0] == pytest.approx(out['einsum'][0], rel=1e-11)
     np.testing.assert_allclose(out['gb300'][1], out['einsum'][1], rtol=1e-8,
                                atol=1e-12)
@@ -117,7 +117,7 @@ def test_model_full_size_249_parameters():
             kw['dtype'] = dtype
         loss = m.loss(p, target, checkpoint_every=8, **kw)
         loss.backward()
-        res[backend] = (float(loss), _flat([p[k].grad for k in names]))
+        res[backend] = (loss.item(), _flat([p[k].grad for k in names]))
     g64, gref, g32 = res['gb300'][1], res['einsum'][1], res['gb300_f32'][1]
     np.testing.assert_allclose(g64, gref, rtol=1e-8, atol=1e-12)
     scale = gref.abs().max()
