@@ -228,6 +228,70 @@ int qsgb_ptm_grad2(const void* x_in, const void* g_out, double* dptm,
                    int dtype, void* scratch, int64_t scratch_bytes,
                    void* stream);
 
+/* ===================================================================
+ * Batched execution: many independent circuits (FP32 Pauli vectors of
+ * qubits in the full 4-element basis) forward AND adjoint in ONE persistent
+ * launch.  No counterpart in the reference (it runs one circuit at a time
+ * through Python).  The program is a list of stages; a stage is a list of
+ * work items whose instances are independent; persistent blocks take items
+ * from a per-stage counter and meet at a grid barrier between stages.
+ * =================================================================== */
+#define QSGB_BOP_INIT 1     /* x[beg:end) = |0..0> (1 at element 0, else 0) */
+#define QSGB_BOP_ZERO_G 2   /* g[beg:end) = 0 */
+#define QSGB_BOP_APPLY 3    /* x = P x on groups [beg, end), in place */
+#define QSGB_BOP_SAVE 4     /* ckpt[ptm][beg:end) = x[beg:end) */
+#define QSGB_BOP_RESTORE 5  /* x[beg:end) = ckpt[ptm][beg:end) */
+#define QSGB_BOP_LOSS 6     /* whole instance: prob = diag(x) (FP64),
+                               loss = KL(target || prob), g[diag] = dloss/dprob */
+#define QSGB_BOP_ADJOINT 7  /* groups [beg, end): x = P^-1 x, g = P^T g, and
+                               grad_partial[slot] = sum g_out (x) x_in (FP64) */
+#define QSGB_BOP_GRADSUM 8  /* grad[ptm] = sum of grad_partial[beg:end) */
+
+typedef struct {
+  float* x;           /* state, 4^n floats */
+  float* g;           /* adjoint state, 4^n floats */
+  float* ckpt;        /* checkpoint slots, 4^n floats each */
+  int64_t size;       /* 4^n */
+  int32_t n_qubits;   /* 1 <= n <= 16 */
+  int32_t diag_offset;/* offset of this instance's 2^n entries in target/prob */
+} qsgb_batch_instance;
+
+typedef struct {
+  int32_t op;         /* QSGB_BOP_* */
+  int32_t inst;       /* instance index */
+  int32_t q0, q1;     /* target qubits, q0 < q1; q1 = -1 for one qubit */
+  int32_t ptm;        /* PTM index (APPLY/ADJOINT/GRADSUM) or checkpoint slot */
+  int32_t slot;       /* gradient partial slot (ADJOINT) */
+  int64_t beg, end;   /* group, element or slot range */
+} qsgb_batch_item;
+
+typedef struct {
+  const qsgb_batch_instance* instances; /* device */
+  const qsgb_batch_item* items;         /* device */
+  const int32_t* stage_begin;           /* device, n_stages + 1 item offsets */
+  int32_t n_stages;
+  uint32_t* work;          /* device, n_stages + 3 words, ZERO before each run */
+  const float* ptm;        /* device, n_ptm x 256: P (sorted qubit order,
+                              row-major out x in; 4x4 in the first 16) */
+  const float* ptm_inv;    /* device, n_ptm x 256: P^-1 (ADJOINT) */
+  double* grad_partial;    /* device, n_slots x 256 */
+  double* grad;            /* device, n_ptm x 256 */
+  const double* target;    /* device, sum of 2^n over instances */
+  double* prob;            /* device, same layout as target */
+  double* loss;            /* device, per instance */
+} qsgb_batch_program;
+
+/* Largest grid (blocks of `block` threads) whose blocks are all resident. */
+int qsgb_batch_max_grid(int block);
+
+/* Run a batch program.  grid <= qsgb_batch_max_grid(block); block = 256.
+ * cooperative != 0 launches cooperatively (co-residency guaranteed).  Every
+ * grid barrier spins at most `spin_limit` polls; on expiry the kernel sets
+ * QSGB_DEV_TIMEOUT in *dev_status and all blocks return. */
+int qsgb_batch_run(const qsgb_batch_program* prog, int grid, int block,
+                   int cooperative, unsigned* dev_status, int64_t spin_limit,
+                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,7 +10,11 @@ from . import bases
 from . import ptm
 from ._lib import load as load_library
 from .pauli_vector import PauliVectorGB300, register
+from .autograd import ApplyPTM, apply_ptm_diff, diagonal_diff, checkpointed
+from .batch import BatchedSimulator
 
-__all__ = ['PauliVectorGB300', 'register', 'bases', 'ptm', 'load_library']
+__all__ = ['PauliVectorGB300', 'register', 'bases', 'ptm', 'load_library',
+           'ApplyPTM', 'apply_ptm_diff', 'diagonal_diff', 'checkpointed',
+           'BatchedSimulator']
 
 register()

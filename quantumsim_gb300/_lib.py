@@ -66,6 +66,9 @@ SIGNATURES = {
     'qsgb_scale': (_int, [_c_void_p, _int, _i64, _dbl, _c_void_p]),
     'qsgb_scale_by_inverse': (_int, [_c_void_p, _int, _i64, _c_void_p, _dbl,
                                      _c_void_p]),
+    'qsgb_batch_max_grid': (_int, [_int]),
+    'qsgb_batch_run': (_int, [_c_void_p, _int, _int, _int, _c_void_p, _i64,
+                              _c_void_p]),
     'qsgb_ptm_grad_scratch_bytes': (_i64, [_i64, _i64, _i64]),
     'qsgb_ptm_grad1': (_int, [_c_void_p, _c_void_p, _c_void_p, _i64, _i64,
                               _i64, _i64, _int, _c_void_p, _i64, _c_void_p]),

@@ -1,0 +1,438 @@
+"""Batched forward + adjoint of many independent noisy circuits.
+
+``BatchedSimulator`` runs B circuits of different qubit counts (each with its
+own noise parameters) -- Pauli vectors in FP32, probabilities, losses and
+PTM gradients accumulated in FP64 -- as ONE persistent launch of the
+``qsgb_batch_run`` kernel, optionally replayed from a CUDA graph.  One step
+computes, for every instance, the probabilities of the final state, the loss
+KL(target || prob) and dL/dP for every PTM of its circuit.
+
+Circuits are the CPU-runnable workload family: per layer a noisy rotation on
+every qubit (rotation, then amplitude + phase damping over 20 ns) and CZs on
+a line matching.  The device program is built once per circuit structure:
+
+    stage 0              INIT  (|0..0>)
+    stages ...           APPLY of op j of every instance (instances aligned
+                         by op index), SAVE at every `checkpoint_every` layers
+                         ZERO_G, LOSS
+    stages ...           ADJOINT of the ops in reverse, RESTORE at the saved
+                         layers (drift refresh)
+    last stage           GRADSUM per PTM
+
+Each op on a large instance is split into tiles of `tile` groups, so blocks
+share big instances while small ones take one item.  ``autotune()`` times the
+candidate tile sizes and keeps the fastest (cached in a JSON file).
+
+The reference has no batching; the per-instance comparison is the plain GPU
+path (``plain_gradients``): one instance at a time through the ``ApplyPTM``
+autograd function and checkpointed layers.
+"""
+import ctypes
+import json
+import math
+import os
+import time
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import bases as _bases
+from . import ptm as P
+from .autograd import apply_ptm_diff, checkpointed, diagonal_diff
+
+BOP_INIT, BOP_ZERO_G, BOP_APPLY, BOP_SAVE, BOP_RESTORE, BOP_LOSS, \
+    BOP_ADJOINT, BOP_GRADSUM = range(1, 9)
+BLOCK = 256
+T_GATE = 20e-9
+
+
+class _Instance(ctypes.Structure):
+    _fields_ = [('x', ctypes.c_void_p), ('g', ctypes.c_void_p),
+                ('ckpt', ctypes.c_void_p), ('size', ctypes.c_int64),
+                ('n_qubits', ctypes.c_int32), ('diag_offset', ctypes.c_int32)]
+
+
+class _Program(ctypes.Structure):
+    _fields_ = [('instances', ctypes.c_void_p), ('items', ctypes.c_void_p),
+                ('stage_begin', ctypes.c_void_p), ('n_stages', ctypes.c_int32),
+                ('work', ctypes.c_void_p), ('ptm', ctypes.c_void_p),
+                ('ptm_inv', ctypes.c_void_p),
+                ('grad_partial', ctypes.c_void_p), ('grad', ctypes.c_void_p),
+                ('target', ctypes.c_void_p), ('prob', ctypes.c_void_p),
+                ('loss', ctypes.c_void_p)]
+
+
+_ITEM_DTYPE = np.dtype([('op', '<i4'), ('inst', '<i4'), ('q0', '<i4'),
+                        ('q1', '<i4'), ('ptm', '<i4'), ('slot', '<i4'),
+                        ('beg', '<i8'), ('end', '<i8')])
+
+
+class CircuitSpec:
+    """Structure and noise of one instance (seeded)."""
+
+    def __init__(self, n_qubits, depth, seed):
+        rng = np.random.default_rng(seed)
+        self.n = n_qubits
+        self.depth = depth
+        self.axes = [['xyz'[i] for i in rng.integers(3, size=n_qubits)]
+                     for _ in range(depth)]
+        self.angles = rng.uniform(0, 2 * math.pi, (depth, n_qubits))
+        t1 = rng.uniform(20, 60, n_qubits)
+        self.t1 = t1
+        self.t2 = rng.uniform(10, t1)
+        self.pairs = []
+        for l in range(depth):
+            off = int(rng.integers(2)) if n_qubits % 2 else l % 2
+            self.pairs.append([(i, i + 1) for i in range(off, n_qubits - 1,
+                                                         2)])
+
+    def ops(self):
+        """[(layer, qubits)] in application order."""
+        out = []
+        for l in range(self.depth):
+            out += [(l, (q,)) for q in range(self.n)]
+            out += [(l, pr) for pr in self.pairs[l]]
+        return out
+
+
+def instance_ptms(spec, angle_offset=0.0, device='cpu'):
+    """Float64 PTMs of an instance's ops, in op order: (K, K) matrices with
+    K = 4 or 16 (two-qubit ones in (q0, q1) = sorted order)."""
+    n, d = spec.n, spec.depth
+    axes = [a for row in spec.axes for a in row]
+    ang = torch.as_tensor(spec.angles, dtype=torch.float64, device=device)
+    rot = P.rotations_batched(axes, (ang + angle_offset).reshape(-1))
+    g, lam = P.damping_rates(torch.as_tensor(spec.t1 * 1e-6, device=device),
+                             torch.as_tensor(spec.t2 * 1e-6, device=device),
+                             T_GATE)
+    damp = P.amp_phase_damping_batched(g, lam)
+    one = (damp[None] @ rot.reshape(d, n, 4, 4))
+    cz = P.cphase(math.pi).to(device).reshape(16, 16)
+    out = []
+    for l, qs in spec.ops():
+        out.append(one[l, qs[0]] if len(qs) == 1 else cz)
+    return out
+
+
+def target_probabilities(spec, seed):
+    """A target distribution: the exact FP64 probabilities of the same
+    circuit with perturbed rotation angles (computed on the GPU in FP64)."""
+    rng = np.random.default_rng(seed)
+    off = torch.from_numpy(rng.normal(0, 0.05, (spec.depth, spec.n)))
+    ptms = instance_ptms(spec, angle_offset=off)
+    x = torch.zeros((4,) * spec.n, dtype=torch.float64, device='cuda')
+    x[(0,) * spec.n] = 1
+    for pt, (_, qs) in zip(ptms, spec.ops()):
+        pt = pt if len(qs) == 1 else pt.reshape(4, 4, 4, 4)
+        x = apply_ptm_diff(x, pt, *qs)
+    return diagonal_diff(x, [_bases.general(2)] * spec.n).detach()
+
+
+class BatchedSimulator:
+    """Forward + adjoint of many circuits in one persistent launch."""
+
+    def __init__(self, specs, targets, checkpoint_every=8, tile=None,
+                 device=None, cooperative=True):
+        self.lib = L.load()
+        self.device = torch.device(device or 'cuda')
+        self.specs = specs
+        self.every = checkpoint_every
+        self.cooperative = cooperative
+        self.n_inst = len(specs)
+        dev = self.device
+        # ---- per-instance buffers
+        self.sizes = [4 ** s.n for s in specs]
+        self.n_ckpt = [max(0, (s.depth - 1) // checkpoint_every)
+                       for s in specs]
+        self.x = [torch.empty(sz, dtype=torch.float32, device=dev)
+                  for sz in self.sizes]
+        self.g = [torch.empty(sz, dtype=torch.float32, device=dev)
+                  for sz in self.sizes]
+        self.ckpt = [torch.empty(max(1, c) * sz, dtype=torch.float32,
+                                 device=dev)
+                     for c, sz in zip(self.n_ckpt, self.sizes)]
+        self.diag_off = np.cumsum([0] + [2 ** s.n for s in specs])
+        self.target = torch.cat([t.to(dev, torch.float64).reshape(-1)
+                                 for t in targets])
+        self.prob = torch.empty_like(self.target)
+        self.loss = torch.empty(self.n_inst, dtype=torch.float64, device=dev)
+        inst = (_Instance * self.n_inst)()
+        for i, s in enumerate(specs):
+            inst[i] = _Instance(self.x[i].data_ptr(), self.g[i].data_ptr(),
+                                self.ckpt[i].data_ptr(), self.sizes[i], s.n,
+                                int(self.diag_off[i]))
+        self.inst_dev = torch.frombuffer(bytearray(bytes(inst)),
+                                         dtype=torch.uint8).to(dev)
+        # ---- PTM pool: one slot per op of every instance
+        self.op_base = np.cumsum([0] + [len(s.ops()) for s in specs])
+        self.n_ptm = int(self.op_base[-1])
+        self.ptm = torch.zeros(self.n_ptm, 256, dtype=torch.float32,
+                               device=dev)
+        self.ptm_inv = torch.zeros_like(self.ptm)
+        self.grad = torch.zeros(self.n_ptm, 256, dtype=torch.float64,
+                                device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.max_grid = self.lib.qsgb_batch_max_grid(BLOCK)
+        if self.max_grid < 1:
+            raise RuntimeError('batched kernel cannot be made resident')
+        self.tile = tile or self._cached_tile() or 8192
+        self._build_program(self.tile)
+        self.graph = None
+
+    # ------------------------------------------------------------ program
+    def _build_program(self, tile):
+        stages = []  # list of per-stage item lists
+
+        def stage(k):
+            while len(stages) <= k:
+                stages.append([])
+            return stages[k]
+
+        slot = 0
+        slots_of = {}
+        for i, s in enumerate(self.specs):
+            size, n = self.sizes[i], s.n
+            seq = []  # list of item lists, one per stage of this instance
+
+            def split(total, mk):
+                items, b = [], 0
+                step = tile * 16
+                while b < total:
+                    e = min(total, b + step)
+                    items.append(mk(b, e))
+                    b = e
+                return items
+
+            seq.append(split(size, lambda b, e: (BOP_INIT, i, -1, -1, 0, 0,
+                                                 b, e)))
+            ops = s.ops()
+            layer_of = [l for l, _ in ops]
+            for j, (l, qs) in enumerate(ops):
+                pidx = int(self.op_base[i]) + j
+                q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
+                groups = size // (4 if q1 < 0 else 16)
+                seq.append(self._tiles(groups, tile, BOP_APPLY, i, q0, q1,
+                                       pidx, 0))
+                last_of_layer = j + 1 == len(ops) or layer_of[j + 1] != l
+                if last_of_layer and (l + 1) % self.every == 0 and \
+                        l + 1 < s.depth:
+                    c = (l + 1) // self.every - 1
+                    seq.append(split(size, lambda b, e, c=c: (
+                        BOP_SAVE, i, -1, -1, c, 0, b, e)))
+            seq.append(split(size, lambda b, e: (BOP_ZERO_G, i, -1, -1, 0, 0,
+                                                 b, e)))
+            seq.append([(BOP_LOSS, i, -1, -1, 0, 0, 0, 0)])
+            for j in reversed(range(len(ops))):
+                l, qs = ops[j]
+                pidx = int(self.op_base[i]) + j
+                q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
+                groups = size // (4 if q1 < 0 else 16)
+                items = self._tiles(groups, tile, BOP_ADJOINT, i, q0, q1,
+                                    pidx, slot)
+                slots_of[pidx] = (slot, slot + len(items))
+                slot += len(items)
+                seq.append(items)
+                first_of_layer = j == 0 or layer_of[j - 1] != l
+                if first_of_layer and l > 0 and l % self.every == 0:
+                    c = l // self.every - 1
+                    seq.append(split(size, lambda b, e, c=c: (
+                        BOP_RESTORE, i, -1, -1, c, 0, b, e)))
+            for k, items in enumerate(seq):
+                stage(k).extend(items)
+        gstage = []
+        for pidx in range(self.n_ptm):
+            b, e = slots_of[pidx]
+            gstage.append((BOP_GRADSUM, 0, -1, -1, pidx, 0, b, e))
+        stages.append(gstage)
+        items = np.array([it for st in stages for it in st],
+                         dtype=_ITEM_DTYPE)
+        begin = np.cumsum([0] + [len(st) for st in stages]).astype(np.int32)
+        dev = self.device
+        self.n_stages = len(stages)
+        self.n_items = len(items)
+        self.items_dev = torch.from_numpy(items.view(np.uint8).copy()).to(dev)
+        self.stage_dev = torch.from_numpy(begin).to(dev)
+        self.work = torch.zeros(self.n_stages + 3, dtype=torch.int32,
+                                device=dev)
+        self.grad_partial = torch.zeros(max(1, slot), 256,
+                                        dtype=torch.float64, device=dev)
+        self.n_slots = slot
+        prog = _Program()
+        prog.instances = self.inst_dev.data_ptr()
+        prog.items = self.items_dev.data_ptr()
+        prog.stage_begin = self.stage_dev.data_ptr()
+        prog.n_stages = self.n_stages
+        prog.work = self.work.data_ptr()
+        prog.ptm = self.ptm.data_ptr()
+        prog.ptm_inv = self.ptm_inv.data_ptr()
+        prog.grad_partial = self.grad_partial.data_ptr()
+        prog.grad = self.grad.data_ptr()
+        prog.target = self.target.data_ptr()
+        prog.prob = self.prob.data_ptr()
+        prog.loss = self.loss.data_ptr()
+        self.prog = prog
+        self.tile = tile
+        self.graph = None
+
+    @staticmethod
+    def _tiles(groups, tile, op, i, q0, q1, pidx, slot):
+        items, b = [], 0
+        k = 0
+        while b < groups:
+            e = min(groups, b + tile)
+            items.append((op, i, q0, q1, pidx, slot + k, b, e))
+            b = e
+            k += 1
+        return items
+
+    # ------------------------------------------------------------ PTMs
+    def set_ptms(self, ptms_per_instance):
+        """ptms_per_instance[i][j]: (K, K) float64 PTM of op j of instance i
+        (any device).  Builds the FP32 pool of P and P^-1 on the GPU."""
+        flat = [p.reshape(p.shape[0], -1) if p.dim() == 2 else
+                p.reshape(16, 16) for ps in ptms_per_instance for p in ps]
+        dev = self.device
+        one = [k for k, p in enumerate(flat) if p.shape[0] == 4]
+        two = [k for k, p in enumerate(flat) if p.shape[0] == 16]
+        for idx, K in ((one, 4), (two, 16)):
+            if not idx:
+                continue
+            m = torch.stack([flat[k].to(dev, torch.float64) for k in idx])
+            inv = torch.linalg.inv(m)
+            pool = torch.zeros(len(idx), 256, dtype=torch.float64,
+                               device=dev)
+            ipool = torch.zeros_like(pool)
+            pool[:, :K * K] = m.reshape(len(idx), -1)
+            ipool[:, :K * K] = inv.reshape(len(idx), -1)
+            sel = torch.as_tensor(idx, device=dev)
+            self.ptm[sel] = pool.float()
+            self.ptm_inv[sel] = ipool.float()
+
+    # ------------------------------------------------------------ run
+    def _launch(self, grid):
+        self.work.zero_()
+        st = self.lib.qsgb_batch_run(
+            ctypes.byref(self.prog), grid, BLOCK, 1 if self.cooperative else 0,
+            ctypes.c_void_p(self.status.data_ptr()), 1 << 26,
+            ctypes.c_void_p(torch.cuda.current_stream(self.device)
+                            .cuda_stream))
+        L.check(st, 'qsgb_batch_run')
+
+    def step(self, grid=None, use_graph=True):
+        """One forward + adjoint of every instance (asynchronous)."""
+        grid = grid or self.max_grid
+        if use_graph:
+            if self.graph is None:
+                self._launch(grid)  # warm-up outside capture
+                torch.cuda.synchronize(self.device)
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._launch(grid)
+                self.graph = g
+            self.graph.replay()
+        else:
+            self._launch(grid)
+
+    def check(self):
+        val = int(self.status.item())
+        if val:
+            self.status.zero_()
+            raise RuntimeError('batched kernel device status {}'.format(val))
+
+    def results(self):
+        """(probabilities per instance, loss per instance, PTM gradients per
+        instance as lists of (K, K) float64 tensors)."""
+        self.check()
+        probs = [self.prob[self.diag_off[i]:self.diag_off[i + 1]]
+                 for i in range(self.n_inst)]
+        grads = []
+        for i, s in enumerate(self.specs):
+            gi = []
+            for j, (_, qs) in enumerate(s.ops()):
+                K = 4 if len(qs) == 1 else 16
+                gi.append(self.grad[int(self.op_base[i]) + j, :K * K]
+                          .view(K, K))
+            grads.append(gi)
+        return probs, self.loss, grads
+
+    # ------------------------------------------------------------ autotune
+    def _cache_key(self):
+        sig = sorted(s.n for s in self.specs)
+        return '{}:{}:{}'.format(len(sig), sum(4 ** n for n in sig),
+                                 self.max_grid)
+
+    @staticmethod
+    def _cache_path():
+        return os.environ.get('QSGB_AUTOTUNE_CACHE', os.path.join(
+            os.path.dirname(os.path.abspath(__file__)), '_build',
+            'batch_autotune.json'))
+
+    def _cached_tile(self):
+        try:
+            with open(self._cache_path()) as f:
+                return int(json.load(f)[self._cache_key()]['tile'])
+        except Exception:
+            return None
+
+    def autotune(self, candidates=(2048, 4096, 8192, 16384, 32768), reps=2):
+        """Time one step per tile size, keep the fastest; returns
+        {tile: ms}."""
+        times = {}
+        for t in candidates:
+            self._build_program(t)
+            self.step(use_graph=False)
+            torch.cuda.synchronize(self.device)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                self.step(use_graph=False)
+            e1.record()
+            torch.cuda.synchronize(self.device)
+            times[t] = e0.elapsed_time(e1) / reps
+        best = min(times, key=times.get)
+        self._build_program(best)
+        path = self._cache_path()
+        try:
+            data = {}
+            if os.path.exists(path):
+                with open(path) as f:
+                    data = json.load(f)
+            data[self._cache_key()] = {'tile': best, 'ms': times}
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            with open(path, 'w') as f:
+                json.dump(data, f, indent=1, default=str)
+        except Exception:
+            pass
+        return times
+
+
+def plain_gradients(spec, ptms, target, dtype=torch.float32,
+                    checkpoint_every=8):
+    """The plain GPU path for one instance: ApplyPTM autograd op by op with
+    checkpointed layers.  Returns (probabilities, loss, [dL/dP per op])."""
+    params = [p.detach().clone().to(torch.float64).requires_grad_()
+              for p in ptms]
+    x = torch.zeros((4,) * spec.n, dtype=dtype, device='cuda')
+    x[(0,) * spec.n] = 1
+    ops = spec.ops()
+    layers = []
+    for l in range(spec.depth):
+        idx = [j for j, (ll, _) in enumerate(ops) if ll == l]
+
+        def layer(s, idx=idx):
+            for j in idx:
+                qs = ops[j][1]
+                pt = params[j] if len(qs) == 1 else params[j].view(4, 4, 4, 4)
+                s = apply_ptm_diff(s, pt, *qs)
+            return s
+        layers.append(layer)
+    x = checkpointed(layers, x, checkpoint_every)
+    prob = diagonal_diff(x, [_bases.general(2)] * spec.n)
+    t = target.to(prob.device, torch.float64)
+    pe = prob.clamp_min(1e-300)
+    loss = torch.sum(torch.where(t > 0, t * (torch.log(t) - torch.log(pe)),
+                                 torch.zeros_like(t)))
+    loss.backward()
+    return prob.detach(), loss.detach(), [p.grad for p in params]

@@ -1,0 +1,414 @@
+// Batched forward + adjoint of many independent circuits in one persistent
+// launch (FP32 Pauli vectors, FP64 reductions).
+//
+// Work model: a program is a sequence of stages; each stage holds work items
+// (one op of one instance on a range of groups or elements).  Items of a
+// stage belong to independent instances, so persistent blocks take them from
+// the stage's atomic counter in any order; a grid barrier separates stages.
+// Small instances finish in one item, large ones are split into tiles, so a
+// few hundred blocks keep busy across instances of 4..16 qubits.
+//
+// Adjoint without stored intermediates: an op's input state is rebuilt from
+// its output with the inverse PTM (rotations, controlled phases and damping
+// are invertible and well conditioned), while the adjoint state moves back
+// through P^T; the host refreshes the state from checkpoints every few
+// layers.  One ADJOINT item therefore reads x_out and g_out once, writes x_in
+// and g_in, and accumulates its share of dL/dP = sum g_out (x) x_in.
+//
+// Every grid barrier polls a bounded number of times; on expiry the kernel
+// flags QSGB_DEV_TIMEOUT and all blocks return.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
+#include "qsgb_common.cuh"
+
+namespace qsgb {
+namespace {
+
+constexpr int kBatchBlock = 256;
+constexpr int kSlices = kBatchBlock / 16;  // group slices in the dP reduction
+
+struct BatchSmem {
+  float P[256];
+  float Pi[256];
+  // adjoint tile: g_out and x_in per group, [group][16]; reused for the FP64
+  // cross-slice reduction of the dP partials
+  union {
+    struct {
+      float g[kBatchBlock][16];
+      float x[kBatchBlock][16];
+    } t;
+    double red[kSlices][256];
+  } u __attribute__((aligned(16)));
+  double acc[kBatchBlock][16];  // per-thread FP64 dP partials (ADJOINT)
+  int item;
+  int ok;
+  double lsum[kBatchBlock / 32];
+};
+
+__device__ __forceinline__ volatile uint32_t* vol(uint32_t* p) { return p; }
+
+// Grid barrier (sense by generation).  Returns false when the wait expired
+// or another block aborted.
+__device__ bool grid_barrier(uint32_t* count, uint32_t* gen, uint32_t* abort_flag, long long limit,
+                             unsigned* status, BatchSmem& sm) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sm.ok = 1;
+    const uint32_t g0 = *vol(gen);
+    __threadfence();
+    if (atomicAdd(count, 1u) == gridDim.x - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      long long it = 0;
+      while (*vol(gen) == g0) {
+        if (*vol(abort_flag) || ++it > limit) {
+          sm.ok = 0;
+          if (it > limit && status) atomicOr(status, QSGB_DEV_TIMEOUT);
+          atomicExch(abort_flag, 1u);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return sm.ok != 0;
+}
+
+// ---------------------------------------------------------------- geometry
+struct Geo {
+  int k;          // 4 or 16 inputs per group
+  int lz, ly;     // log2 of Z and Y (powers of 4)
+};
+
+__device__ __forceinline__ Geo geometry(int n, int q0, int q1) {
+  Geo g;
+  if (q1 < 0) {
+    g.k = 4;
+    g.lz = 2 * (n - 1 - q0);
+    g.ly = 0;
+  } else {
+    g.k = 16;
+    g.lz = 2 * (n - 1 - q1);
+    g.ly = 2 * (q1 - q0 - 1);
+  }
+  return g;
+}
+
+// base element of group `gi` and offset of input k
+__device__ __forceinline__ int64_t group_base(const Geo& g, int64_t gi) {
+  const int64_t z = gi & ((1ll << g.lz) - 1);
+  const int64_t t = gi >> g.lz;
+  if (g.k == 4) return ((t << (g.lz + 2)) | z);
+  const int64_t y = t & ((1ll << g.ly) - 1);
+  const int64_t x = t >> g.ly;
+  return (x << (g.lz + g.ly + 4)) + (y << (g.lz + 2)) + z;
+}
+
+template <int K>
+__device__ __forceinline__ int64_t in_offset(const Geo& g, int k) {
+  if (K == 4) return (int64_t)k << g.lz;
+  return ((int64_t)(k >> 2) << (g.lz + g.ly + 2)) + ((int64_t)(k & 3) << g.lz);
+}
+
+// ---------------------------------------------------------------- items
+template <int K>
+__device__ void apply_groups(float* __restrict__ x, const Geo& geo, int64_t beg, int64_t end, const float* P) {
+  for (int64_t gi = beg + threadIdx.x; gi < end; gi += blockDim.x) {
+    const int64_t b = group_base(geo, gi);
+    float v[K], y[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = x[b + in_offset<K>(geo, k)];
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+      float a = 0.f;
+#pragma unroll
+      for (int k = 0; k < K; ++k) a = fmaf(P[r * K + k], v[k], a);
+      y[r] = a;
+    }
+#pragma unroll
+    for (int r = 0; r < K; ++r) x[b + in_offset<K>(geo, r)] = y[r];
+  }
+}
+
+// x = P^-1 x, g = P^T g on groups [beg, end); returns this thread's FP64
+// share of sum_g g_out (x) x_in, accumulated into acc (16 entries: a 4x4
+// sub-block for K = 16, one entry for K = 4).
+template <int K>
+__device__ void adjoint_groups(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
+                               int64_t end, BatchSmem& sm) {
+  double* acc = sm.acc[threadIdx.x];
+  const int tid = threadIdx.x;
+  const int sub = tid & 15, slice = tid >> 4;
+  for (int64_t t0 = beg; t0 < end; t0 += blockDim.x) {
+    const int64_t gi = t0 + tid;
+    if (gi < end) {
+      const int64_t b = group_base(geo, gi);
+      {  // x_in = P^-1 x_out
+        float xo[K], xi[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) xo[k] = x[b + in_offset<K>(geo, k)];
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+          float a = 0.f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) a = fmaf(sm.Pi[r * K + k], xo[k], a);
+          xi[r] = a;
+        }
+#pragma unroll
+        for (int r = 0; r < K; ++r) x[b + in_offset<K>(geo, r)] = xi[r];
+#pragma unroll
+        for (int k = 0; k < K; k += 4)
+          *reinterpret_cast<float4*>(&sm.u.t.x[tid][k]) = make_float4(xi[k], xi[k + 1], xi[k + 2], xi[k + 3]);
+      }
+      {  // g_in = P^T g_out
+        float go[K], gn[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) go[k] = gv[b + in_offset<K>(geo, k)];
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+          float c = 0.f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) c = fmaf(sm.P[k * K + r], go[k], c);
+          gn[r] = c;
+        }
+#pragma unroll
+        for (int r = 0; r < K; ++r) gv[b + in_offset<K>(geo, r)] = gn[r];
+#pragma unroll
+        for (int k = 0; k < K; k += 4)
+          *reinterpret_cast<float4*>(&sm.u.t.g[tid][k]) = make_float4(go[k], go[k + 1], go[k + 2], go[k + 3]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < K; k += 4) {
+        *reinterpret_cast<float4*>(&sm.u.t.x[tid][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4*>(&sm.u.t.g[tid][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    __syncthreads();
+    // this thread: groups slice*16 .. slice*16+15 of the tile
+    if (K == 16) {
+      const int rb = (sub >> 2) * 4, cb = (sub & 3) * 4;
+      float s[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) s[i] = 0.f;
+      for (int gg = slice * 16; gg < slice * 16 + 16; ++gg) {
+        const float4 a = *reinterpret_cast<const float4*>(&sm.u.t.g[gg][rb]);
+        const float4 c = *reinterpret_cast<const float4*>(&sm.u.t.x[gg][cb]);
+        const float av[4] = {a.x, a.y, a.z, a.w};
+        const float cv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) s[i * 4 + j] = fmaf(av[i], cv[j], s[i * 4 + j]);
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) acc[i] += (double)s[i];
+    } else {
+      const int r = sub >> 2, c = sub & 3;
+      float s = 0.f;
+      for (int gg = slice * 16; gg < slice * 16 + 16; ++gg) s = fmaf(sm.u.t.g[gg][r], sm.u.t.x[gg][c], s);
+      acc[0] += (double)s;
+    }
+    __syncthreads();
+  }
+}
+
+// write the block's dP partial (sum over slices) to grad_partial[slot]
+template <int K>
+__device__ void store_partial(double* __restrict__ dst, BatchSmem& sm) {
+  const int tid = threadIdx.x;
+  const double* acc = sm.acc[tid];
+  const int sub = tid & 15, slice = tid >> 4;
+  if (K == 16) {
+    const int rb = (sub >> 2) * 4, cb = (sub & 3) * 4;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) sm.u.red[slice][(rb + i) * 16 + cb + j] = acc[i * 4 + j];
+  } else {
+    sm.u.red[slice][sub] = acc[0];
+  }
+  __syncthreads();
+  for (int e = tid; e < K * K; e += blockDim.x) {
+    double s = 0.0;
+    for (int sl = 0; sl < kSlices; ++sl) s += sm.u.red[sl][e];
+    dst[e] = s;
+  }
+  __syncthreads();
+}
+
+__device__ void loss_item(const qsgb_batch_program& p, const qsgb_batch_instance& in, int inst, BatchSmem& sm) {
+  const int n = in.n_qubits;
+  const int64_t D = 1ll << n;
+  double part = 0.0;
+  for (int64_t j = threadIdx.x; j < D; j += blockDim.x) {
+    // element of the diagonal entry j: bit q of j (from the top) selects
+    // Pauli element 0 (|0><0|) or 1 (|1><1|) of qubit q
+    int64_t idx = 0;
+    for (int q = 0; q < n; ++q) idx |= ((j >> (n - 1 - q)) & 1ll) << (2 * (n - 1 - q));
+    const double pr = (double)in.x[idx];
+    const double t = p.target[in.diag_offset + j];
+    p.prob[in.diag_offset + j] = pr;
+    const double pe = pr > 1e-300 ? pr : 1e-300;
+    if (t > 0) {
+      part += t * (log(t) - log(pe));
+      in.g[idx] = (float)(-t / pe);
+    } else {
+      in.g[idx] = 0.f;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0) sm.lsum[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sm.lsum[w];
+    p.loss[inst] = s;
+  }
+  __syncthreads();
+}
+
+__device__ void process(const qsgb_batch_program& p, const qsgb_batch_item& it, BatchSmem& sm) {
+  const qsgb_batch_instance in = p.instances[it.inst];
+  switch (it.op) {
+    case QSGB_BOP_INIT:
+      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) in.x[e] = (e == 0) ? 1.f : 0.f;
+      break;
+    case QSGB_BOP_ZERO_G:
+      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) in.g[e] = 0.f;
+      break;
+    case QSGB_BOP_SAVE: {
+      float* dst = in.ckpt + (int64_t)it.ptm * in.size;
+      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) dst[e] = in.x[e];
+      break;
+    }
+    case QSGB_BOP_RESTORE: {
+      const float* src = in.ckpt + (int64_t)it.ptm * in.size;
+      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) in.x[e] = src[e];
+      break;
+    }
+    case QSGB_BOP_APPLY:
+    case QSGB_BOP_ADJOINT: {
+      const Geo geo = geometry(in.n_qubits, it.q0, it.q1);
+      const int kk = geo.k * geo.k;
+      for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+        sm.P[e] = p.ptm[(int64_t)it.ptm * 256 + e];
+        if (it.op == QSGB_BOP_ADJOINT) sm.Pi[e] = p.ptm_inv[(int64_t)it.ptm * 256 + e];
+      }
+      __syncthreads();
+      if (it.op == QSGB_BOP_APPLY) {
+        if (geo.k == 4)
+          apply_groups<4>(in.x, geo, it.beg, it.end, sm.P);
+        else
+          apply_groups<16>(in.x, geo, it.beg, it.end, sm.P);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) sm.acc[threadIdx.x][i] = 0.0;
+        double* dst = p.grad_partial + (int64_t)it.slot * 256;
+        if (geo.k == 4) {
+          adjoint_groups<4>(in.x, in.g, geo, it.beg, it.end, sm);
+          store_partial<4>(dst, sm);
+        } else {
+          adjoint_groups<16>(in.x, in.g, geo, it.beg, it.end, sm);
+          store_partial<16>(dst, sm);
+        }
+      }
+      __syncthreads();
+      break;
+    }
+    case QSGB_BOP_LOSS:
+      loss_item(p, in, it.inst, sm);
+      break;
+    case QSGB_BOP_GRADSUM:
+      for (int e = threadIdx.x; e < 256; e += blockDim.x) {
+        double s = 0.0;
+        for (int64_t sl = it.beg; sl < it.end; ++sl) s += p.grad_partial[sl * 256 + e];
+        p.grad[(int64_t)it.ptm * 256 + e] = s;
+      }
+      break;
+    default:
+      if (threadIdx.x == 0 && p.work) atomicExch(&p.work[p.n_stages + 2], 1u);
+      break;
+  }
+}
+
+__global__ void __launch_bounds__(kBatchBlock, 2) batch_kernel(const __grid_constant__ qsgb_batch_program p,
+                                                               unsigned* status, long long spin_limit) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  BatchSmem& sm = *reinterpret_cast<BatchSmem*>(dsm);
+  uint32_t* bar_count = p.work + p.n_stages;
+  uint32_t* bar_gen = p.work + p.n_stages + 1;
+  uint32_t* abort_flag = p.work + p.n_stages + 2;
+  for (int s = 0; s < p.n_stages; ++s) {
+    const int beg = p.stage_begin[s], end = p.stage_begin[s + 1];
+    while (true) {
+      __syncthreads();
+      if (threadIdx.x == 0) sm.item = beg + (int)atomicAdd(&p.work[s], 1u);
+      __syncthreads();
+      const int i = sm.item;
+      if (i >= end) break;
+      const qsgb_batch_item it = p.items[i];
+      if (it.op < QSGB_BOP_INIT || it.op > QSGB_BOP_GRADSUM || it.inst < 0) {
+        if (threadIdx.x == 0 && status) atomicOr(status, QSGB_DEV_BADITEM);
+        continue;
+      }
+      process(p, it, sm);
+    }
+    if (s + 1 < p.n_stages && !grid_barrier(bar_count, bar_gen, abort_flag, spin_limit, status, sm)) return;
+  }
+}
+
+}  // namespace
+}  // namespace qsgb
+
+static int batch_smem_setup() {
+  const int bytes = (int)sizeof(qsgb::BatchSmem);
+  if (cudaFuncSetAttribute(qsgb::batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return bytes;
+}
+
+extern "C" int qsgb_batch_max_grid(int block) {
+  if (block != qsgb::kBatchBlock) return 0;
+  const int smem = batch_smem_setup();
+  if (smem < 0) return 0;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, qsgb::batch_kernel, block, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return occ * qsgb::sm_count();
+}
+
+extern "C" int qsgb_batch_run(const qsgb_batch_program* prog, int grid, int block, int cooperative,
+                              unsigned* dev_status, int64_t spin_limit, void* stream) {
+  if (!prog || !prog->instances || !prog->items || !prog->stage_begin || !prog->work || !prog->ptm)
+    return QSGB_ERR_INVALID;
+  if (block != qsgb::kBatchBlock || grid < 1 || prog->n_stages < 1 || spin_limit < 1) return QSGB_ERR_INVALID;
+  const int maxg = qsgb_batch_max_grid(block);
+  if (maxg < 1) return QSGB_ERR_CUDA;
+  if (grid > maxg) return QSGB_ERR_INVALID;  // every block must be resident for the barriers
+  qsgb_batch_program p = *prog;
+  long long lim = (long long)spin_limit;
+  cudaStream_t s = qsgb::as_stream(stream);
+  void* args[] = {(void*)&p, (void*)&dev_status, (void*)&lim};
+  cudaError_t e;
+  const size_t smem = sizeof(qsgb::BatchSmem);
+  if (cooperative)
+    e = cudaLaunchCooperativeKernel((const void*)qsgb::batch_kernel, dim3(grid), dim3(block), args, smem, s);
+  else
+    e = cudaLaunchKernel((const void*)qsgb::batch_kernel, dim3(grid), dim3(block), args, smem, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return QSGB_ERR_CUDA;
+  }
+  return QSGB_OK;
+}
