@@ -181,83 +181,91 @@ class BatchedSimulator:
         self.graph = None
 
     # ------------------------------------------------------------ program
-    def _build_program(self, tile):
-        stages = []  # list of per-stage item lists
-
-        def stage(k):
-            while len(stages) <= k:
-                stages.append([])
-            return stages[k]
-
-        slot = 0
-        slots_of = {}
+    def _build_program(self, tile, max_items=64):
+        """Device program for the current circuits.  Every op is one stage
+        entry per instance; an entry covering `total` groups (or elements)
+        becomes ceil(total / chunk) items with chunk = max(tile,
+        ceil(total / max_items)) -- large ops are shared by many blocks, and
+        no op has more than `max_items` items."""
+        ent = []  # (stage, op, inst, q0, q1, ptm or checkpoint, total)
         for i, s in enumerate(self.specs):
-            size, n = self.sizes[i], s.n
-            seq = []  # list of item lists, one per stage of this instance
-
-            def split(total, mk):
-                items, b = [], 0
-                step = tile * 16
-                while b < total:
-                    e = min(total, b + step)
-                    items.append(mk(b, e))
-                    b = e
-                return items
-
-            seq.append(split(size, lambda b, e: (BOP_INIT, i, -1, -1, 0, 0,
-                                                 b, e)))
+            size = self.sizes[i]
             ops = s.ops()
             layer_of = [l for l, _ in ops]
+            seq = [(BOP_INIT, -1, -1, 0, size)]
             for j, (l, qs) in enumerate(ops):
                 pidx = int(self.op_base[i]) + j
                 q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
-                groups = size // (4 if q1 < 0 else 16)
-                seq.append(self._tiles(groups, tile, BOP_APPLY, i, q0, q1,
-                                       pidx, 0))
+                seq.append((BOP_APPLY, q0, q1, pidx,
+                            size // (4 if q1 < 0 else 16)))
                 last_of_layer = j + 1 == len(ops) or layer_of[j + 1] != l
                 if last_of_layer and (l + 1) % self.every == 0 and \
                         l + 1 < s.depth:
-                    c = (l + 1) // self.every - 1
-                    seq.append(split(size, lambda b, e, c=c: (
-                        BOP_SAVE, i, -1, -1, c, 0, b, e)))
-            seq.append(split(size, lambda b, e: (BOP_ZERO_G, i, -1, -1, 0, 0,
-                                                 b, e)))
-            seq.append([(BOP_LOSS, i, -1, -1, 0, 0, 0, 0)])
+                    seq.append((BOP_SAVE, -1, -1, (l + 1) // self.every - 1,
+                                size))
+            seq.append((BOP_ZERO_G, -1, -1, 0, size))
+            seq.append((BOP_LOSS, -1, -1, 0, 1))
             for j in reversed(range(len(ops))):
                 l, qs = ops[j]
                 pidx = int(self.op_base[i]) + j
                 q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
-                groups = size // (4 if q1 < 0 else 16)
-                items = self._tiles(groups, tile, BOP_ADJOINT, i, q0, q1,
-                                    pidx, slot)
-                slots_of[pidx] = (slot, slot + len(items))
-                slot += len(items)
-                seq.append(items)
+                seq.append((BOP_ADJOINT, q0, q1, pidx,
+                            size // (4 if q1 < 0 else 16)))
                 first_of_layer = j == 0 or layer_of[j - 1] != l
                 if first_of_layer and l > 0 and l % self.every == 0:
-                    c = l // self.every - 1
-                    seq.append(split(size, lambda b, e, c=c: (
-                        BOP_RESTORE, i, -1, -1, c, 0, b, e)))
-            for k, items in enumerate(seq):
-                stage(k).extend(items)
-        gstage = []
-        for pidx in range(self.n_ptm):
-            b, e = slots_of[pidx]
-            gstage.append((BOP_GRADSUM, 0, -1, -1, pidx, 0, b, e))
-        stages.append(gstage)
-        items = np.array([it for st in stages for it in st],
-                         dtype=_ITEM_DTYPE)
-        begin = np.cumsum([0] + [len(st) for st in stages]).astype(np.int32)
+                    seq.append((BOP_RESTORE, -1, -1, l // self.every - 1,
+                                size))
+            for k, (op, q0, q1, pp, total) in enumerate(seq):
+                ent.append((k, op, i, q0, q1, pp, total))
+        e = np.array(ent, dtype=np.int64)
+        stage, op, inst, q0, q1, pp, total = e.T
+        is_loss = op == BOP_LOSS
+        chunk = np.where(is_loss, 1, np.maximum(tile, -(-total // max_items)))
+        n_items = -(-total // chunk)
+        # one dP partial slot per ADJOINT item
+        adj = op == BOP_ADJOINT
+        slot_base = np.zeros(len(e), dtype=np.int64)
+        slot_base[adj] = np.cumsum(np.concatenate([[0], n_items[adj][:-1]]))
+        n_slots = int(n_items[adj].sum())
+        # expand entries into items
+        rep = np.repeat(np.arange(len(e)), n_items)
+        first = np.repeat(np.cumsum(n_items) - n_items, n_items)
+        j = np.arange(len(rep)) - first
+        beg = j * chunk[rep]
+        end_ = np.minimum(total[rep], beg + chunk[rep])
+        items = np.zeros(len(rep), dtype=_ITEM_DTYPE)
+        items['op'] = op[rep]
+        items['inst'] = inst[rep]
+        items['q0'] = q0[rep]
+        items['q1'] = q1[rep]
+        items['ptm'] = pp[rep]
+        items['slot'] = np.where(adj[rep], slot_base[rep] + j, 0)
+        items['beg'] = np.where(is_loss[rep], 0, beg)
+        items['end'] = np.where(is_loss[rep], 0, end_)
+        st = stage[rep]
+        n_main = int(st.max()) + 1
+        # last stage: GRADSUM per PTM over the slots of its ADJOINT items
+        gitems = np.zeros(int(adj.sum()), dtype=_ITEM_DTYPE)
+        gitems['op'] = BOP_GRADSUM
+        gitems['ptm'] = pp[adj]
+        gitems['q1'] = -1
+        gitems['beg'] = slot_base[adj]
+        gitems['end'] = slot_base[adj] + n_items[adj]
+        order = np.argsort(st, kind='stable')
+        items = np.concatenate([items[order], gitems])
+        counts = np.concatenate([np.bincount(st, minlength=n_main),
+                                 [len(gitems)]])
+        begin = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
         dev = self.device
-        self.n_stages = len(stages)
+        self.n_stages = n_main + 1
         self.n_items = len(items)
         self.items_dev = torch.from_numpy(items.view(np.uint8).copy()).to(dev)
         self.stage_dev = torch.from_numpy(begin).to(dev)
         self.work = torch.zeros(self.n_stages + 3, dtype=torch.int32,
                                 device=dev)
-        self.grad_partial = torch.zeros(max(1, slot), 256,
+        self.grad_partial = torch.zeros(max(1, n_slots), 256,
                                         dtype=torch.float64, device=dev)
-        self.n_slots = slot
+        self.n_slots = n_slots
         prog = _Program()
         prog.instances = self.inst_dev.data_ptr()
         prog.items = self.items_dev.data_ptr()
@@ -273,18 +281,8 @@ class BatchedSimulator:
         prog.loss = self.loss.data_ptr()
         self.prog = prog
         self.tile = tile
+        self.max_items = max_items
         self.graph = None
-
-    @staticmethod
-    def _tiles(groups, tile, op, i, q0, q1, pidx, slot):
-        items, b = [], 0
-        k = 0
-        while b < groups:
-            e = min(groups, b + tile)
-            items.append((op, i, q0, q1, pidx, slot + k, b, e))
-            b = e
-            k += 1
-        return items
 
     # ------------------------------------------------------------ PTMs
     def set_ptms(self, ptms_per_instance):

@@ -136,6 +136,176 @@ __device__ void apply_groups(float* __restrict__ x, const Geo& geo, int64_t beg,
   }
 }
 
+// Vectorised in-place apply.  Z >= 4: a thread takes V consecutive groups
+// (z .. z+V-1, 16- or 8-byte accesses per input); Z == 1: the K inputs of a
+// group along the less significant qubit are contiguous (16-byte accesses).
+template <int K>
+__device__ void apply_vec(float* __restrict__ x, const Geo& geo, int64_t beg, int64_t end, const float* P) {
+  if (geo.lz >= 2) {
+    constexpr int V = (K == 4) ? 4 : 2;
+    for (int64_t gi = beg + (int64_t)threadIdx.x * V; gi < end; gi += (int64_t)blockDim.x * V) {
+      const int64_t b = group_base(geo, gi);
+      float v[K][V];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const float* src = x + b + in_offset<K>(geo, k);
+        if (V == 4) {
+          const float4 t = *reinterpret_cast<const float4*>(src);
+          v[k][0] = t.x; v[k][1] = t.y; v[k][2 % V] = t.z; v[k][3 % V] = t.w;
+        } else {
+          const float2 t = *reinterpret_cast<const float2*>(src);
+          v[k][0] = t.x; v[k][1] = t.y;
+        }
+      }
+#pragma unroll 4
+      for (int r = 0; r < K; ++r) {
+        float y[V];
+#pragma unroll
+        for (int l = 0; l < V; ++l) y[l] = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const float pk = P[r * K + k];
+#pragma unroll
+          for (int l = 0; l < V; ++l) y[l] = fmaf(pk, v[k][l], y[l]);
+        }
+        float* dst = x + b + in_offset<K>(geo, r);
+        if (V == 4)
+          *reinterpret_cast<float4*>(dst) = make_float4(y[0], y[1], y[2 % V], y[3 % V]);
+        else
+          *reinterpret_cast<float2*>(dst) = make_float2(y[0], y[1]);
+      }
+    }
+  } else {
+    for (int64_t gi = beg + threadIdx.x; gi < end; gi += blockDim.x) {
+      const int64_t b = group_base(geo, gi);
+      float v[K], y[K];
+#pragma unroll
+      for (int k = 0; k < K; k += 4) {
+        const float4 t = *reinterpret_cast<const float4*>(x + b + in_offset<K>(geo, k));
+        v[k] = t.x; v[k + 1] = t.y; v[k + 2] = t.z; v[k + 3] = t.w;
+      }
+#pragma unroll
+      for (int r = 0; r < K; ++r) {
+        float a = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; ++k) a = fmaf(P[r * K + k], v[k], a);
+        y[r] = a;
+      }
+#pragma unroll
+      for (int k = 0; k < K; k += 4)
+        *reinterpret_cast<float4*>(x + b + in_offset<K>(geo, k)) = make_float4(y[k], y[k + 1], y[k + 2], y[k + 3]);
+    }
+  }
+}
+
+// One-qubit adjoint (pairs of groups when Z >= 4, one contiguous group when
+// Z == 1): x = P^-1 x, g = P^T g, and
+// dP[r][k] = sum g_out[r] x_in[k] accumulated in FP32 registers, folded to
+// FP64 every 16 groups, reduced over the block and written to dst (16
+// doubles).
+__device__ void adjoint1_vec(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
+                             int64_t end, const float* P, const float* Pi, BatchSmem& sm, double* __restrict__ dst) {
+  float acc[16];
+  double* accd = sm.acc[threadIdx.x];  // FP64 running sums live in shared memory
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    acc[e] = 0.f;
+    accd[e] = 0.0;
+  }
+  auto one = [&](const float* xo, const float* go, float* xi, float* gn) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float a = 0.f, c = 0.f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        a = fmaf(Pi[r * 4 + k], xo[k], a);
+        c = fmaf(P[k * 4 + r], go[k], c);
+      }
+      xi[r] = a;
+      gn[r] = c;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[r * 4 + k] = fmaf(go[r], xi[k], acc[r * 4 + k]);
+  };
+  int since = 0;
+  if (geo.lz >= 2) {  // pairs of groups (z, z+1): 8-byte accesses
+    for (int64_t gi = beg + (int64_t)threadIdx.x * 2; gi < end; gi += (int64_t)blockDim.x * 2) {
+      const int64_t b = group_base(geo, gi);
+      float xv[4][2], gvv[4][2];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float2 a = *reinterpret_cast<const float2*>(x + b + in_offset<4>(geo, k));
+        const float2 c = *reinterpret_cast<const float2*>(gv + b + in_offset<4>(geo, k));
+        xv[k][0] = a.x; xv[k][1] = a.y;
+        gvv[k][0] = c.x; gvv[k][1] = c.y;
+      }
+      float xi[4][2], gn[4][2];
+#pragma unroll
+      for (int l = 0; l < 2; ++l) {
+        const float xo[4] = {xv[0][l], xv[1][l], xv[2][l], xv[3][l]};
+        const float go[4] = {gvv[0][l], gvv[1][l], gvv[2][l], gvv[3][l]};
+        float a[4], c[4];
+        one(xo, go, a, c);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          xi[r][l] = a[r];
+          gn[r][l] = c[r];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        *reinterpret_cast<float2*>(x + b + in_offset<4>(geo, r)) = make_float2(xi[r][0], xi[r][1]);
+        *reinterpret_cast<float2*>(gv + b + in_offset<4>(geo, r)) = make_float2(gn[r][0], gn[r][1]);
+      }
+      if (++since == 8) {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          accd[e] += (double)acc[e];
+          acc[e] = 0.f;
+        }
+        since = 0;
+      }
+    }
+  } else {
+    for (int64_t gi = beg + threadIdx.x; gi < end; gi += blockDim.x) {
+      const int64_t b = group_base(geo, gi);
+      const float4 a = *reinterpret_cast<const float4*>(x + b);
+      const float4 c = *reinterpret_cast<const float4*>(gv + b);
+      const float xo[4] = {a.x, a.y, a.z, a.w};
+      const float go[4] = {c.x, c.y, c.z, c.w};
+      float xi[4], gn[4];
+      one(xo, go, xi, gn);
+      *reinterpret_cast<float4*>(x + b) = make_float4(xi[0], xi[1], xi[2], xi[3]);
+      *reinterpret_cast<float4*>(gv + b) = make_float4(gn[0], gn[1], gn[2], gn[3]);
+      if (++since == 16) {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          accd[e] += (double)acc[e];
+          acc[e] = 0.f;
+        }
+        since = 0;
+      }
+    }
+  }
+  // block reduction: warps by shuffle, then across warps in shared memory
+  const int w = threadIdx.x >> 5;
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    double v = accd[e] + (double)acc[e];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sm.u.red[w][e] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 16) {
+    double s = 0.0;
+    for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) s += sm.u.red[ww][threadIdx.x];
+    dst[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
 // x = P^-1 x, g = P^T g on groups [beg, end); returns this thread's FP64
 // share of sum_g g_out (x) x_in, accumulated into acc (16 entries: a 4x4
 // sub-block for K = 16, one entry for K = 4).
@@ -304,20 +474,17 @@ __device__ void process(const qsgb_batch_program& p, const qsgb_batch_item& it, 
       __syncthreads();
       if (it.op == QSGB_BOP_APPLY) {
         if (geo.k == 4)
-          apply_groups<4>(in.x, geo, it.beg, it.end, sm.P);
+          apply_vec<4>(in.x, geo, it.beg, it.end, sm.P);
         else
-          apply_groups<16>(in.x, geo, it.beg, it.end, sm.P);
+          apply_vec<16>(in.x, geo, it.beg, it.end, sm.P);
+      } else if (geo.k == 4) {
+        adjoint1_vec(in.x, in.g, geo, it.beg, it.end, sm.P, sm.Pi, sm, p.grad_partial + (int64_t)it.slot * 256);
       } else {
 #pragma unroll
         for (int i = 0; i < 16; ++i) sm.acc[threadIdx.x][i] = 0.0;
         double* dst = p.grad_partial + (int64_t)it.slot * 256;
-        if (geo.k == 4) {
-          adjoint_groups<4>(in.x, in.g, geo, it.beg, it.end, sm);
-          store_partial<4>(dst, sm);
-        } else {
-          adjoint_groups<16>(in.x, in.g, geo, it.beg, it.end, sm);
-          store_partial<16>(dst, sm);
-        }
+        adjoint_groups<16>(in.x, in.g, geo, it.beg, it.end, sm);
+        store_partial<16>(dst, sm);
       }
       __syncthreads();
       break;
