@@ -15,6 +15,11 @@ CUDA-event duration against the measured HBM copy peak; ``cpu_baseline`` =
 the oracle (numpy einsum restatement of the reference backend) on the host
 cores for a bounded sample.
 
+``batched`` = the batched configuration: 512 circuits of 4..12 qubits, depth
+30, FP32 Pauli vectors with FP64 reductions, forward + adjoint of all of them
+in one persistent launch (CUDA graph), against the plain GPU path run one
+instance at a time, with the maximum probability error against FP64.
+
 ``--impl reference`` times the reference's CPU implementation of the path
 (the oracle port of PauliVectorNumpy, all host threads) on the same
 workload and prints the same line with ``"impl": "reference"``.
@@ -302,6 +307,13 @@ def run_gb300(args):
     h2d = APPS_PER_STEP * 16 * 16 * 8
     qops.check_device_status(dev)
 
+    # ---- batched FP32 forward + adjoint vs the plain path (rank 0, N = 1)
+    batched = None
+    if rank == 0 and world == 1 and not args.no_batched:
+        from quantumsim_gb300 import batch as qbatch
+        batched = qbatch.benchmark(n_instances=args.batch_instances,
+                                   f64_check='all')
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -341,6 +353,7 @@ def run_gb300(args):
             'gpu_launches': apps,
             'clocks': clocks,
             'per_target_gbs': per_target,
+            'batched': batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -406,6 +419,9 @@ def main():
     ap.add_argument('--cpu-apps', type=int, default=16)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-sweep', action='store_true')
+    ap.add_argument('--no-batched', action='store_true',
+                    help='skip the batched FP32 forward+adjoint measurement')
+    ap.add_argument('--batch-instances', type=int, default=512)
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', action='store_true',

@@ -434,3 +434,92 @@ def plain_gradients(spec, ptms, target, dtype=torch.float32,
                                  torch.zeros_like(t)))
     loss.backward()
     return prob.detach(), loss.detach(), [p.grad for p in params]
+
+
+def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
+              steps=3, autotune=True, f64_check='all', log=None):
+    """The batched configuration: `n_instances` circuits with qubit counts
+    uniform in [q_min, q_max], own seeded noise, `depth` layers; FP32 Pauli
+    vectors with FP64 probabilities / losses / PTM gradients.
+
+    Returns a dict with the batched gradient-step time (forward + adjoint of
+    every instance, one persistent launch replayed from a CUDA graph), the
+    plain GPU path's time (one instance at a time through ApplyPTM autograd,
+    timed once per qubit count and summed over the instances) and the
+    maximum probability error against FP64 (`f64_check`: 'all' instances or
+    one per qubit count)."""
+    say = log or (lambda *a: None)
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(q_min, q_max + 1, n_instances)
+    specs = [CircuitSpec(int(n), depth, 100 + i) for i, n in enumerate(ns)]
+    ptms = [instance_ptms(s) for s in specs]
+    uniform = [torch.full((2 ** s.n,), 1.0 / 2 ** s.n, dtype=torch.float64)
+               for s in specs]
+    t0 = time.perf_counter()
+    sim = BatchedSimulator(specs, uniform, checkpoint_every=8)
+    build_s = time.perf_counter() - t0
+    # targets: probabilities of the same circuits with perturbed angles
+    sim.set_ptms([instance_ptms(s, angle_offset=torch.from_numpy(
+        np.random.default_rng(7 + i).normal(0, 0.05, (depth, s.n))))
+        for i, s in enumerate(specs)])
+    sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    sim.target.copy_(sim.prob)
+    targets = [t.clone() for t in sim.results()[0]]
+    sim.set_ptms(ptms)
+    tuned = sim.autotune(candidates=(2048, 8192, 32768), reps=1) \
+        if autotune else None
+    say('batched: {} stages, {} items, tile {}'.format(
+        sim.n_stages, sim.n_items, sim.tile))
+    for _ in range(2):
+        sim.step(use_graph=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        sim.step(use_graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    step_s = e0.elapsed_time(e1) / 1e3 / steps
+    probs, loss, grads = sim.results()
+    # plain GPU path, one instance of every qubit count
+    plain = {}
+    for n in sorted(set(int(v) for v in ns)):
+        i = int(np.where(ns == n)[0][0])
+        plain_gradients(specs[i], ptms[i], targets[i])
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        plain_gradients(specs[i], ptms[i], targets[i])
+        torch.cuda.synchronize()
+        plain[n] = time.perf_counter() - a
+    plain_s = float(sum(plain[int(n)] for n in ns))
+    # probabilities against FP64 (the exact-arithmetic plain path)
+    from .pauli_vector import PauliVectorGB300
+    idx = range(n_instances) if f64_check == 'all' else \
+        [int(np.where(ns == n)[0][0]) for n in sorted(set(int(v) for v in ns))]
+    err = 0.0
+    for i in idx:
+        s = specs[i]
+        pv = PauliVectorGB300([_bases.general(2)] * s.n, force=True)
+        for pt, (_, qs) in zip(ptms[i], s.ops()):
+            arr = pt.numpy() if len(qs) == 1 else pt.numpy().reshape(4, 4, 4, 4)
+            pv.apply_ptm(arr, *qs)
+        d = pv.diagonal(get_data=False)
+        err = max(err, float((d - probs[i]).abs().max()))
+    total_entries = int(sum(4 ** int(n) for n in ns))
+    return {
+        'instances': n_instances, 'qubits': [q_min, q_max], 'depth': depth,
+        'entries_total': total_entries,
+        'storage': 'f32 Pauli vectors; f64 probabilities, losses, dL/dPTM',
+        'step_s': step_s, 'grad_steps_per_s': 1.0 / step_s,
+        'plain_step_s_est': plain_s,
+        'plain_per_qubits_s': {str(k): v for k, v in plain.items()},
+        'speedup_vs_plain': plain_s / step_s,
+        'max_prob_err_vs_f64': err,
+        'f64_checked_instances': len(list(idx)),
+        'tile': sim.tile, 'autotune_ms': tuned,
+        'stages': sim.n_stages, 'items': sim.n_items,
+        'program_build_s': build_s,
+        'launches_per_step': 1, 'cuda_graph': True,
+    }
