@@ -314,6 +314,11 @@ def run_gb300(args):
         batched = qbatch.benchmark(n_instances=args.batch_instances,
                                    f64_check='all')
 
+    extra = {}
+    if rank == 0 and world == 1 and not args.no_configs:
+        extra['qutrit_8q'] = run_qutrit_config()
+        extra['grad_10q'] = run_grad_config()
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -354,10 +359,68 @@ def run_gb300(args):
             'clocks': clocks,
             'per_target_gbs': per_target,
             'batched': batched,
+            'configs': extra,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_qutrit_config():
+    """8 qutrits (9^8 float64 entries, 344 MB): the 30-layer leakage
+    circuit with the mid-circuit basis reduction, projection and
+    renormalisation; plus per-application GB/s of the 9x9 and 81x81 PTMs."""
+    import numpy as np
+    import torch
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads
+    ops = workloads.config2_circuit(seed=2)
+    n_ptm = sum(1 for op in ops if op[0] == 'ptm')
+    for rep in range(2):  # the first pass compiles the PTM patterns
+        s = qg.PauliVectorGB300([bases.general(3)] * 8, force=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        traces = workloads.run(s, ops)
+        tr = s.trace()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    rng = np.random.default_rng(5)
+    s = qg.PauliVectorGB300([bases.general(3)] * 8, force=True)
+    nbytes = 2 * 9 ** 8 * 8
+    res = {'workload': '8 qutrits, 30 layers (9x9 and 81x81 PTMs), '
+                       'reduce+project 2 qutrits mid-circuit',
+           'circuit_s': dt, 'ptm_apps': n_ptm, 'apps_per_s': n_ptm / dt,
+           'renorm_trace': traces[0] if traces else None,
+           'final_trace': tr}
+    for name, ptm, qs in (('9x9_q4', workloads.qutrit_1q(rng), (4,)),
+                          ('81x81_q2_q5', workloads.qutrit_2q(rng), (2, 5)),
+                          ('81x81_q7_q6', workloads.qutrit_2q(rng), (7, 6))):
+        res[name + '_gbs'] = _time_app(s, ptm, qs, nbytes)
+    return res
+
+
+def run_grad_config():
+    """10 qubits, 40 layers, 249 physical parameters: one gradient step
+    (forward, KL loss, adjoint with checkpoints every 8 layers) in FP64 and
+    with FP32 storage."""
+    import torch
+    from quantumsim_gb300 import fitting
+    m = fitting.NoisyCircuitModel()
+    target = m.probabilities(m.perturbed()).detach()
+    out = {'params': m.n_params, 'qubits': m.n, 'layers': m.n_layers,
+           'checkpoint_every': 8}
+    for name, dtype in (('f64', torch.float64), ('f32', torch.float32)):
+        ts = []
+        for rep in range(3):
+            p = m.params()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            loss = m.loss(p, target, dtype=dtype, checkpoint_every=8)
+            loss.backward()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        out[name + '_step_s'] = min(ts[1:])
+    return out
 
 
 def qops_arith(name):
@@ -422,6 +485,8 @@ def main():
     ap.add_argument('--no-batched', action='store_true',
                     help='skip the batched FP32 forward+adjoint measurement')
     ap.add_argument('--batch-instances', type=int, default=512)
+    ap.add_argument('--no-configs', action='store_true',
+                    help='skip the qutrit and differentiation measurements')
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', action='store_true',
