@@ -473,6 +473,56 @@ def run_profile_case(args):
     print(json.dumps({'profile_case': n, 'trace': s.trace()}))
 
 
+def run_profile_qutrits(args):
+    """Small workload for ncu captures of the qutrit kernels: 8 qutrits
+    (9^8 float64 entries, 344 MB); one layer of 9x9 PTMs on every qutrit, then
+    3x [9x9 on qutrit 4, 81x81 CZ with leakage on (2, 5), the same on
+    (7, 6)].  Launch order: 8 setup applications, then 3 per repetition."""
+    import numpy as np
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads
+    rng = np.random.default_rng(5)
+    s = qg.PauliVectorGB300([bases.general(3)] * 8, force=True)
+    for q in range(8):
+        s.apply_ptm(workloads.qutrit_1q(rng), q)
+    p1 = workloads.qutrit_1q(rng)
+    p2 = workloads.qutrit_2q(rng)
+    for _ in range(3):
+        s.apply_ptm(p1, 4)
+        s.apply_ptm(p2, 2, 5)
+        s.apply_ptm(p2, 7, 6)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_case': 'qutrits', 'trace': s.trace()}))
+
+
+def run_profile_batched(args):
+    """Small workload for ncu captures of the batched kernel: 64 circuits of
+    4..10 qubits, depth 10, FP32; one plain (non-graph) launch after the
+    tile has been fixed, so the capture sees exactly one qsgb batch launch
+    per step; 2 steps."""
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    from quantumsim_gb300 import batch as BT
+    import numpy as np
+    rng = np.random.default_rng(0)
+    specs = [BT.CircuitSpec(int(n), 10, i)
+             for i, n in enumerate(rng.integers(4, 11, 64))]
+    targets = [BT.target_probabilities(sp, 1000 + i)
+               for i, sp in enumerate(specs)]
+    sim = BT.BatchedSimulator(specs, targets, checkpoint_every=4, tile=2048)
+    sim.set_ptms([BT.instance_ptms(sp) for sp in specs])
+    for _ in range(2):
+        sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    sim.check()
+    print(json.dumps({'profile_case': 'batched',
+                      'loss0': float(sim.results()[1][0])}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
     ap.add_argument('--gpus', type=int, default=1)
@@ -489,12 +539,14 @@ def main():
                     help='skip the qutrit and differentiation measurements')
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
-    ap.add_argument('--profile-case', action='store_true',
-                    help='run the small ncu profiling workload and exit')
+    ap.add_argument('--profile-case', nargs='?', const='apply',
+                    choices=['apply', 'qutrits', 'batched'],
+                    help='run a small ncu profiling workload and exit')
     ap.add_argument('--profile-qubits', type=int, default=12)
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args)
+        {'apply': run_profile_case, 'qutrits': run_profile_qutrits,
+         'batched': run_profile_batched}[args.profile_case](args)
         return
     if args.warmup < 3 and args.impl == 'gb300':
         print('warning: fewer than 3 warm-up steps', file=sys.stderr)

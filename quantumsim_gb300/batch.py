@@ -287,7 +287,8 @@ class BatchedSimulator:
     # ------------------------------------------------------------ PTMs
     def set_ptms(self, ptms_per_instance):
         """ptms_per_instance[i][j]: (K, K) float64 PTM of op j of instance i
-        (any device).  Builds the FP32 pool of P and P^-1 on the GPU."""
+        (any device).  Builds the FP32 pool of P and P^-1 on the GPU (the
+        inverses are computed on the host in FP64)."""
         flat = [p.reshape(p.shape[0], -1) if p.dim() == 2 else
                 p.reshape(16, 16) for ps in ptms_per_instance for p in ps]
         dev = self.device
@@ -296,8 +297,12 @@ class BatchedSimulator:
         for idx, K in ((one, 4), (two, 16)):
             if not idx:
                 continue
-            m = torch.stack([flat[k].to(dev, torch.float64) for k in idx])
-            inv = torch.linalg.inv(m)
+            # inverted on the host in float64: the matrices are tiny, and
+            # this keeps the device free of the solver libraries
+            m = torch.stack([flat[k].detach().to('cpu', torch.float64)
+                             for k in idx])
+            inv = torch.linalg.inv(m).to(dev)
+            m = m.to(dev)
             pool = torch.zeros(len(idx), 256, dtype=torch.float64,
                                device=dev)
             ipool = torch.zeros_like(pool)

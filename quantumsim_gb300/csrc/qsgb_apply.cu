@@ -564,105 +564,12 @@ int launch_apply(ApplyParams& p, cudaStream_t stream) {
 
 
 // ---------------------------------------------------------------------------
-// host-side planning of the run-time specialised kernel (see qsgb_jit.cu)
+// run-time specialised kernel (qsgb_jit.cu)
 // ---------------------------------------------------------------------------
-// Row modes for the specialised kernel under QSGB_ARITH_AUTO: rows in
-// ascending term count are computed in FP64 while that lowers the larger of
-// the estimated times per group (SM clock cycles) of HBM traffic, the FP64
-// pipe (~1.6 ops/clk sustained in these kernels), the integer pipe (64 lanes/clk: ~16 ops per split
-// input, ~30 per float-float row result) and instruction issue (128/clk;
-// ~12 per float-float term).
-void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, size_t esz, std::vector<int>& mode) {
-  const int kout = (int)cols.size();
-  mode.assign(kout, jit::kModeZero);
-  for (int r = 0; r < kout; ++r) {
-    const int n = (int)cols[r].size();
-    if (n == 0) continue;
-    if (arith == QSGB_ARITH_F32) mode[r] = jit::kModeF32;
-    else if (arith == QSGB_ARITH_F64 || n == 1) mode[r] = jit::kModeDP;
-    else mode[r] = jit::kModeDF;
-  }
-  if (arith != QSGB_ARITH_AUTO) return;
-  std::vector<int> order;
-  for (int r = 0; r < kout; ++r)
-    if (cols[r].size() > 1) order.push_back(r);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cols[a].size() < cols[b].size(); });
-  auto cost = [&](const std::vector<int>& m) {
-    double dp = 0, alu = 0, issue = 0;
-    std::vector<char> split(kin, 0);
-    int n_used = 0;
-    std::vector<char> used(kin, 0);
-    for (int r = 0; r < kout; ++r) {
-      for (int k : cols[r]) {
-        if (!used[k]) {
-          used[k] = 1;
-          ++n_used;
-        }
-        if (m[r] == jit::kModeDF) split[k] = 1;
-      }
-      if (m[r] == jit::kModeDP) {
-        dp += (double)cols[r].size();
-        issue += (double)cols[r].size();
-      } else if (m[r] == jit::kModeDF) {
-        issue += 12.0 * cols[r].size() + 30.0;
-        alu += 30.0;
-      }
-    }
-    for (int k = 0; k < kin; ++k)
-      if (split[k]) {
-        alu += 16.0;
-        issue += 16.0;
-      }
-    issue += 2.0 * (n_used + kout);
-    const double hbm = (double)(kin + kout) * (double)esz / 23.0;
-    return std::max(std::max(hbm, dp / 1.6), std::max(alu / 64.0, issue / 128.0));
-  };
-  std::vector<int> m = mode;
-  double best = cost(m);
-  std::vector<int> best_m = m;
-  for (int r : order) {
-    m[r] = jit::kModeDP;
-    const double c = cost(m);
-    if (c < best * 0.999) {
-      best = c;
-      best_m = m;
-    }
-  }
-  mode = best_m;
-}
-
 // Returns QSGB_ERR_UNSUPPORTED when the specialised path does not apply.
 int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_in, int64_t db_in, int64_t Z,
             int flags, int dtype, int arith, bool pair, ApplyParams& p, cudaStream_t stream) {
   if (!(flags & QSGB_PTM_HOST) || (flags & QSGB_PTM_NOJIT) || !jit::available()) return QSGB_ERR_UNSUPPORTED;
-  const int kin = (int)(da_in * db_in), kout = (int)(da_out * db_out);
-  if (kin > 81 || kout > 81) return QSGB_ERR_UNSUPPORTED;
-  // op matrix M[r][k] from the stored layout (same mapping as ptm_index)
-  std::vector<double> M((size_t)kin * kout);
-  double amax = 0.0;
-  for (int r = 0; r < kout; ++r)
-    for (int k = 0; k < kin; ++k) {
-      const int ra = r / (int)db_out, rb = r % (int)db_out;
-      const int ka = k / (int)db_in, kb = k % (int)db_in;
-      int idx;
-      switch (flags & 3) {
-        case 0: idx = r * kin + k; break;
-        case QSGB_PTM_SWAPPED: idx = ((rb * (int)da_out + ra) * (int)db_in + kb) * (int)da_in + ka; break;
-        case QSGB_PTM_TRANSPOSED: idx = k * kout + r; break;
-        default: idx = ((kb * (int)da_in + ka) * (int)db_out + rb) * (int)da_out + ra; break;
-      }
-      const double v = ptm_host[idx];
-      M[(size_t)r * kin + k] = v;
-      amax = std::max(amax, std::fabs(v));
-    }
-  const double thr = arith == QSGB_ARITH_F64 ? 0.0 : amax * (arith == QSGB_ARITH_F32 ? 0x1p-30 : 0x1p-52);
-  jit::Spec spec;
-  spec.kin = kin;
-  spec.kout = kout;
-  spec.db_in = (int)db_in;
-  spec.db_out = (int)db_out;
-  spec.pair = pair;
-  spec.f32 = dtype == QSGB_F32;
   // Z == 1: the db inputs (outputs) of a group along the less significant
   // target are contiguous; move them with 2- or 4-wide vector accesses
   auto vwidth = [&](int64_t db, const void* ptr) {
@@ -672,30 +579,15 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
       if (db % w == 0 && (uintptr_t)ptr % (w * esz) == 0) return w;
     return 1;
   };
-  spec.vin = vwidth(db_in, p.in);
-  spec.vout = vwidth(db_out, p.out);
-  spec.cols.assign(kout, {});
-  for (int r = 0; r < kout; ++r)
-    for (int k = 0; k < kin; ++k)
-      if (std::fabs(M[(size_t)r * kin + k]) > thr) spec.cols[r].push_back(k);
-  plan_modes(spec.cols, kin, arith, dtype == QSGB_F64 ? 8 : 4, spec.mode);
+  jit::Spec spec;
   std::vector<double> coef;
-  coef.reserve(spec.n_coef());
-  for (int r = 0; r < kout; ++r)
-    for (int k : spec.cols[r]) {
-      const double v = M[(size_t)r * kin + k];
-      if (spec.mode[r] == jit::kModeDF) {
-        const float h = (float)v;
-        const float l = (float)(v - (double)h);
-        uint64_t bits = ((uint64_t)__builtin_bit_cast(uint32_t, h) << 32) | __builtin_bit_cast(uint32_t, l);
-        coef.push_back(__builtin_bit_cast(double, bits));
-      } else if (spec.mode[r] == jit::kModeF32) {
-        uint64_t bits = __builtin_bit_cast(uint32_t, (float)v);
-        coef.push_back(__builtin_bit_cast(double, bits));
-      } else {
-        coef.push_back(v);
-      }
-    }
+  // groups of consecutive items are adjacent (item it starts at it * K) when
+  // Z == 1 and either Y == 1 (two adjacent last qudits) or Da == 1 (one qudit)
+  const bool contiguous = Z == 1 && (p.div_y.d == 1 || (da_in == 1 && da_out == 1)) &&
+                          (uintptr_t)p.in % 16 == 0 && (uintptr_t)p.out % 16 == 0;
+  if (!jit::make_spec(ptm_host, (int)da_out, (int)db_out, (int)da_in, (int)db_in, flags & 3, dtype, arith, pair,
+                      Z == 1, contiguous, vwidth(db_in, p.in), vwidth(db_out, p.out), spec, coef))
+    return QSGB_ERR_UNSUPPORTED;
   const int NL = pair ? 2 : 1;
   jit::Geometry g;
   g.in = p.in;

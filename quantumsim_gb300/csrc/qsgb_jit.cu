@@ -5,22 +5,23 @@
 // a sparse PTM.  When the PTM is on the host, this module instead emits the
 // CUDA source of a kernel specialised to the PTM's *sparsity pattern* (which
 // entries are non-zero, and for each row whether it is computed in FP64 or
-// float-float), compiles it for sm_103a with NVRTC, and caches it by source
-// text.  The PTM *values* travel in the kernel parameters, so every PTM with
-// the same pattern (e.g. every noisy CZ, whatever its T1/T2) reuses one
-// compiled kernel.  The generated kernel keeps the Kin inputs of an item in
-// registers, unrolls every row, and issues one load and one store per
-// element.
+// float-float), compiles it for sm_103a with NVRTC, and caches it (in
+// process by pattern, on disk by source text).  The PTM *values* travel in
+// the kernel parameters, so every PTM with the same pattern (e.g. every
+// noisy CZ, whatever its T1/T2) reuses one compiled kernel.  The generated
+// kernel holds an item's inputs in registers, unrolls every row, and issues
+// one load and one store per element.
 //
 // NVRTC is loaded with dlopen on first use; if it is missing or a
-// compilation fails, qsgb_jit_apply() returns QSGB_ERR_UNSUPPORTED and the
-// caller uses the generic kernel.
+// compilation fails, launch() returns QSGB_ERR_UNSUPPORTED and the caller
+// uses the generic kernel.
 #include <dlfcn.h>
 #include <nvrtc.h>
 #include <sys/stat.h>
 #include <unistd.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -85,6 +86,11 @@ struct Hdr {
 };
 static_assert(sizeof(Hdr) == 18 * 8, "header layout");
 constexpr int kMaxCoef = (32764 - (int)sizeof(Hdr)) / 8;
+// Patterns with more terms are left to the generic kernel: they are
+// arithmetic-bound whatever the code, and NVRTC needs 12-65 s for a 2000-term
+// 81x81 pattern (255 registers plus spills), against ~1 s for the sparse
+// PTMs of physical gates (<= 256 terms).
+constexpr int kMaxJitTerms = 1024;
 
 const char* kHdrSrc =
     "struct H { const void* in; void* out; unsigned* status; qsgb_u64 n_items;\n"
@@ -92,6 +98,63 @@ const char* kHdrSrc =
     "  qsgb_i64 sxi, syi, sai, sbi, sxo, syo, sao, sbo; };\n";
 
 // ------------------------------------------------------------------ codegen
+// Component id (its smallest row) of every row of the row/column graph: two
+// rows are connected when they read a common input.
+std::vector<int> row_components(const Spec& s) {
+  std::vector<int> parent(s.kout);
+  for (int r = 0; r < s.kout; ++r) parent[r] = r;
+  auto find = [&](int r) {
+    while (parent[r] != r) r = parent[r] = parent[parent[r]];
+    return r;
+  };
+  std::vector<int> first_row(s.kin, -1);
+  for (int r = 0; r < s.kout; ++r)
+    for (int k : s.cols[r]) {
+      if (first_row[k] < 0) {
+        first_row[k] = r;
+      } else {
+        const int a = find(first_row[k]), b = find(r);
+        if (a != b) parent[std::max(a, b)] = std::min(a, b);
+      }
+    }
+  std::vector<int> comp(s.kout);
+  for (int r = 0; r < s.kout; ++r) comp[r] = find(r);
+  return comp;
+}
+
+// Rows grouped by component, components in order of their first row, rows
+// ascending within a component.
+std::vector<int> row_order(const Spec& s) {
+  const std::vector<int> comp = row_components(s);
+  std::vector<std::vector<int>> members(s.kout);
+  for (int r = 0; r < s.kout; ++r) members[comp[r]].push_back(r);
+  std::vector<int> order;
+  order.reserve(s.kout);
+  for (int r = 0; r < s.kout; ++r)
+    for (int m : members[r]) order.push_back(m);
+  return order;
+}
+
+// A staged kernel writes each component's results over the tile slots of
+// their own row indices; that is safe when no later component reads those
+// slots as inputs.
+bool staged_in_place_ok(const Spec& s) {
+  if (s.lookahead >= s.kin) return true;  // all inputs are read before any write
+  const std::vector<int> order = row_order(s);
+  const std::vector<int> comp = row_components(s);
+  std::vector<int> at(s.kout);
+  for (size_t i = 0; i < order.size(); ++i) at[order[i]] = (int)i;
+  // position of the last row of each component, and of the last reader of each input
+  std::vector<int> comp_end(s.kout, -1), last_read(s.kin, -1);
+  for (int r = 0; r < s.kout; ++r) {
+    comp_end[comp[r]] = std::max(comp_end[comp[r]], at[r]);
+    for (int k : s.cols[r]) last_read[k] = std::max(last_read[k], at[r]);
+  }
+  for (int r = 0; r < s.kout && r < s.kin; ++r)
+    if (last_read[r] > comp_end[comp[r]]) return false;
+  return true;
+}
+
 std::string gen_source(const Spec& s) {
   const int NL = s.pair ? 2 : 1;
   const bool f32 = s.f32;
@@ -125,6 +188,110 @@ std::string gen_source(const Spec& s) {
                   cs, scal, scal, scal, scal, scal, ty, cs, cs, cs, cs);
     src += buf;
   }
+  const int KS = std::max(s.kin, s.kout);  // staged tile: values per item
+  if (s.stage_warps) {
+    // Z == 1 with odd (or unaligned) target dims: each warp stages the items
+    // of 32 consecutive groups in shared memory with coalesced copies,
+    // computes from there, and writes the results back through the same
+    // tile.  When the 32 groups form one contiguous span (stage_bulk: one
+    // qudit, or two adjacent last qudits; square PTM), one bulk copy (TMA,
+    // completion on an mbarrier) moves the tile each way; a tile whose size
+    // is not a multiple of 16 bytes uses the per-element copies.
+    const int esz = f32 ? 4 : 8;
+    std::snprintf(buf, sizeof buf,
+                  "extern \"C\" __global__ void __launch_bounds__(%d) qsgb_jit(const __grid_constant__ P p) {\n"
+                  "  typedef %s V;\n"
+                  "  __shared__ __align__(128) V tiles[%d][32 * %d];\n"
+                  "  V* const t = tiles[threadIdx.x >> 5];\n"
+                  "  const unsigned lane = threadIdx.x & 31u;\n"
+                  "  const V* __restrict__ in = (const V*)p.h.in;\n"
+                  "  V* __restrict__ out = (V*)p.h.out;\n"
+                  "  const unsigned tb = (unsigned)__cvta_generic_to_shared(t);\n"
+                  "  unsigned bad_all = 0;\n",
+                  32 * s.stage_warps, scal, s.stage_warps, KS);
+    src += buf;
+    if (s.stage_bulk) {
+      std::snprintf(buf, sizeof buf,
+                    "  __shared__ __align__(8) qsgb_u64 bars[%d];\n"
+                    "  const unsigned bar = (unsigned)__cvta_generic_to_shared(&bars[threadIdx.x >> 5]);\n"
+                    "  if (lane == 0) {\n"
+                    "    asm volatile(\"mbarrier.init.shared::cta.b64 [%%0], 1;\" :: \"r\"(bar) : \"memory\");\n"
+                    "    asm volatile(\"fence.proxy.async.shared::cta;\" ::: \"memory\");\n"
+                    "  }\n"
+                    "  __syncwarp();\n"
+                    "  unsigned phase = 0;\n",
+                    s.stage_warps);
+      src += buf;
+    }
+    std::snprintf(buf, sizeof buf,
+                  "  const qsgb_u64 n_tiles = (p.h.n_items + 31) >> 5;\n"
+                  "  const qsgb_u64 wstride = (qsgb_u64)gridDim.x * %d;\n"
+                  "  for (qsgb_u64 wt = (qsgb_u64)blockIdx.x * %d + (threadIdx.x >> 5); wt < n_tiles; wt += wstride) "
+                  "{\n"
+                  "    const qsgb_u64 left = p.h.n_items - wt * 32;\n"
+                  "    const unsigned nv = left < 32 ? (unsigned)left : 32u;\n"
+                  "    qsgb_i64 bi = 0, bo = 0;\n"
+                  "    if (lane < nv) {\n"
+                  "      const qsgb_u64 it = wt * 32 + lane;\n"
+                  "      const qsgb_u64 xx = qsgb_fdiv(it, p.h.ym, (int)p.h.yl);\n"
+                  "      const qsgb_u64 yy = it - xx * p.h.yd;\n"
+                  "      bi = (qsgb_i64)xx * p.h.sxi + (qsgb_i64)yy * p.h.syi;\n"
+                  "      bo = (qsgb_i64)xx * p.h.sxo + (qsgb_i64)yy * p.h.syo;\n"
+                  "    }\n"
+                  "    unsigned bad = 0;\n",
+                  s.stage_warps, s.stage_warps);
+    src += buf;
+    if (s.stage_bulk) {
+      std::snprintf(buf, sizeof buf,
+                    "    const unsigned nbytes = nv * %du;\n"
+                    "    const bool bulk = (nbytes & 15u) == 0u;\n"
+                    "    if (bulk) {\n"
+                    "      if (lane == 0) {\n"
+                    "        // the previous tile's store has finished reading the tile\n"
+                    "        asm volatile(\"cp.async.bulk.wait_group.read 0;\" ::: \"memory\");\n"
+                    "        asm volatile(\"mbarrier.arrive.expect_tx.shared::cta.b64 _, [%%0], %%1;\" :: \"r\"(bar), "
+                    "\"r\"(nbytes) : \"memory\");\n"
+                    "        asm volatile(\"cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%%0], "
+                    "[%%1], %%2, [%%3];\" :: \"r\"(tb), \"l\"(in + wt * %du), \"r\"(nbytes), \"r\"(bar) : \"memory\");\n"
+                    "      }\n"
+                    "      // bounded wait for the tile (parity of this warp's barrier phase)\n"
+                    "      unsigned ok = 0;\n"
+                    "      for (unsigned spin = 0; spin < (1u << 24) && !ok; ++spin) {\n"
+                    "        unsigned w;\n"
+                    "        asm volatile(\"{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%%1], %%2; "
+                    "selp.u32 %%0, 1, 0, q; }\" : \"=r\"(w) : \"r\"(bar), \"r\"(phase) : \"memory\");\n"
+                    "        ok = __all_sync(0xffffffffu, w != 0u);\n"
+                    "      }\n"
+                    "      phase ^= 1u;\n"
+                    "      if (!ok) {\n"
+                    "        if (lane == 0 && p.h.status) atomicOr(p.h.status, 2u);\n"
+                    "        break;\n"
+                    "      }\n"
+                    "    } else {\n"
+                    "      if (lane == 0) asm volatile(\"cp.async.bulk.wait_group.read 0;\" ::: \"memory\");\n"
+                    "      __syncwarp();\n",
+                    KS * esz, 32 * KS);
+      src += buf;
+    }
+    std::snprintf(buf, sizeof buf,
+                  "    // coalesced global -> shared copies (cp.async: no registers held)\n"
+                  "#pragma unroll 3\n"
+                  "    for (int ka = 0; ka < %d; ++ka) {\n"
+                  "#pragma unroll\n"
+                  "      for (int j = 0; j < %d; ++j) {\n"
+                  "        const unsigned f = lane + 32u * j, i = f / %du, kb = f - i * %du;\n"
+                  "        const qsgb_i64 src = __shfl_sync(0xffffffffu, bi, i);\n"
+                  "        if (i < nv)\n"
+                  "          asm volatile(\"cp.async.ca.shared.global [%%0], [%%1], %d;\" :: \"r\"(tb + (i * %du + ka * "
+                  "%du + kb) * %du), \"l\"(in + src + ka * p.h.sai + kb) : \"memory\");\n"
+                  "      }\n"
+                  "    }\n"
+                  "    asm volatile(\"cp.async.wait_all;\" ::: \"memory\");\n"
+                  "%s"
+                  "    __syncwarp();\n",
+                  s.kin / s.db_in, s.db_in, s.db_in, s.db_in, esz, KS, s.db_in, esz, s.stage_bulk ? "    }\n" : "");
+    src += buf;
+  } else {
   std::snprintf(buf, sizeof buf,
                 "extern \"C\" __global__ void __launch_bounds__(128) qsgb_jit(const __grid_constant__ P p) {\n"
                 "  typedef %s V;\n"
@@ -142,54 +309,106 @@ std::string gen_source(const Spec& s) {
                 "    const qsgb_i64 bo = (qsgb_i64)xx * p.h.sxo + (qsgb_i64)yy * p.h.syo + (qsgb_i64)zi;\n",
                 V);
   src += buf;
-  // which inputs are used, and which feed df rows
-  std::vector<char> used(s.kin, 0), split(s.kin, 0);
-  for (int r = 0; r < s.kout; ++r)
-    for (int k : s.cols[r]) {
-      used[k] = 1;
-      if (s.mode[r] == kModeDF) split[k] = 1;
-    }
+  }
   const char* lanes[2] = {s.pair ? ".x" : "", ".y"};
-  if (s.vin > 1) {  // Z == 1: runs of vin inputs along kb are contiguous
-    for (int k0 = 0; k0 < s.kin; k0 += s.vin) {
-      bool any = false;
-      for (int j = 0; j < s.vin; ++j) any |= used[k0 + j] != 0;
-      if (!any) continue;
-      const int ka = k0 / s.db_in, kb = k0 % s.db_in;
+  // Small items load (and split) every input first and emit rows in natural
+  // order.  Large ones emit rows component by component (rows that share an
+  // input form one component of the row/column graph), each input loaded a
+  // few inputs ahead of its first use, so the live registers of an item are
+  // those of a few components rather than all Kin inputs.  Every result is
+  // stored as soon as it (or its vector of vout results) is complete.
+  std::vector<int> order(s.kout);
+  if (s.lookahead >= s.kin) {
+    for (int r = 0; r < s.kout; ++r) order[r] = r;
+  } else {
+    order = row_order(s);
+  }
+  // comp_last[r]: r is the last row (in `order`) of its component; with all
+  // inputs loaded first the whole row set counts as one component
+  std::vector<char> comp_last(s.kout, 0);
+  {
+    const std::vector<int> comp = row_components(s);
+    for (size_t i = 0; i < order.size(); ++i) {
+      const bool last = i + 1 == order.size() ||
+                        (s.lookahead < s.kin && comp[order[i + 1]] != comp[order[i]]);
+      comp_last[order[i]] = last ? 1 : 0;
+    }
+  }
+  std::vector<int> pending;
+  std::vector<int> ci0(s.kout + 1, 0);
+  for (int r = 0; r < s.kout; ++r) ci0[r + 1] = ci0[r] + (int)s.cols[r].size();
+  std::vector<char> loaded(s.kin, 0), splitd(s.kin, 0), done(s.kout, 0);
+  auto load = [&](int k) {
+    if (s.vin > 1) {  // Z == 1: runs of vin inputs along kb are contiguous
+      const int k0 = k - k % s.vin;
+      if (loaded[k0]) return;
       std::string vars;
       for (int j = 0; j < s.vin; ++j) {
+        loaded[k0 + j] = 1;
         std::snprintf(buf, sizeof buf, "    V x%d;\n", k0 + j);
         src += buf;
         vars += ", x" + std::to_string(k0 + j);
       }
-      std::snprintf(buf, sizeof buf, "    qld%d((const V*)p.h.in + bi + %dLL * p.h.sai + %d%s);\n", s.vin, ka, kb,
-                    vars.c_str());
+      std::snprintf(buf, sizeof buf, "    qld%d((const V*)p.h.in + bi + %dLL * p.h.sai + %d%s);\n", s.vin,
+                    k0 / s.db_in, k0 % s.db_in, vars.c_str());
+      src += buf;
+    } else {
+      if (loaded[k]) return;
+      loaded[k] = 1;
+      if (s.stage_warps)
+        std::snprintf(buf, sizeof buf, "    const V x%d = t[lane * %d + %d];\n", k, KS, k);
+      else
+        std::snprintf(buf, sizeof buf, "    const V x%d = in[bi + %dLL * p.h.sai + %dLL * p.h.sbi];\n", k,
+                      k / s.db_in, k % s.db_in);
       src += buf;
     }
-  } else {
-    for (int k = 0; k < s.kin; ++k) {
-      if (!used[k]) continue;
-      const int ka = k / s.db_in, kb = k % s.db_in;
-      std::snprintf(buf, sizeof buf, "    const V x%d = in[bi + %dLL * p.h.sai + %dLL * p.h.sbi];\n", k, ka, kb);
-      src += buf;
-    }
-  }
-  for (int k = 0; k < s.kin; ++k) {
-    if (!split[k]) continue;
+  };
+  auto split_input = [&](int k) {
+    if (splitd[k]) return;
+    splitd[k] = 1;
     for (int l = 0; l < NL; ++l) {
       std::snprintf(buf, sizeof buf, "    float h%d_%d, l%d_%d; qsgb_split_f64(x%d%s, h%d_%d, l%d_%d, bad);\n", k, l, k,
                     l, k, lanes[l], k, l, k, l);
       src += buf;
     }
-  }
+  };
   for (int r = 0; r < s.kout; ++r) {
     std::snprintf(buf, sizeof buf, "    V y%d;\n", r);
     src += buf;
   }
-  int ci = 0;
-  for (int r = 0; r < s.kout; ++r) {
+  // loads run `lookahead` inputs ahead of their first use
+  std::vector<int> seq, pos(s.kin, 0);
+  {
+    std::vector<char> seen(s.kin, 0);
+    for (int r : order)
+      for (int k : s.cols[r])
+        if (!seen[k]) {
+          seen[k] = 1;
+          pos[k] = (int)seq.size();
+          seq.push_back(k);
+        }
+  }
+  size_t lp = 0;
+  auto load_upto = [&](size_t n) {
+    for (; lp < seq.size() && lp < n; ++lp) load(seq[lp]);
+  };
+  load_upto((size_t)s.lookahead);
+  if (s.lookahead >= s.kin) {  // small items: everything loaded and split up front
+    for (int r = 0; r < s.kout; ++r)
+      if (s.mode[r] == kModeDF)
+        for (int k : s.cols[r]) split_input(k);
+  }
+  for (int r : order) {
     const int ra = r / s.db_out, rb = r % s.db_out;
     const auto& cols = s.cols[r];
+    size_t need = 0;
+    for (int k : cols) need = std::max(need, (size_t)pos[k] + 1);
+    load_upto(need + (size_t)s.lookahead);
+    for (int k : cols) {
+      load(k);
+      if (s.mode[r] == kModeDF) split_input(k);
+    }
+    const int ci = ci0[r];
     src += "    {\n";
     std::string vals[2];
     for (int l = 0; l < NL; ++l) {
@@ -235,11 +454,23 @@ std::string gen_source(const Spec& s) {
       src += "      y" + std::to_string(r) + " = " + vals[0] + ";\n";
     }
     src += "    }\n";
-    ci += (int)cols.size();
-    // store as soon as a row (or a vector of vout rows) is complete
-    if (s.vout > 1) {
-      if ((r + 1) % s.vout == 0) {
-        const int r0 = r + 1 - s.vout;
+    done[r] = 1;
+    if (s.stage_warps) {
+      // results go to the tile once every row of the component (every row,
+      // when all inputs were loaded first) is done
+      pending.push_back(r);
+      if (comp_last[r]) {
+        for (int q : pending) {
+          std::snprintf(buf, sizeof buf, "    t[lane * %d + %d] = y%d;\n", KS, q, q);
+          src += buf;
+        }
+        pending.clear();
+      }
+    } else if (s.vout > 1) {
+      const int r0 = r - r % s.vout;
+      bool full = true;
+      for (int j = 0; j < s.vout; ++j) full &= done[r0 + j] != 0;
+      if (full) {
         std::string vars;
         for (int j = 0; j < s.vout; ++j) vars += ", y" + std::to_string(r0 + j);
         std::snprintf(buf, sizeof buf, "    qst%d((V*)p.h.out + bo + %dLL * p.h.sao + %d%s);\n", s.vout,
@@ -251,7 +482,44 @@ std::string gen_source(const Spec& s) {
       src += buf;
     }
   }
-  src += "  }\n  if (bad && p.h.status) atomicOr(p.h.status, 1u);\n}\n";
+  if (s.stage_warps) {
+    src += "    __syncwarp();\n";
+    if (s.stage_bulk) {
+      // generic-proxy tile writes -> visible to the bulk (async-proxy) store
+      std::snprintf(buf, sizeof buf,
+                    "    if (bulk) {\n"
+                    "      asm volatile(\"fence.proxy.async.shared::cta;\" ::: \"memory\");\n"
+                    "      __syncwarp();\n"
+                    "      if (lane == 0) {\n"
+                    "        asm volatile(\"cp.async.bulk.global.shared::cta.bulk_group [%%0], [%%1], %%2;\" :: "
+                    "\"l\"(out + wt * %du), \"r\"(tb), \"r\"(nbytes) : \"memory\");\n"
+                    "        asm volatile(\"cp.async.bulk.commit_group;\" ::: \"memory\");\n"
+                    "      }\n"
+                    "    } else {\n",
+                    32 * KS);
+      src += buf;
+    }
+    std::snprintf(buf, sizeof buf,
+                  "#pragma unroll 1\n"
+                  "    for (int ra = 0; ra < %d; ++ra) {\n"
+                  "#pragma unroll\n"
+                  "      for (int j = 0; j < %d; ++j) {\n"
+                  "        const unsigned f = lane + 32u * j, i = f / %du, rb = f - i * %du;\n"
+                  "        const qsgb_i64 dst = __shfl_sync(0xffffffffu, bo, i);\n"
+                  "        if (i < nv) out[dst + ra * p.h.sao + rb] = t[i * %d + ra * %d + rb];\n"
+                  "      }\n"
+                  "    }\n"
+                  "%s"
+                  "    __syncwarp();\n"
+                  "    if (lane < nv) bad_all |= bad;\n"
+                  "  }\n",
+                  s.kout / s.db_out, s.db_out, s.db_out, s.db_out, KS, s.db_out, s.stage_bulk ? "    }\n" : "");
+    src += buf;
+    if (s.stage_bulk) src += "  if (lane == 0) asm volatile(\"cp.async.bulk.wait_group 0;\" ::: \"memory\");\n";
+    src += "  if (bad_all && p.h.status) atomicOr(p.h.status, 1u);\n}\n";
+  } else {
+    src += "  }\n  if (bad && p.h.status) atomicOr(p.h.status, 1u);\n}\n";
+  }
   return src;
 }
 
@@ -358,6 +626,76 @@ int compile(const std::string& src, cudaKernel_t* out) {
   return st;
 }
 
+// ------------------------------------------------------------------ planning
+// Row modes for the specialised kernel under QSGB_ARITH_AUTO: rows in
+// ascending term count are computed in FP64 while that lowers the combined
+// estimated times per group (SM clock cycles) of HBM traffic, the FP64
+// pipe (~1.6 ops/clk sustained in these kernels), the integer pipe (64 lanes/clk: ~16 ops per split
+// input, ~30 per float-float row result) and instruction issue (128/clk;
+// ~12 per float-float term).
+void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, size_t esz, std::vector<int>& mode) {
+  const int kout = (int)cols.size();
+  mode.assign(kout, kModeZero);
+  for (int r = 0; r < kout; ++r) {
+    const int n = (int)cols[r].size();
+    if (n == 0) continue;
+    if (arith == QSGB_ARITH_F32) mode[r] = kModeF32;
+    else if (arith == QSGB_ARITH_F64 || n == 1) mode[r] = kModeDP;
+    else mode[r] = kModeDF;
+  }
+  if (arith != QSGB_ARITH_AUTO) return;
+  std::vector<int> order;
+  for (int r = 0; r < kout; ++r)
+    if (cols[r].size() > 1) order.push_back(r);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cols[a].size() < cols[b].size(); });
+  auto cost = [&](const std::vector<int>& m) {
+    double dp = 0, alu = 0, issue = 0;
+    std::vector<char> split(kin, 0);
+    int n_used = 0;
+    std::vector<char> used(kin, 0);
+    for (int r = 0; r < kout; ++r) {
+      for (int k : cols[r]) {
+        if (!used[k]) {
+          used[k] = 1;
+          ++n_used;
+        }
+        if (m[r] == kModeDF) split[k] = 1;
+      }
+      if (m[r] == kModeDP) {
+        dp += (double)cols[r].size();
+        issue += (double)cols[r].size();
+      } else if (m[r] == kModeDF) {
+        issue += 12.0 * cols[r].size() + 30.0;
+        alu += 30.0;
+      }
+    }
+    for (int k = 0; k < kin; ++k)
+      if (split[k]) {
+        alu += 16.0;
+        issue += 16.0;
+      }
+    issue += 2.0 * (n_used + kout);
+    const double hbm = (double)(kin + kout) * (double)esz / 23.0;
+    // the four times overlap imperfectly: a 6-norm rather than their maximum
+    // (measured on GB300: 9x9 qutrit PTM 4853 -> 5539 GB/s, dense 16x16 and
+    // the qubit PTMs unchanged)
+    auto p6 = [](double t) { return t * t * t * t * t * t; };
+    return std::pow(p6(hbm) + p6(dp / 1.6) + p6(alu / 64.0) + p6(issue / 128.0), 1.0 / 6.0);
+  };
+  std::vector<int> m = mode;
+  double best = cost(m);
+  std::vector<int> best_m = m;
+  for (int r : order) {
+    m[r] = kModeDP;
+    const double c = cost(m);
+    if (c < best * 0.999) {
+      best = c;
+      best_m = m;
+    }
+  }
+  mode = best_m;
+}
+
 }  // namespace
 
 int Spec::n_coef() const {
@@ -366,30 +704,126 @@ int Spec::n_coef() const {
   return n;
 }
 
+// How many inputs the generated loads run ahead of their first use.  Items
+// of up to 36 values (16x16 pairs, 9x9) load everything first and compute
+// rows in natural order; larger ones (81x81) go component by component with
+// loads 8 inputs ahead, which keeps them near 80 registers instead of 255.
+// Measured on GB300 (GB/s, 14 qubits / 8 qutrits): everything first gives
+// noisy CZ 6354 and 81x81 on (2, 5) 2477; components with lookahead 8 give
+// 6326 and 4863; lookahead 16 to 255 lose up to 18 % on the CZ pair kernel.
+int lookahead_for(int kin, bool pair) { return kin * (pair ? 2 : 1) <= 36 ? kin : 8; }
+
+bool make_spec(const double* ptm_host, int da_out, int db_out, int da_in, int db_in, int layout, int dtype,
+               int arith, bool pair, bool z1, bool contiguous, int vin, int vout, Spec& spec,
+               std::vector<double>& coef) {
+  const int kin = da_in * db_in, kout = da_out * db_out;
+  if (kin > 81 || kout > 81) return false;
+  // op matrix M[r][k] from the stored layout (the generic kernel's ptm_index)
+  std::vector<double> M((size_t)kin * kout);
+  double amax = 0.0;
+  for (int r = 0; r < kout; ++r)
+    for (int k = 0; k < kin; ++k) {
+      const int ra = r / db_out, rb = r % db_out;
+      const int ka = k / db_in, kb = k % db_in;
+      int idx;
+      switch (layout & 3) {
+        case 0: idx = r * kin + k; break;
+        case QSGB_PTM_SWAPPED: idx = ((rb * da_out + ra) * db_in + kb) * da_in + ka; break;
+        case QSGB_PTM_TRANSPOSED: idx = k * kout + r; break;
+        default: idx = ((kb * da_in + ka) * db_out + rb) * da_out + ra; break;
+      }
+      const double v = ptm_host[idx];
+      M[(size_t)r * kin + k] = v;
+      amax = std::max(amax, std::fabs(v));
+    }
+  const double thr = arith == QSGB_ARITH_F64 ? 0.0 : amax * (arith == QSGB_ARITH_F32 ? 0x1p-30 : 0x1p-52);
+  spec.kin = kin;
+  spec.kout = kout;
+  spec.db_in = db_in;
+  spec.db_out = db_out;
+  spec.pair = pair;
+  spec.f32 = dtype == QSGB_F32;
+  spec.vin = vin;
+  spec.vout = vout;
+  spec.lookahead = lookahead_for(kin, pair);
+  spec.cols.assign(kout, {});
+  for (int r = 0; r < kout; ++r)
+    for (int k = 0; k < kin; ++k)
+      if (std::fabs(M[(size_t)r * kin + k]) > thr) spec.cols[r].push_back(k);
+  if (spec.n_coef() > kMaxJitTerms) return false;
+  plan_modes(spec.cols, kin, arith, dtype == QSGB_F64 ? 8 : 4, spec.mode);
+  // Z == 1 without full vector accesses on both sides: stage through shared
+  // memory, as many warps per block as fit 48 KB of tiles (at most 4)
+  spec.stage_warps = 0;
+  spec.stage_bulk = false;
+  if (z1 && !pair && (vin == 1 || vout == 1) && staged_in_place_ok(spec)) {
+    const int tile = 32 * std::max(kin, kout) * (dtype == QSGB_F64 ? 8 : 4);
+    spec.stage_warps = std::max(1, std::min(4, 49152 / tile));
+    spec.stage_bulk = contiguous && kin == kout;
+    spec.vin = spec.vout = 1;
+  }
+  coef.clear();
+  coef.reserve(spec.n_coef());
+  for (int r = 0; r < kout; ++r)
+    for (int k : spec.cols[r]) {
+      const double v = M[(size_t)r * kin + k];
+      if (spec.mode[r] == kModeDF) {
+        const float h = (float)v;
+        const float l = (float)(v - (double)h);
+        uint64_t bits = ((uint64_t)__builtin_bit_cast(uint32_t, h) << 32) | __builtin_bit_cast(uint32_t, l);
+        coef.push_back(__builtin_bit_cast(double, bits));
+      } else if (spec.mode[r] == kModeF32) {
+        uint64_t bits = __builtin_bit_cast(uint32_t, (float)v);
+        coef.push_back(__builtin_bit_cast(double, bits));
+      } else {
+        coef.push_back(v);
+      }
+    }
+  return true;
+}
+
+std::string source(const Spec& s) { return gen_source(s); }
+
 bool available() { return nvrtc().ok && !std::getenv("QSGB_NO_JIT"); }
+
+// In-process cache key: everything gen_source reads, one byte per field (all
+// values are below 256), so a cached pattern costs no code generation.
+std::string spec_key(const Spec& s) {
+  std::string k;
+  k.reserve(8 + 2 * s.kout + s.n_coef());
+  for (int v : {s.kin, s.kout, s.db_in, s.db_out, (int)s.pair, (int)s.f32, s.vin, s.vout, s.lookahead,
+                s.stage_warps, (int)s.stage_bulk})
+    k.push_back((char)v);
+  for (int r = 0; r < s.kout; ++r) {
+    k.push_back((char)s.mode[r]);
+    k.push_back((char)s.cols[r].size());
+    for (int c : s.cols[r]) k.push_back((char)c);
+  }
+  return k;
+}
 
 int kernel_for(const Spec& s, cudaKernel_t* k, std::string* src_out) {
   if (s.n_coef() > kMaxCoef) return QSGB_ERR_UNSUPPORTED;
-  const std::string src = gen_source(s);
-  if (src_out) *src_out = src;
+  if (src_out) *src_out = gen_source(s);
+  const std::string key = spec_key(s);
   Cache& c = cache();
   {
     std::lock_guard<std::mutex> g(c.mu);
-    auto it = c.kernels.find(src);
+    auto it = c.kernels.find(key);
     if (it != c.kernels.end()) {
       *k = it->second;
       return QSGB_OK;
     }
-    if (c.failed.count(src)) return QSGB_ERR_UNSUPPORTED;
+    if (c.failed.count(key)) return QSGB_ERR_UNSUPPORTED;
   }
   cudaKernel_t kern;
-  const int st = compile(src, &kern);
+  const int st = compile(src_out ? *src_out : gen_source(s), &kern);
   std::lock_guard<std::mutex> g(c.mu);
   if (st != QSGB_OK) {
-    c.failed[src] = st;
+    c.failed[key] = st;
     return QSGB_ERR_UNSUPPORTED;
   }
-  c.kernels[src] = kern;
+  c.kernels[key] = kern;
   *k = kern;
   return QSGB_OK;
 }
@@ -422,7 +856,7 @@ int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t st
   std::memcpy(blob.data(), &h, sizeof h);
   std::memcpy(blob.data() + sizeof h, coef, 8 * (size_t)s.n_coef());
   void* args[] = {blob.data()};
-  const unsigned block = 128;
+  const unsigned block = s.stage_warps ? 32u * (unsigned)s.stage_warps : 128u;
   const uint64_t need = (g.n_items + block - 1) / block;
   const uint64_t cap = (uint64_t)sm_count() * 16;
   const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(need, cap));

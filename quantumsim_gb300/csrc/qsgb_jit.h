@@ -21,6 +21,9 @@ struct Spec {
   bool f32;            // FP32 storage
   int vin, vout;       // 1, or 2 / 4: vector width of loads / stores along
                        // the less significant target (only when Z == 1)
+  int lookahead;        // loads are emitted this many inputs ahead of first use
+  int stage_warps;      // > 0: Z == 1 items staged in shared memory, warps per block
+  bool stage_bulk;      // staged tiles are contiguous spans moved by bulk copies
   std::vector<int> mode;               // per output row
   std::vector<std::vector<int>> cols;  // per output row: input indices of its terms
   int n_coef() const;
@@ -37,6 +40,19 @@ struct Geometry {
 };
 
 bool available();
+// Spec and coefficient list (the layout of `launch`) of a host PTM stored in
+// `layout` (QSGB_PTM_SWAPPED / QSGB_PTM_TRANSPOSED bits); z1: the view has
+// Z == 1; contiguous: consecutive items' groups are adjacent, contiguous
+// spans in both tensors (one qudit, or Y == 1) and both tensors start on a
+// 16-byte boundary; vin / vout are the vector widths along the less
+// significant target (1 unless Z == 1).  Returns false when the specialised
+// path does not apply (more than 81 inputs or outputs, or more than 1024
+// non-zero terms).
+bool make_spec(const double* ptm_host, int da_out, int db_out, int da_in, int db_in, int layout, int dtype,
+               int arith, bool pair, bool z1, bool contiguous, int vin, int vout, Spec& spec,
+               std::vector<double>& coef);
+// CUDA source of the kernel of `s`.
+std::string source(const Spec& s);
 // Compile (or fetch from the cache) the kernel of `s`; optionally return its source.
 int kernel_for(const Spec& s, cudaKernel_t* k, std::string* src_out);
 // coef: one double per term in row order (dp: value; df: hi/lo float words;

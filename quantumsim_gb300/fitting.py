@@ -108,12 +108,17 @@ class NoisyCircuitModel:
         return x
 
     def probabilities(self, p, backend='gb300', dtype=torch.float64,
-                      checkpoint_every=8, device=None):
+                      checkpoint_every=8, device=None, arith=None):
+        """Computational-basis probabilities of the final state.  `arith`
+        (gb300 backend) selects the kernel arithmetic as in
+        ``apply_ptm_diff``; the default picks per PTM row."""
         if backend == 'gb300':
             device = device or torch.device('cuda')
             x = self.initial_state(device, dtype)
+            kw = {} if arith is None else {'arith': arith}
             x = checkpointed(
-                self.layers(p, lambda s, pt, qs: apply_ptm_diff(s, pt, *qs)),
+                self.layers(p, lambda s, pt, qs: apply_ptm_diff(s, pt, *qs,
+                                                                **kw)),
                 x, checkpoint_every)
             return diagonal_diff(x, [self.basis] * self.n)
         device = device or torch.device('cpu')

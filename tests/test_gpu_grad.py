@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 import torch
 
+from quantumsim_gb300 import _lib as L
 from quantumsim_gb300 import autograd as AG
 from quantumsim_gb300 import fitting
 from quantumsim_gb300.fitting import _einsum_apply
@@ -77,7 +78,9 @@ def test_model_gradients_small_match_reference_and_fd():
     assert out['gb300'][0] == pytest.approx(out['einsum'][0], rel=1e-11)
     np.testing.assert_allclose(out['gb300'][1], out['einsum'][1], rtol=1e-8,
                                atol=1e-12)
-    # central finite differences on a few parameters, through the GPU
+    # central finite differences on a few parameters, through the GPU with
+    # native FP64 arithmetic (a loss error e moves the difference quotient
+    # by e / h, so the forward must be as accurate as numpy's)
     h = 1e-6
     base = m.params(requires_grad=False)
     checks = [('angle_offset', (1, 2)), ('t1', (3,)), ('t2', (0,)),
@@ -93,7 +96,8 @@ def test_model_gradients_small_match_reference_and_fd():
             q = {kk: vv.clone() for kk, vv in base.items()}
             q[k][idx] += sgn * h
             with torch.no_grad():
-                vals.append(float(m.loss(q, target, backend='gb300')))
+                vals.append(float(m.loss(q, target, backend='gb300',
+                                         arith=L.ARITH_F64)))
         fd = (vals[0] - vals[1]) / (2 * h)
         flat_i = offs[k] + int(np.ravel_multi_index(idx, base[k].shape))
         ad = float(out['gb300'][1][flat_i])

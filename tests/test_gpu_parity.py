@@ -156,6 +156,51 @@ def test_two_qutrit_81x81_dense_and_cphase():
                          O.apply_ptm(np.abs(pv), np.abs(ptm), *qs))
 
 
+@pytest.mark.parametrize('arith', [0, 2])
+def test_last_qudit_shared_memory_staging(arith):
+    """PTMs on the last qudit with odd dimensions (the specialised kernel
+    stages 32 groups per warp in shared memory): 1 and 2 qutrits, adjacent
+    and distant pairs, rectangular, item counts that leave partial warp
+    tiles (1, 25 of 32), and FP32 storage."""
+    rng = np.random.default_rng(16)
+    dev = torch.device('cuda')
+    cases = [((9,) * 5, (4,), (9, 9)),
+             ((9,) * 5, (4, 3), (9, 9, 9, 9)),
+             ((9,) * 5, (3, 4), (9, 9, 9, 9)),
+             ((9,) * 5, (0, 4), (9, 9, 9, 9)),
+             ((9, 9), (1, 0), (9, 9, 9, 9)),
+             ((9, 4, 9), (2,), (3, 9)),
+             ((4, 9, 3), (2, 1), (1, 9, 3, 9)),
+             ((4, 4, 3), (2,), (3, 3))]
+    for shape, qs, pshape in cases:
+        x = rand_pv(rng, shape)
+        for ptm in (rand_ptm(rng, pshape, 0.3), rand_ptm(rng, pshape)):
+            ref = O.apply_ptm(x, ptm, *qs)
+            absref = O.apply_ptm(np.abs(x), np.abs(ptm), *qs)
+            y = torch.ops.qsgb.apply_ptm(torch.from_numpy(x).to(dev),
+                                         torch.from_numpy(ptm), list(qs),
+                                         arith, ptm.size, False, True)
+            assert_close_dot(y.cpu().numpy(), ref, absref)
+            y32 = torch.ops.qsgb.apply_ptm(
+                torch.from_numpy(x).to(dev).float(), torch.from_numpy(ptm),
+                list(qs), 3, ptm.size, False, True)
+            np.testing.assert_allclose(y32.cpu().numpy(), ref, rtol=1e-4,
+                                       atol=1e-5 * np.abs(absref).max())
+    # the leakage CZ and the qutrit rotation of the qutrit workload; at 7
+    # qutrits each warp takes several tiles (bulk copies, then a ragged
+    # last tile of 17 groups)
+    bases = [B.general(3)] * 7
+    pv = rand_pv(rng, (9,) * 7)
+    s = GB(bases, pv, force=True)
+    ref = pv
+    for ptm, qs in [(workloads.qutrit_2q(rng), (6, 5)),
+                    (workloads.qutrit_1q(rng), (6,)),
+                    (workloads.qutrit_2q(rng), (2, 6))]:
+        s.apply_ptm(ptm, *qs)
+        ref = O.apply_ptm(ref, ptm, *qs)
+    assert_close_f64(s.to_pv(), ref)
+
+
 @pytest.mark.parametrize('arith', [0, 1, 2])
 def test_specialised_and_generic_kernels_agree(arith):
     """The run-time specialised kernel and the generic one give the same
