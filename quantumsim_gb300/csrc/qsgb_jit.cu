@@ -273,23 +273,29 @@ std::string gen_source(const Spec& s) {
                     KS * esz, 32 * KS);
       src += buf;
     }
+    // lane copies elements f = lane + 32 j of each run of db values (one run
+    // per item and ka): item i = f / db, offset kb = f % db, with the item's
+    // base taken from lane i
     std::snprintf(buf, sizeof buf,
                   "    // coalesced global -> shared copies (cp.async: no registers held)\n"
+                  "    qsgb_i64 srcj[%d];\n"
+                  "#pragma unroll\n"
+                  "    for (int j = 0; j < %d; ++j) srcj[j] = __shfl_sync(0xffffffffu, bi, (lane + 32u * j) / %du);\n"
                   "#pragma unroll 3\n"
                   "    for (int ka = 0; ka < %d; ++ka) {\n"
                   "#pragma unroll\n"
                   "      for (int j = 0; j < %d; ++j) {\n"
                   "        const unsigned f = lane + 32u * j, i = f / %du, kb = f - i * %du;\n"
-                  "        const qsgb_i64 src = __shfl_sync(0xffffffffu, bi, i);\n"
                   "        if (i < nv)\n"
                   "          asm volatile(\"cp.async.ca.shared.global [%%0], [%%1], %d;\" :: \"r\"(tb + (i * %du + ka * "
-                  "%du + kb) * %du), \"l\"(in + src + ka * p.h.sai + kb) : \"memory\");\n"
+                  "%du + kb) * %du), \"l\"(in + srcj[j] + ka * p.h.sai + kb) : \"memory\");\n"
                   "      }\n"
                   "    }\n"
                   "    asm volatile(\"cp.async.wait_all;\" ::: \"memory\");\n"
                   "%s"
                   "    __syncwarp();\n",
-                  s.kin / s.db_in, s.db_in, s.db_in, s.db_in, esz, KS, s.db_in, esz, s.stage_bulk ? "    }\n" : "");
+                  s.db_in, s.db_in, s.db_in, s.kin / s.db_in, s.db_in, s.db_in, s.db_in, esz, KS, s.db_in, esz,
+                  s.stage_bulk ? "    }\n" : "");
     src += buf;
   } else {
   std::snprintf(buf, sizeof buf,
@@ -500,20 +506,23 @@ std::string gen_source(const Spec& s) {
       src += buf;
     }
     std::snprintf(buf, sizeof buf,
+                  "    qsgb_i64 dstj[%d];\n"
+                  "#pragma unroll\n"
+                  "    for (int j = 0; j < %d; ++j) dstj[j] = __shfl_sync(0xffffffffu, bo, (lane + 32u * j) / %du);\n"
                   "#pragma unroll 1\n"
                   "    for (int ra = 0; ra < %d; ++ra) {\n"
                   "#pragma unroll\n"
                   "      for (int j = 0; j < %d; ++j) {\n"
                   "        const unsigned f = lane + 32u * j, i = f / %du, rb = f - i * %du;\n"
-                  "        const qsgb_i64 dst = __shfl_sync(0xffffffffu, bo, i);\n"
-                  "        if (i < nv) out[dst + ra * p.h.sao + rb] = t[i * %d + ra * %d + rb];\n"
+                  "        if (i < nv) out[dstj[j] + ra * p.h.sao + rb] = t[i * %d + ra * %d + rb];\n"
                   "      }\n"
                   "    }\n"
                   "%s"
                   "    __syncwarp();\n"
                   "    if (lane < nv) bad_all |= bad;\n"
                   "  }\n",
-                  s.kout / s.db_out, s.db_out, s.db_out, s.db_out, KS, s.db_out, s.stage_bulk ? "    }\n" : "");
+                  s.db_out, s.db_out, s.db_out, s.kout / s.db_out, s.db_out, s.db_out, s.db_out, KS, s.db_out,
+                  s.stage_bulk ? "    }\n" : "");
     src += buf;
     if (s.stage_bulk) src += "  if (lane == 0) asm volatile(\"cp.async.bulk.wait_group 0;\" ::: \"memory\");\n";
     src += "  if (bad_all && p.h.status) atomicOr(p.h.status, 1u);\n}\n";
@@ -756,6 +765,8 @@ bool make_spec(const double* ptm_host, int da_out, int db_out, int da_in, int db
   // memory, as many warps per block as fit 48 KB of tiles (at most 4)
   spec.stage_warps = 0;
   spec.stage_bulk = false;
+  // (measured on GB300: staging instead of 32-byte vector accesses loses 20 %
+  // on a 16x16 PTM on the last two qubits, 5453 -> 4324 GB/s)
   if (z1 && !pair && (vin == 1 || vout == 1) && staged_in_place_ok(spec)) {
     const int tile = 32 * std::max(kin, kout) * (dtype == QSGB_F64 ? 8 : 4);
     spec.stage_warps = std::max(1, std::min(4, 49152 / tile));
