@@ -131,6 +131,23 @@ def _dist():
     return world, rank, local
 
 
+def max_over_ranks(x, device, world):
+    """Maximum of the float x over all ranks (x itself on one rank)."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Units all ranks processed per second of the slowest rank (every
+    replica does the same work: weak scaling)."""
+    return units_per_rank * world / seconds
+
+
 def cpu_baseline_sample(n_apps, seed=123):
     """Time the oracle (numpy einsum restatement of PauliVectorNumpy) on
     `n_apps` noisy-CZ applications of the 14-qubit workload."""
@@ -231,13 +248,9 @@ def run_gb300(args):
     e1.record(stream)
     barrier()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), dev, world)
     apps = args.steps * APPS_PER_STEP
-    value = apps * world / (ms / 1e3)
+    value = whole_job_rate(apps, world, ms / 1e3)
     bytes_per_app = 2 * n_entries * 8
 
     # ---- per-launch durations of the dominant kernel (same stream)
@@ -298,12 +311,8 @@ def run_gb300(args):
         step(e2e_steps[i])
         s.trace()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = apps * world / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dev, world)
+    e2e_value = whole_job_rate(apps, world, e2e_s)
     h2d = APPS_PER_STEP * 16 * 16 * 8
     qops.check_device_status(dev)
 
@@ -313,6 +322,9 @@ def run_gb300(args):
         from quantumsim_gb300 import batch as qbatch
         batched = qbatch.benchmark(n_instances=args.batch_instances,
                                    f64_check='all')
+        # whole step (forward + adjoint of every circuit) against HBM;
+        # instances of up to 10 qubits largely live in L2
+        batched['hbm_frac'] = batched['achieved_gbs'] / peak
 
     extra = {}
     if rank == 0 and world == 1 and not args.no_configs:
@@ -477,7 +489,8 @@ def run_profile_qutrits(args):
     """Small workload for ncu captures of the qutrit kernels: 8 qutrits
     (9^8 float64 entries, 344 MB); one layer of 9x9 PTMs on every qutrit, then
     3x [9x9 on qutrit 4, 81x81 CZ with leakage on (2, 5), the same on
-    (7, 6)].  Launch order: 8 setup applications, then 3 per repetition."""
+    (7, 6), 9x9 on qutrit 7, 81x81 on (0, 7)].  Launch order: 8 setup
+    applications, then 5 per repetition."""
     import numpy as np
     import torch
     from quantumsim_gb300 import build as qbuild
@@ -494,33 +507,42 @@ def run_profile_qutrits(args):
         s.apply_ptm(p1, 4)
         s.apply_ptm(p2, 2, 5)
         s.apply_ptm(p2, 7, 6)
+        s.apply_ptm(p1, 7)
+        s.apply_ptm(p2, 0, 7)
     torch.cuda.synchronize()
     print(json.dumps({'profile_case': 'qutrits', 'trace': s.trace()}))
 
 
 def run_profile_batched(args):
-    """Small workload for ncu captures of the batched kernel: 64 circuits of
-    4..10 qubits, depth 10, FP32; one plain (non-graph) launch after the
-    tile has been fixed, so the capture sees exactly one qsgb batch launch
-    per step; 2 steps."""
+    """Workload for ncu captures of the batched kernel: 16 circuits of 11 and
+    12 qubits (0.9 GB of FP32 state, 2.6 GB with adjoint and checkpoints),
+    depth 3, checkpoints every 2 layers; one plain (non-graph) launch per
+    step with a fixed tile, 2 steps."""
     import torch
     from quantumsim_gb300 import build as qbuild
     qbuild.build()
     from quantumsim_gb300 import batch as BT
     import numpy as np
-    rng = np.random.default_rng(0)
-    specs = [BT.CircuitSpec(int(n), 10, i)
-             for i, n in enumerate(rng.integers(4, 11, 64))]
+    specs = [BT.CircuitSpec(11 + (i % 2), 3, i) for i in range(16)]
     targets = [BT.target_probabilities(sp, 1000 + i)
                for i, sp in enumerate(specs)]
-    sim = BT.BatchedSimulator(specs, targets, checkpoint_every=4, tile=2048)
+    sim = BT.BatchedSimulator(specs, targets, checkpoint_every=2, tile=8192)
     sim.set_ptms([BT.instance_ptms(sp) for sp in specs])
     for _ in range(2):
         sim.step(use_graph=False)
     torch.cuda.synchronize()
     sim.check()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sim.step(use_graph=False)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
     print(json.dumps({'profile_case': 'batched',
-                      'loss0': float(sim.results()[1][0])}))
+                      'loss0': float(sim.results()[1][0]), 'step_ms': ms,
+                      'algorithmic_bytes': sim.algorithmic_bytes(),
+                      'achieved_gbs': sim.algorithmic_bytes() / ms / 1e6}))
 
 
 def main():

@@ -284,6 +284,19 @@ class BatchedSimulator:
         self.max_items = max_items
         self.graph = None
 
+    def algorithmic_bytes(self):
+        """HBM bytes one step must move with FP32 vectors of N entries:
+        APPLY reads and writes the state (8 N), ADJOINT reads x_out and g_out
+        and writes x_in and g_in (16 N), SAVE and RESTORE copy it (8 N each),
+        INIT and ZERO_G write it (4 N each), LOSS reads the 2^n diagonal
+        entries.  PTMs, dP partials and their sums are negligible."""
+        total = 0
+        for i, s in enumerate(self.specs):
+            n_ops = len(s.ops())
+            total += self.sizes[i] * (24 * n_ops + 16 * self.n_ckpt[i] + 8) \
+                + 4 * 2 ** s.n
+        return total
+
     # ------------------------------------------------------------ PTMs
     def set_ptms(self, ptms_per_instance):
         """ptms_per_instance[i][j]: (K, K) float64 PTM of op j of instance i
@@ -518,6 +531,8 @@ def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
         'entries_total': total_entries,
         'storage': 'f32 Pauli vectors; f64 probabilities, losses, dL/dPTM',
         'step_s': step_s, 'grad_steps_per_s': 1.0 / step_s,
+        'algorithmic_bytes_per_step': sim.algorithmic_bytes(),
+        'achieved_gbs': sim.algorithmic_bytes() / step_s / 1e9,
         'plain_step_s_est': plain_s,
         'plain_per_qubits_s': {str(k): v for k, v in plain.items()},
         'speedup_vs_plain': plain_s / step_s,
