@@ -86,8 +86,9 @@ int qsgb_jit_available(void);
  * ptm : FP64 matrix, row-major (d_out, d_in), on the device (or on the host
  *       with QSGB_PTM_HOST); with QSGB_PTM_TRANSPOSED it is stored as
  *       (d_in, d_out) and its transpose is applied
- * max_terms : upper bound on the number of non-zero PTM entries
- *       (d_out*d_in is always safe; smaller values shrink shared memory)
+ * max_terms : upper bound on the number of non-zero entries of a device
+ *       PTM (d_out*d_in or 0 is always safe; smaller values shrink shared
+ *       memory); ignored for a host PTM, whose entries the call counts
  */
 int qsgb_apply_ptm1(const void* in, void* out, const double* ptm,
                     int64_t d_out, int64_t d_in, int64_t dim_y, int64_t dim_z,

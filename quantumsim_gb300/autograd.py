@@ -38,7 +38,7 @@ class ApplyPTM(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, ptm, qudits, arith):
         ptm_host = ptm.detach().to('cpu', torch.float64).contiguous()
-        max_terms = ops.nnz_terms(ptm_host.numpy(), arith)
+        max_terms = 0  # host PTM: counted by the library
         out = torch.ops.qsgb.apply_ptm(x.contiguous(), ptm_host, list(qudits),
                                        arith, max_terms, False)
         ctx.save_for_backward(x)

@@ -658,7 +658,17 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   // 2. generic kernel; a host PTM travels inside its launch parameters
   if (flags & QSGB_PTM_HOST) {
     if (kin * kout > kMaxInline) return QSGB_ERR_UNSUPPORTED;
-    for (int64_t i = 0; i < kin * kout; ++i) p.ptm_inline[i] = ptm[i];
+    // the term capacity is counted here with the device's rule (entries
+    // above 2^-52 max|P|, 2^-30 for FP32, non-zero for native FP64)
+    double amax = 0.0;
+    for (int64_t i = 0; i < kin * kout; ++i) amax = std::max(amax, std::fabs(ptm[i]));
+    const double thr = arith == QSGB_ARITH_F64 ? 0.0 : amax * (arith == QSGB_ARITH_F32 ? 0x1p-30 : 0x1p-52);
+    int n = 0;
+    for (int64_t i = 0; i < kin * kout; ++i) {
+      p.ptm_inline[i] = ptm[i];
+      n += std::fabs(ptm[i]) > thr ? 1 : 0;
+    }
+    p.max_terms = std::max(1, n);
     p.ptm = nullptr;
   }
   if (pair) {

@@ -20,8 +20,48 @@ from . import _lib as L
 
 _STATUS = {}
 
+# Operators are defined on a torch.library.Library with a CUDA kernel each
+# (and a CPU kernel that raises): one dispatch costs ~5 us on the host, where
+# torch.library.custom_op's Python wrapper adds ~16 us -- most of a small
+# state's apply_ptm.
+_LIB = torch.library.Library('qsgb', 'DEF')
+
+
+def _cpu_kernel(name):
+    def refuse(*args, **kwargs):
+        raise RuntimeError('qsgb::{} runs on CUDA tensors only (there is no '
+                           'CPU path)'.format(name))
+    return refuse
+
+
+def _op(schema):
+    """Define torch.ops.qsgb.<name> from `schema` with the decorated function
+    as its CUDA kernel; returns the function unchanged."""
+    name = schema.split('(', 1)[0]
+
+    def deco(fn):
+        _LIB.define(schema)
+        _LIB.impl(name, fn, 'CUDA')
+        _LIB.impl(name, _cpu_kernel(name), 'CPU')
+        return fn
+    return deco
+
+
+def _fake(name):
+    """Shape function of torch.ops.qsgb.<name> for meta / fake tensors."""
+    def deco(fn):
+        torch.library.register_fake('qsgb::' + name, fn, lib=_LIB)
+        return fn
+    return deco
+
+
+_RAW_STREAM = getattr(torch._C, '_cuda_getCurrentRawStream', None)
+
 
 def _stream_handle(t):
+    """The current CUDA stream of t's device (cudaStream_t)."""
+    if _RAW_STREAM is not None:
+        return ctypes.c_void_p(_RAW_STREAM(t.device.index))
     return ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
 
 
@@ -118,14 +158,17 @@ def apply_geometry(shape, qudits, ptm_shape, transpose=False):
 
 
 # --------------------------------------------------------------- apply_ptm
-@torch.library.custom_op('qsgb::apply_ptm', mutates_args=())
+@_op('apply_ptm(Tensor pv, Tensor ptm, int[] qudits, int arith, int max_terms, '
+     'bool transpose, bool jit=True) -> Tensor')
 def apply_ptm(pv: torch.Tensor, ptm: torch.Tensor, qudits: List[int],
               arith: int, max_terms: int, transpose: bool,
               jit: bool = True) -> torch.Tensor:
     """Apply a 1- or 2-qudit PTM (float64) to a Pauli-vector tensor.
 
-    ``ptm`` may live on the device or (up to 16x16) on the host, in which
-    case it is passed inside the kernel launch."""
+    ``ptm`` may live on the device or on the host, in which case the library
+    reads it during the call and passes its values inside the kernel launch.
+    ``max_terms`` bounds the non-zero terms a device PTM keeps (0: all
+    entries; a host PTM's terms are counted by the library)."""
     _require_cuda(pv)
     if ptm.dtype != torch.float64:
         raise TypeError('PTM must be float64')
@@ -168,19 +211,21 @@ def apply_ptm(pv: torch.Tensor, ptm: torch.Tensor, qudits: List[int],
         # (stream-ordered allocator: freeing dev_ptm after the enqueue is
         # safe for work on this stream)
         dev_ptm = ptm.to(pv.device)
+        if max_terms < 1:
+            max_terms = nnz_terms(ptm.numpy(), arith)
         status = call(dev_ptm, flags & ~L.PTM_HOST)
     L.check(status, 'qsgb_apply_ptm')
     return out
 
 
-@apply_ptm.register_fake
+@_fake('apply_ptm')
 def _(pv, ptm, qudits, arith, max_terms, transpose, jit=True):
     new_shape = apply_geometry(pv.shape, qudits, ptm.shape, transpose)[0]
     return pv.new_empty(new_shape)
 
 
 # --------------------------------------------------------------- ptm_grad
-@torch.library.custom_op('qsgb::ptm_grad', mutates_args=())
+@_op('ptm_grad(Tensor x_in, Tensor g_out, int[] qudits) -> Tensor')
 def ptm_grad(x_in: torch.Tensor, g_out: torch.Tensor,
              qudits: List[int]) -> torch.Tensor:
     """dL/dPTM for out = apply_ptm(x_in, PTM, qudits), given dL/dout.
@@ -231,14 +276,14 @@ def ptm_grad(x_in: torch.Tensor, g_out: torch.Tensor,
     return res
 
 
-@ptm_grad.register_fake
+@_fake('ptm_grad')
 def _(x_in, g_out, qudits):
     shape = [g_out.shape[q] for q in qudits] + [x_in.shape[q] for q in qudits]
     return x_in.new_empty(shape, dtype=torch.float64)
 
 
 # --------------------------------------------------------------- gathers
-@torch.library.custom_op('qsgb::gather', mutates_args=())
+@_op('gather(Tensor pv, int[] idx_off, int[] idx, bool out_f64) -> Tensor')
 def gather(pv: torch.Tensor, idx_off: List[int], idx: List[int],
            out_f64: bool) -> torch.Tensor:
     """Multitake: pv[np.ix_(idx_0, ...)] (flattened); -1 selects a zero."""
@@ -258,7 +303,7 @@ def gather(pv: torch.Tensor, idx_off: List[int], idx: List[int],
     return out
 
 
-@gather.register_fake
+@_fake('gather')
 def _(pv, idx_off, idx, out_f64):
     n_out = 1
     for a in range(pv.dim()):
@@ -266,7 +311,7 @@ def _(pv, idx_off, idx, out_f64):
     return pv.new_empty(n_out, dtype=torch.float64 if out_f64 else pv.dtype)
 
 
-@torch.library.custom_op('qsgb::take_axis', mutates_args=())
+@_op('take_axis(Tensor pv, int axis, int[] idx) -> Tensor')
 def take_axis(pv: torch.Tensor, axis: int, idx: List[int]) -> torch.Tensor:
     """pv.index_select(axis, idx) as a bit-exact copy; -1 selects a zero."""
     _require_cuda(pv)
@@ -286,7 +331,7 @@ def take_axis(pv: torch.Tensor, axis: int, idx: List[int]) -> torch.Tensor:
     return out
 
 
-@take_axis.register_fake
+@_fake('take_axis')
 def _(pv, axis, idx):
     shape = list(pv.shape)
     shape[axis] = len(idx)
@@ -294,7 +339,7 @@ def _(pv, axis, idx):
 
 
 # --------------------------------------------------------------- reductions
-@torch.library.custom_op('qsgb::marginals', mutates_args=())
+@_op('marginals(Tensor diag, int[] shape, int axis) -> Tensor')
 def marginals(diag: torch.Tensor, shape: List[int],
               axis: int) -> torch.Tensor:
     """Marginal sums of an FP64 diagonal along `axis` (-1: the trace)."""
@@ -315,12 +360,12 @@ def marginals(diag: torch.Tensor, shape: List[int],
     return out
 
 
-@marginals.register_fake
+@_fake('marginals')
 def _(diag, shape, axis):
     return diag.new_empty(1 if axis < 0 else shape[axis])
 
 
-@torch.library.custom_op('qsgb::partial_trace', mutates_args=())
+@_op('partial_trace(Tensor pv, int[] keep, float[] weights) -> Tensor')
 def partial_trace(pv: torch.Tensor, keep: List[int],
                   weights: List[float]) -> torch.Tensor:
     """Trace out the qudits not flagged in `keep` with per-element weights
@@ -337,12 +382,12 @@ def partial_trace(pv: torch.Tensor, keep: List[int],
     return out
 
 
-@partial_trace.register_fake
+@_fake('partial_trace')
 def _(pv, keep, weights):
     return pv.new_empty([d for d, k in zip(pv.shape, keep) if k])
 
 
-@torch.library.custom_op('qsgb::scale_', mutates_args=('pv',))
+@_op('scale_(Tensor(a!) pv, float alpha) -> ()')
 def scale_(pv: torch.Tensor, alpha: float) -> None:
     """pv *= alpha in place."""
     _require_cuda(pv)
@@ -353,7 +398,7 @@ def scale_(pv: torch.Tensor, alpha: float) -> None:
     L.check(status, 'qsgb_scale')
 
 
-@torch.library.custom_op('qsgb::scale_by_inverse_', mutates_args=('pv',))
+@_op('scale_by_inverse_(Tensor(a!) pv, Tensor denom, float threshold) -> ()')
 def scale_by_inverse_(pv: torch.Tensor, denom: torch.Tensor,
                       threshold: float) -> None:
     """pv *= 1/denom[0] in place when denom[0] > threshold (device scalar)."""

@@ -243,10 +243,10 @@ class PauliVectorGB300(_Base):
                     'PTM acts on a {}-dimensional Pauli space, qubit {} has '
                     'dim_pauli {}'.format(din, q, self._data.shape[q]))
         if ptm_t is None:
-            max_terms = ops.nnz_terms(ptm, self._arith)
+            max_terms = 0  # host PTM: the library counts its terms
             ptm_t = self._device_ptm(ptm)
         else:
-            max_terms = math.prod(shape)
+            max_terms = 0 if not ptm_t.is_cuda else math.prod(shape)
         self._data = torch.ops.qsgb.apply_ptm(
             self._data, ptm_t, list(qubits), self._arith, max_terms, False)
 
