@@ -308,21 +308,33 @@ __device__ void adjoint1_vec(float* __restrict__ x, float* __restrict__ gv, cons
 
 // x = P^-1 x, g = P^T g on groups [beg, end); returns this thread's FP64
 // share of sum_g g_out (x) x_in, accumulated into acc (16 entries: a 4x4
-// sub-block for K = 16, one entry for K = 4).
+// sub-block for K = 16, one entry for K = 4).  Each thread loads its group's
+// x_out and g_out together (2K loads in flight), and the FP32 dP products of
+// a thread's slice are carried over 4 tiles (64 groups) before they are
+// folded into the FP64 sums.
 template <int K>
 __device__ void adjoint_groups(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
                                int64_t end, BatchSmem& sm) {
   double* acc = sm.acc[threadIdx.x];
   const int tid = threadIdx.x;
   const int sub = tid & 15, slice = tid >> 4;
+  constexpr int NS = (K == 16) ? 16 : 1;
+  float s[NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) s[i] = 0.f;
+  int tiles = 0;
   for (int64_t t0 = beg; t0 < end; t0 += blockDim.x) {
     const int64_t gi = t0 + tid;
     if (gi < end) {
       const int64_t b = group_base(geo, gi);
-      {  // x_in = P^-1 x_out
-        float xo[K], xi[K];
+      float xo[K], go[K];
 #pragma unroll
-        for (int k = 0; k < K; ++k) xo[k] = x[b + in_offset<K>(geo, k)];
+      for (int k = 0; k < K; ++k) {
+        xo[k] = x[b + in_offset<K>(geo, k)];
+        go[k] = gv[b + in_offset<K>(geo, k)];
+      }
+      {  // x_in = P^-1 x_out
+        float xi[K];
 #pragma unroll
         for (int r = 0; r < K; ++r) {
           float a = 0.f;
@@ -337,9 +349,7 @@ __device__ void adjoint_groups(float* __restrict__ x, float* __restrict__ gv, co
           *reinterpret_cast<float4*>(&sm.u.t.x[tid][k]) = make_float4(xi[k], xi[k + 1], xi[k + 2], xi[k + 3]);
       }
       {  // g_in = P^T g_out
-        float go[K], gn[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k) go[k] = gv[b + in_offset<K>(geo, k)];
+        float gn[K];
 #pragma unroll
         for (int r = 0; r < K; ++r) {
           float c = 0.f;
@@ -364,9 +374,6 @@ __device__ void adjoint_groups(float* __restrict__ x, float* __restrict__ gv, co
     // this thread: groups slice*16 .. slice*16+15 of the tile
     if (K == 16) {
       const int rb = (sub >> 2) * 4, cb = (sub & 3) * 4;
-      float s[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) s[i] = 0.f;
       for (int gg = slice * 16; gg < slice * 16 + 16; ++gg) {
         const float4 a = *reinterpret_cast<const float4*>(&sm.u.t.g[gg][rb]);
         const float4 c = *reinterpret_cast<const float4*>(&sm.u.t.x[gg][cb]);
@@ -377,16 +384,21 @@ __device__ void adjoint_groups(float* __restrict__ x, float* __restrict__ gv, co
 #pragma unroll
           for (int j = 0; j < 4; ++j) s[i * 4 + j] = fmaf(av[i], cv[j], s[i * 4 + j]);
       }
-#pragma unroll
-      for (int i = 0; i < 16; ++i) acc[i] += (double)s[i];
     } else {
       const int r = sub >> 2, c = sub & 3;
-      float s = 0.f;
-      for (int gg = slice * 16; gg < slice * 16 + 16; ++gg) s = fmaf(sm.u.t.g[gg][r], sm.u.t.x[gg][c], s);
-      acc[0] += (double)s;
+      for (int gg = slice * 16; gg < slice * 16 + 16; ++gg) s[0] = fmaf(sm.u.t.g[gg][r], sm.u.t.x[gg][c], s[0]);
+    }
+    if ((++tiles & 3) == 0) {
+#pragma unroll
+      for (int i = 0; i < NS; ++i) {
+        acc[i] += (double)s[i];
+        s[i] = 0.f;
+      }
     }
     __syncthreads();
   }
+#pragma unroll
+  for (int i = 0; i < NS; ++i) acc[i] += (double)s[i];
 }
 
 // write the block's dP partial (sum over slices) to grad_partial[slot]
