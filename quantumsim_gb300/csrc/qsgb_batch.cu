@@ -142,7 +142,7 @@ __device__ void apply_groups(float* __restrict__ x, const Geo& geo, int64_t beg,
 template <int K>
 __device__ void apply_vec(float* __restrict__ x, const Geo& geo, int64_t beg, int64_t end, const float* P) {
   if (geo.lz >= 2) {
-    constexpr int V = (K == 4) ? 4 : 2;
+    constexpr int V = 4;
     for (int64_t gi = beg + (int64_t)threadIdx.x * V; gi < end; gi += (int64_t)blockDim.x * V) {
       const int64_t b = group_base(geo, gi);
       float v[K][V];
@@ -157,7 +157,7 @@ __device__ void apply_vec(float* __restrict__ x, const Geo& geo, int64_t beg, in
           v[k][0] = t.x; v[k][1] = t.y;
         }
       }
-#pragma unroll 4
+#pragma unroll 2
       for (int r = 0; r < K; ++r) {
         float y[V];
 #pragma unroll
