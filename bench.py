@@ -330,6 +330,7 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_configs:
         extra['qutrit_8q'] = run_qutrit_config()
         extra['grad_10q'] = run_grad_config()
+        extra.update(run_circuit_configs())
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -409,6 +410,85 @@ def run_qutrit_config():
                           ('81x81_q7_q6', workloads.qutrit_2q(rng), (7, 6))):
         res[name + '_gbs'] = _time_app(s, ptm, qs, nbytes)
     return res
+
+
+def run_circuit_configs():
+    """Whole circuits, unit by unit against fused (quantumsim_gb300.circuit):
+    the 14-qubit noisy circuit (50 layers of 14 noisy rotations and 7 noisy
+    CZs on random pairs, 1050 units, then the partial trace keeping 4
+    qubits) and the 6-qubit, 20-layer circuit (eager, fused, fused CUDA-graph
+    replay, and the oracle on the host for scale)."""
+    import numpy as np
+    import torch
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads, circuit as qc
+    out = {}
+    ops, keep = workloads.config1_circuit(seed=1)
+    units = [(p, qs) for _, p, qs in ops]
+    t0 = time.perf_counter()
+    fused = qc.FusedCircuit(units)
+    plan_s = time.perf_counter() - t0
+    unfused = qc.FusedCircuit(units, fuse=False)
+    rng = np.random.default_rng(2)
+    res = {}
+    for name, circ in (('unit_by_unit', unfused), ('fused', fused)):
+        for rep in range(2):  # the first pass compiles the PTM patterns
+            s = qg.PauliVectorGB300([bases.general(2)] * 14, force=True)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            circ(s)
+            pt = s.partial_trace(*keep)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+        res[name] = (dt, pt.to_pv())
+    diff = float(np.abs(res['fused'][1] - res['unit_by_unit'][1]).max())
+    out['circuit_14q'] = {
+        'workload': '14 qubits FP64, 50 layers x (14 noisy rotations + 7 '
+                    'noisy CZ on random pairs), partial trace keeping {}'
+                    .format(list(keep)),
+        'units': fused.n_units, 'fused_passes': fused.n_passes,
+        'plan_s': plan_s,
+        'unit_by_unit_s': res['unit_by_unit'][0], 'fused_s': res['fused'][0],
+        'speedup': res['unit_by_unit'][0] / res['fused'][0],
+        'max_abs_diff_partial_trace': diff}
+    # small state: host cost per unit dominates
+    ops0 = workloads.config0_circuit(seed=0)
+    units0 = [(p, qs) for _, p, qs in ops0]
+    f0 = qc.FusedCircuit(units0)
+    u0 = qc.FusedCircuit(units0, fuse=False)
+    b6 = [bases.general(2)] * 6
+    times = {}
+    for name, circ in (('unit_by_unit', u0), ('fused', f0)):
+        circ(qg.PauliVectorGB300(b6))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(20):
+            circ(qg.PauliVectorGB300(b6))
+        torch.cuda.synchronize()
+        times[name] = (time.perf_counter() - t0) / 20
+    graph = f0.capture(qg.PauliVectorGB300(b6))
+    s = qg.PauliVectorGB300(b6)
+    graph.run(s)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(200):
+        graph.run(s)
+    torch.cuda.synchronize()
+    times['fused_graph'] = (time.perf_counter() - t0) / 200
+    from oracle import pauli_vector_np as O
+    x = O.initial_pv(b6)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        y = x
+        for p, qs in units0:
+            y = O.apply_ptm(y, p, *qs)
+    times['oracle_host'] = (time.perf_counter() - t0) / 5
+    out['circuit_6q'] = {
+        'workload': '6 qubits FP64, 20 layers x (6 noisy rotations + CZ on '
+                    'a line matching)',
+        'units': f0.n_units, 'fused_passes': f0.n_passes,
+        'seconds': times}
+    return out
 
 
 def run_grad_config():

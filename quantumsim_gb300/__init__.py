@@ -12,9 +12,10 @@ from ._lib import load as load_library
 from .pauli_vector import PauliVectorGB300, register
 from .autograd import ApplyPTM, apply_ptm_diff, diagonal_diff, checkpointed
 from .batch import BatchedSimulator
+from .circuit import FusedCircuit, units_of
 
 __all__ = ['PauliVectorGB300', 'register', 'bases', 'ptm', 'load_library',
            'ApplyPTM', 'apply_ptm_diff', 'diagonal_diff', 'checkpointed',
-           'BatchedSimulator']
+           'BatchedSimulator', 'FusedCircuit', 'units_of']
 
 register()

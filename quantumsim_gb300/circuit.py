@@ -1,0 +1,287 @@
+"""Fused circuit execution: a list of PTM units applied with fewer passes
+over the Pauli vector.
+
+The reference runs a circuit one unit at a time: ``_Chain.__call__`` calls
+every unit's ``PTMOperation.__call__``, which converts the PTM to the
+vector's bases and calls ``pauli_vector.apply_ptm``
+(quantumsim/operations/operation.py:529-604).  Each call streams the whole
+vector through memory once.  On a large state every such pass costs the same
+HBM traffic whatever the PTM, so merging units saves passes:
+
+* a one-qudit unit followed by another on the same qudit becomes their
+  product;
+* a one-qudit unit and the next (or previous) two-qudit unit that touches
+  its qudit, with no unit on that qudit in between, become one two-qudit
+  PTM (the one-qudit unit commutes with everything in between);
+* two two-qudit units on the same pair, with nothing on either qudit in
+  between, become their product.
+
+A merge is made only when the time model says the merged PTM is cheaper
+than the two passes: an application costs
+``max(1 / R_MEM, terms_per_row / R_TERMS)`` per byte streamed, with R_MEM
+and R_TERMS measured on GB300 for the specialised FP64 kernels (denser rows
+take more float-float arithmetic per element).  PTM products are formed in
+FP64 on the host; the fused result differs from unit-by-unit application by
+rounding only.
+
+The reference's compiler merges units too when it compiles an operation
+for given bases (quantumsim/operations/compiler.py); ``plan`` does the same
+job for uncompiled unit lists, with a cost model for this hardware.
+
+``units_of(operation, bases, *qubits)`` turns a reference operation (a
+``_Chain`` or a ``PTMOperation``) into the (ptm, qudits) units that its
+``__call__`` would apply to a vector with those bases, converting each PTM
+to the vector's bases on the way exactly as ``PTMOperation.__call__`` does.
+
+``FusedCircuit(units)`` plans once; calling it on a ``PauliVectorGB300``
+applies the fused PTMs.  ``capture(pv)`` records the fused applications of
+one vector into a CUDA graph (a static input and output buffer), so a
+circuit that is run many times on states of one shape costs one graph
+launch instead of one host call per unit.
+"""
+import numpy as np
+import torch
+
+# GB300, specialised FP64 kernels: sparse PTMs stream at ~6.3 TB/s; the
+# arithmetic of denser rows caps the rate near R_TERMS / terms per row
+# (dense 16x16: 16 terms per row, 1.65 TB/s).
+R_MEM = 6.3e12
+R_TERMS = 26.4e12
+
+
+def terms_per_row(m):
+    """Non-zero entries per output row that the kernels keep (entries above
+    2^-52 of the largest)."""
+    a = np.abs(m)
+    amax = a.max() if a.size else 0.0
+    return float((a > amax * 2.0 ** -52).sum()) / max(1, m.shape[0])
+
+
+def pass_cost(m):
+    """Relative time of one application of the square PTM matrix m."""
+    return max(1.0 / R_MEM, terms_per_row(m) / R_TERMS)
+
+
+class _Unit:
+    """A PTM as a square matrix over its qudits (row index (out_0, out_1),
+    column index (in_0, in_1), qudit order as given)."""
+
+    __slots__ = ('qudits', 'dims', 'mat', 'ptm', 'count')
+
+    def __init__(self, ptm, qudits):
+        ptm = np.ascontiguousarray(ptm, dtype=np.float64)
+        n = len(qudits)
+        self.qudits = tuple(int(q) for q in qudits)
+        self.ptm = ptm
+        self.count = 1
+        if n in (1, 2) and ptm.shape[:n] == ptm.shape[n:]:
+            self.dims = tuple(ptm.shape[:n])
+            k = int(np.prod(self.dims))
+            self.mat = ptm.reshape(k, k)
+        else:  # rectangular or 3+ qudits: applied as given, never merged
+            self.dims = None
+            self.mat = None
+
+    @property
+    def square(self):
+        return self.mat is not None
+
+    def set_mat(self, mat):
+        self.mat = mat
+        self.ptm = mat.reshape(self.dims + self.dims)
+
+
+def _embed(unit1, pair, dims):
+    """The one-qudit matrix of unit1 as a matrix over `pair` (order kept)."""
+    a, b = pair
+    if unit1.qudits[0] == a:
+        return np.kron(unit1.mat, np.eye(dims[1]))
+    return np.kron(np.eye(dims[0]), unit1.mat)
+
+
+def _aligned(unit2, pair):
+    """unit2's matrix with its qudits in the order of `pair`."""
+    if unit2.qudits == tuple(pair):
+        return unit2.mat
+    da, db = unit2.dims  # unit2 is on (pair[1], pair[0])
+    m = unit2.mat.reshape(da, db, da, db).transpose(1, 0, 3, 2)
+    return m.reshape(da * db, da * db)
+
+
+def plan(units):
+    """Fuse a list of (ptm, qudits) units; returns the fused list of
+    (ptm, qudits) in application order."""
+    out = []
+    last = {}  # qudit -> index in `out` of the last unit touching it
+
+    def gain(merged, parts):
+        return pass_cost(merged) < sum(pass_cost(p) for p in parts)
+
+    for ptm, qudits in units:
+        u = _Unit(ptm, qudits)
+        if u.square and len(u.qudits) == 1:
+            (q,) = u.qudits
+            j = last.get(q)
+            prev = out[j] if j is not None else None
+            if prev is not None and prev.square and prev.dims is not None:
+                if len(prev.qudits) == 1:
+                    merged = u.mat @ prev.mat
+                    if gain(merged, [u.mat, prev.mat]):
+                        prev.set_mat(merged)
+                        prev.count += 1
+                        continue
+                else:
+                    emb = _embed(u, prev.qudits, prev.dims)
+                    merged = emb @ prev.mat
+                    if gain(merged, [u.mat, prev.mat]):
+                        prev.set_mat(merged)
+                        prev.count += 1
+                        continue
+        elif u.square and len(u.qudits) == 2:
+            a, b = u.qudits
+            ja, jb = last.get(a), last.get(b)
+            # the previous two-qudit unit on the same pair
+            if ja is not None and ja == jb and out[ja] is not None and \
+                    out[ja].square and len(out[ja].qudits) == 2:
+                prev = out[ja]
+                merged = u.mat @ _aligned(prev, u.qudits)
+                if gain(merged, [u.mat, prev.mat]):
+                    u.set_mat(merged)
+                    u.count += prev.count
+                    out[ja] = None
+                    ja = jb = None
+            # pending one-qudit units on a or b move forward into u
+            for q, j in ((a, ja), (b, jb)):
+                if j is None or out[j] is None:
+                    continue
+                prev = out[j]
+                if prev.square and len(prev.qudits) == 1 and \
+                        prev.qudits[0] == q:
+                    merged = u.mat @ _embed(prev, u.qudits, u.dims)
+                    if gain(merged, [u.mat, prev.mat]):
+                        u.set_mat(merged)
+                        u.count += prev.count
+                        out[j] = None
+        out.append(u)
+        for q in u.qudits:
+            last[q] = len(out) - 1
+    return [(v.ptm, v.qudits) for v in out if v is not None]
+
+
+def units_of(operation, bases, *qubits):
+    """(units, bases_after) of a reference quantumsim operation applied to
+    `qubits` (default 0..n-1) of a vector whose bases are `bases`.
+
+    Follows ``_Chain.__call__`` and ``PTMOperation.__call__``
+    (quantumsim/operations/operation.py:529-551, 600-604): per unit, the PTM
+    is converted to the vector's current bases of its qudits when they
+    differ from the unit's input bases, applied, and the qudits take the
+    unit's output bases."""
+    bases = list(bases)
+    if not qubits:
+        qubits = tuple(range(operation.num_qubits))
+    if len(qubits) != operation.num_qubits:
+        raise ValueError('This is a {}-qubit operation, but number of qubits '
+                         'provided is {}'.format(operation.num_qubits,
+                                                 len(qubits)))
+    units = []
+    for op, idx in operation.units():
+        if not hasattr(op, 'set_bases') or not hasattr(op, 'bases_out'):
+            raise TypeError('unit {!r} is not a PTM operation'.format(op))
+        qs = tuple(qubits[i] for i in idx)
+        b_in = tuple(bases[q] for q in qs)
+        if tuple(op.bases_in) != b_in:
+            op = op.set_bases(bases_in=b_in)
+        units.append((np.asarray(op.ptm(op.bases_in, op.bases_out),
+                                 dtype=np.float64), qs))
+        for q, b in zip(qs, op.bases_out):
+            bases[q] = b
+    return units, bases
+
+
+class FusedCircuit:
+    """A circuit (list of (ptm, qudits) units, PTMs in the vector's bases)
+    planned once and applied with fused PTMs.  `bases_out` (optional, a
+    list with one entry per qudit, None to keep) is assigned to the vector's
+    bases after the circuit, as the reference's operations do."""
+
+    def __init__(self, units, fuse=True, bases_out=None):
+        self.units = [(np.ascontiguousarray(p, dtype=np.float64), tuple(q))
+                      for p, q in units]
+        self.fused = plan(self.units) if fuse else list(self.units)
+        self.bases_out = bases_out
+
+    @classmethod
+    def from_operation(cls, operation, bases, *qubits, fuse=True):
+        """Fused circuit of a reference operation for vectors with
+        `bases` (see units_of)."""
+        units, after = units_of(operation, bases, *qubits)
+        return cls(units, fuse=fuse, bases_out=after)
+
+    @property
+    def n_units(self):
+        return len(self.units)
+
+    @property
+    def n_passes(self):
+        return len(self.fused)
+
+    def __call__(self, pv):
+        """Apply the circuit to a PauliVectorGB300 (in place)."""
+        for ptm, qudits in self.fused:
+            pv.apply_ptm(ptm, *qudits)
+        if self.bases_out is not None:
+            for q, b in enumerate(self.bases_out):
+                if b is not None:
+                    pv.bases[q] = b
+        return pv
+
+    def capture(self, pv):
+        """A CUDA-graph replay of this circuit for vectors shaped like pv's
+        data; see CircuitGraph."""
+        return CircuitGraph(self, pv)
+
+
+class CircuitGraph:
+    """The fused applications of one circuit recorded into a CUDA graph.
+
+    ``run(pv)`` copies pv's data into the graph's static input, replays the
+    graph and leaves the result in pv (pv keeps its bases: the circuit must
+    map every qudit's basis onto itself, i.e. square PTMs).  The first
+    (eager) pass compiles every specialised kernel before capture."""
+
+    def __init__(self, circuit, pv):
+        from . import ops
+        self.circuit = circuit
+        for ptm, qudits in circuit.fused:
+            if ptm.shape[:len(qudits)] != ptm.shape[len(qudits):]:
+                raise ValueError('captured circuits must map every qudit '
+                                 'onto its own basis (square PTMs)')
+        self.device = pv._data.device
+        self.static_in = pv._data.clone()
+        warm = pv.copy()
+        circuit(warm)  # compiles the kernels; no capture of compilation
+        torch.cuda.synchronize(self.device)
+        self.graph = torch.cuda.CUDAGraph()
+        stream = torch.cuda.Stream(self.device)
+        stream.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(stream):
+            x = self.static_in
+            with torch.cuda.graph(self.graph, stream=stream):
+                for ptm, qudits in circuit.fused:
+                    x = torch.ops.qsgb.apply_ptm(
+                        x, torch.from_numpy(ptm), list(qudits), pv._arith,
+                        0, False)
+            self.static_out = x
+        torch.cuda.current_stream(self.device).wait_stream(stream)
+        ops.check_device_status(self.device)
+
+    def run(self, pv):
+        if pv._data.shape != self.static_in.shape or \
+                pv._data.dtype != self.static_in.dtype:
+            raise ValueError('vector shape or dtype differs from the '
+                             'captured one')
+        self.static_in.copy_(pv._data)
+        self.graph.replay()
+        pv._data = self.static_out.clone()
+        return pv
