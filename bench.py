@@ -192,7 +192,54 @@ def run_reference(args):
         'e2e': {'value': value, 'unit': 'apps/s', 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': 0},
     }
+    gk = reference_gpu_kernel(args)
+    if gk is not None:
+        line['gpu_kernel'] = gk
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_kernel(args):
+    """The reference's own CUDA kernel (primitives.cu two_qubit_general_ptm,
+    compiled unchanged for sm_103a into oracle/_ref, launched with the
+    geometry of quantumsim/pauli_vectors/cuda.py:151-221) on this arm's
+    workload: the 14-qubit FP64 vector, steps of 7 noisy CZs on random
+    ordered pairs, CUDA events around `steps` steps after `warmup`.  None
+    when there is no GPU or the kernel was not built."""
+    try:
+        import torch
+        from oracle import ref_gpu
+    except Exception:
+        return None
+    if not torch.cuda.is_available() or not ref_gpu.available():
+        return None
+    import numpy as np
+    from quantumsim_gb300 import workloads
+    rng = np.random.default_rng(7)
+    x = torch.from_numpy(rng.standard_normal((4,) * N_QUBITS) * 2.0 ** -14) \
+        .cuda()
+    n_steps = args.warmup + max(1, args.steps)
+    steps = [workloads.config1_2q_batch(1000 + i, N_QUBITS, APPS_PER_STEP)
+             for i in range(n_steps)]
+    for i in range(args.warmup):
+        for _, ptm, qs in steps[i]:
+            x = ref_gpu.apply(x, ptm, qs)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.warmup, n_steps):
+        for _, ptm, qs in steps[i]:
+            x = ref_gpu.apply(x, ptm, qs)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    apps = (n_steps - args.warmup) * APPS_PER_STEP
+    return {'value': apps / sec, 'unit': 'apps/s',
+            'gbs': apps * 2 * 4 ** N_QUBITS * 8 / sec / 1e9,
+            'kernel': 'two_qubit_general_ptm (quantumsim primitives.cu, '
+                      'compiled unchanged for sm_103a, PyCUDA launch '
+                      'geometry); PTMs uploaded on first use and cached by '
+                      'content, as the reference does'}
 
 
 def run_gb300(args):

@@ -8,6 +8,7 @@ import pytest
 
 from conftest import assert_close_f64, golden_bases, golden_cases
 from oracle import pauli_vector_np as O
+from oracle import ref_gpu
 from quantumsim_gb300 import bases as B
 from quantumsim_gb300 import ptm as P
 from quantumsim_gb300 import workloads
@@ -203,3 +204,17 @@ def test_oracle_runs_qutrit_circuit_trace_one():
     traces = workloads.run(pv, ops)
     assert len(traces) == 1 and 0 < traces[0] <= 1
     assert pv.trace() == pytest.approx(1.0, abs=1e-12)
+
+
+def test_reference_geometry_has_no_partial_blocks_for_qubits():
+    """Host-side check of the launch rule: for qubit states every block of
+    the reference's launch lies inside the output (no early-returning
+    threads before its barrier)."""
+    for n in range(2, 15):
+        shape = (4,) * n
+        for qs in [(0,), (n - 1,), (0, n - 1), (n - 1, 0)] + \
+                ([(1, 2)] if n > 2 else []):
+            pshape = (4, 4) if len(qs) == 1 else (4, 4, 4, 4)
+            _, dims, grid, block, _, _ = ref_gpu.geometry(shape, pshape, qs)
+            assert dims[-1] % (block[0] * block[1] * block[2]) == 0
+            assert grid * block[0] * block[1] * block[2] == dims[-1]
