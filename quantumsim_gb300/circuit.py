@@ -18,9 +18,9 @@ HBM traffic whatever the PTM, so merging units saves passes:
 
 A merge is made only when the time model says the merged PTM is cheaper
 than the two passes: an application costs
-``max(1 / R_MEM, terms_per_row / R_TERMS)`` per byte streamed, with R_MEM
-and R_TERMS measured on GB300 for the specialised FP64 kernels (denser rows
-take more float-float arithmetic per element).  PTM products are formed in
+``max(1 / R_MEM, 1 / R_BASE + terms_per_row / R_TERMS)`` per byte streamed,
+fitted to the specialised FP64 kernels on GB300 (denser rows take more
+float-float arithmetic per element).  PTM products are formed in
 FP64 on the host; the fused result differs from unit-by-unit application by
 rounding only.
 
@@ -42,11 +42,14 @@ launch instead of one host call per unit.
 import numpy as np
 import torch
 
-# GB300, specialised FP64 kernels: sparse PTMs stream at ~6.3 TB/s; the
-# arithmetic of denser rows caps the rate near R_TERMS / terms per row
-# (dense 16x16: 16 terms per row, 1.65 TB/s).
-R_MEM = 6.3e12
-R_TERMS = 26.4e12
+# GB300, specialised FP64 kernels, 14 qubits: sparse PTMs stream at
+# ~6.4 TB/s; denser rows take 1/R_BASE + t/R_TERMS seconds per byte for t
+# terms per row.  Fitted to measured two-qubit PTMs (GB/s): CZ between two
+# rotations, 4.38 terms/row 5245, 6.12 terms/row 3984, 11.25 terms/row
+# 2458, 12.25 terms/row 2107; dense 16x16 1650.
+R_MEM = 6.4e12
+R_BASE = 25.0e12
+R_TERMS = 28.8e12
 
 
 def terms_per_row(m):
@@ -59,7 +62,7 @@ def terms_per_row(m):
 
 def pass_cost(m):
     """Relative time of one application of the square PTM matrix m."""
-    return max(1.0 / R_MEM, terms_per_row(m) / R_TERMS)
+    return max(1.0 / R_MEM, 1.0 / R_BASE + terms_per_row(m) / R_TERMS)
 
 
 class _Unit:

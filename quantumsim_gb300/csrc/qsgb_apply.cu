@@ -588,13 +588,30 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
   if (!jit::make_spec(ptm_host, (int)da_out, (int)db_out, (int)da_in, (int)db_in, flags & 3, dtype, arith, pair,
                       Z == 1, contiguous, vwidth(db_in, p.in), vwidth(db_out, p.out), spec, coef))
     return QSGB_ERR_UNSUPPORTED;
+  uint64_t n_items = p.n_items;
+  FastDiv div_z = p.div_z;
+  // Two groups per thread (16-byte accesses) pay off for one-qudit PTMs and
+  // for two-qudit PTMs of up to 2.5 terms per row; denser two-qudit rows
+  // run faster one group per thread.  Measured on GB300 (14 qubits, GB/s,
+  // pair / single): noisy CZ 6335 / 6427; CZ after one rotation 2.19
+  // terms/row 6274 / 5487, 3.12 terms/row 3810 / 5218; CZ between rotations
+  // 4.38 terms/row 4534 / 5245, 6.12 terms/row 2629 / 3984; two rotations
+  // on one qubit 5968 / 5042.
+  if (pair && spec.kin > 4 && spec.n_coef() > 2.5 * spec.kout) {
+    pair = false;
+    n_items *= 2;
+    div_z = make_fastdiv((uint64_t)Z);
+    if (!jit::make_spec(ptm_host, (int)da_out, (int)db_out, (int)da_in, (int)db_in, flags & 3, dtype, arith, false,
+                        Z == 1, contiguous, vwidth(db_in, p.in), vwidth(db_out, p.out), spec, coef))
+      return QSGB_ERR_UNSUPPORTED;
+  }
   const int NL = pair ? 2 : 1;
   jit::Geometry g;
   g.in = p.in;
   g.out = p.out;
   g.status = p.status;
-  g.n_items = p.n_items;
-  g.div_z = p.div_z;
+  g.n_items = n_items;
+  g.div_z = div_z;
   g.div_y = p.div_y;
   g.sxi = p.sxi / NL;
   g.syi = p.syi / NL;
