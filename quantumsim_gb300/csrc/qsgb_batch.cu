@@ -27,19 +27,19 @@ namespace qsgb {
 namespace {
 
 constexpr int kBatchBlock = 256;
-constexpr int kSlices = kBatchBlock / 16;  // group slices in the dP reduction
+constexpr int kRedRows = kBatchBlock / 16;  // rows of the FP64 dP reduction buffer (>= warps)
 
 struct BatchSmem {
   float P[256];
   float Pi[256];
-  // adjoint tile: g_out and x_in per group, [group][16]; reused for the FP64
-  // cross-slice reduction of the dP partials
+  // adjoint tile: g_out and x_in per group, [group][16], one 32-group slice
+  // per warp; reused for the FP64 cross-warp sums of the dP partials
   union {
     struct {
       float g[kBatchBlock][16];
       float x[kBatchBlock][16];
     } t;
-    double red[kSlices][256];
+    double red[kRedRows][256];
   } u __attribute__((aligned(16)));
   double acc[kBatchBlock][16];  // per-thread FP64 dP partials (ADJOINT)
   int item;
@@ -306,25 +306,34 @@ __device__ void adjoint1_vec(float* __restrict__ x, float* __restrict__ gv, cons
   __syncthreads();
 }
 
-// x = P^-1 x, g = P^T g on groups [beg, end); returns this thread's FP64
-// share of sum_g g_out (x) x_in, accumulated into acc (16 entries: a 4x4
-// sub-block for K = 16, one entry for K = 4).  Each thread loads its group's
-// x_out and g_out together (2K loads in flight), and the FP32 dP products of
-// a thread's slice are carried over 4 tiles (64 groups) before they are
-// folded into the FP64 sums.
-template <int K>
-__device__ void adjoint_groups(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
-                               int64_t end, BatchSmem& sm) {
-  double* acc = sm.acc[threadIdx.x];
-  const int tid = threadIdx.x;
-  const int sub = tid & 15, slice = tid >> 4;
-  constexpr int NS = (K == 16) ? 16 : 1;
-  float s[NS];
+// Two-qubit ADJOINT with independent warps: each warp takes tiles of 32
+// consecutive groups (lane = group), computes x_in = P^-1 x_out and
+// g_in = P^T g_out, stages x_in and g_out of its tile in its own slice of
+// the shared tile, and after a __syncwarp each lane accumulates a 2 x 4
+// block of dP over the tile's 32 groups.  No block barrier inside the loop.
+// FP32 products are carried over 4 tiles, then folded into the thread's FP64
+// sums in shared memory;
+// at the end the warps' blocks are summed in a fixed order and written to
+// dst (256 doubles).
+__device__ void adjoint2_warp(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
+                              int64_t end, BatchSmem& sm, double* __restrict__ dst) {
+  constexpr int K = 16;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  // this warp's slice of the tile: x_in and g_out of 32 groups, [group][16]
+  float(*wx)[16] = &sm.u.t.x[warp * 32];
+  float(*wg)[16] = &sm.u.t.g[warp * 32];
+  const int r0 = 2 * (lane >> 2), c0 = 4 * (lane & 3);
+  float s[8];
+  double* acc = sm.acc[threadIdx.x];  // FP64 running sums in shared memory
 #pragma unroll
-  for (int i = 0; i < NS; ++i) s[i] = 0.f;
+  for (int i = 0; i < 8; ++i) {
+    s[i] = 0.f;
+    acc[i] = 0.0;
+  }
   int tiles = 0;
-  for (int64_t t0 = beg; t0 < end; t0 += blockDim.x) {
-    const int64_t gi = t0 + tid;
+  for (int64_t t0 = beg + (int64_t)warp * 32; t0 < end; t0 += (int64_t)nwarps * 32) {
+    const int64_t gi = t0 + lane;
     if (gi < end) {
       const int64_t b = group_base(geo, gi);
       float xo[K], go[K];
@@ -333,94 +342,63 @@ __device__ void adjoint_groups(float* __restrict__ x, float* __restrict__ gv, co
         xo[k] = x[b + in_offset<K>(geo, k)];
         go[k] = gv[b + in_offset<K>(geo, k)];
       }
-      {  // x_in = P^-1 x_out
-        float xi[K];
 #pragma unroll
-        for (int r = 0; r < K; ++r) {
-          float a = 0.f;
+      for (int r = 0; r < K; ++r) {
+        float a = 0.f, c = 0.f;
 #pragma unroll
-          for (int k = 0; k < K; ++k) a = fmaf(sm.Pi[r * K + k], xo[k], a);
-          xi[r] = a;
+        for (int k = 0; k < K; ++k) {
+          a = fmaf(sm.Pi[r * K + k], xo[k], a);
+          c = fmaf(sm.P[k * K + r], go[k], c);
         }
-#pragma unroll
-        for (int r = 0; r < K; ++r) x[b + in_offset<K>(geo, r)] = xi[r];
-#pragma unroll
-        for (int k = 0; k < K; k += 4)
-          *reinterpret_cast<float4*>(&sm.u.t.x[tid][k]) = make_float4(xi[k], xi[k + 1], xi[k + 2], xi[k + 3]);
+        x[b + in_offset<K>(geo, r)] = a;
+        gv[b + in_offset<K>(geo, r)] = c;
+        wx[lane][r] = a;
       }
-      {  // g_in = P^T g_out
-        float gn[K];
 #pragma unroll
-        for (int r = 0; r < K; ++r) {
-          float c = 0.f;
-#pragma unroll
-          for (int k = 0; k < K; ++k) c = fmaf(sm.P[k * K + r], go[k], c);
-          gn[r] = c;
-        }
-#pragma unroll
-        for (int r = 0; r < K; ++r) gv[b + in_offset<K>(geo, r)] = gn[r];
-#pragma unroll
-        for (int k = 0; k < K; k += 4)
-          *reinterpret_cast<float4*>(&sm.u.t.g[tid][k]) = make_float4(go[k], go[k + 1], go[k + 2], go[k + 3]);
-      }
+      for (int k = 0; k < K; k += 4)
+        *reinterpret_cast<float4*>(&wg[lane][k]) = make_float4(go[k], go[k + 1], go[k + 2], go[k + 3]);
     } else {
 #pragma unroll
       for (int k = 0; k < K; k += 4) {
-        *reinterpret_cast<float4*>(&sm.u.t.x[tid][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
-        *reinterpret_cast<float4*>(&sm.u.t.g[tid][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4*>(&wx[lane][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4*>(&wg[lane][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
-    __syncthreads();
-    // this thread: groups slice*16 .. slice*16+15 of the tile
-    if (K == 16) {
-      const int rb = (sub >> 2) * 4, cb = (sub & 3) * 4;
-      for (int gg = slice * 16; gg < slice * 16 + 16; ++gg) {
-        const float4 a = *reinterpret_cast<const float4*>(&sm.u.t.g[gg][rb]);
-        const float4 c = *reinterpret_cast<const float4*>(&sm.u.t.x[gg][cb]);
-        const float av[4] = {a.x, a.y, a.z, a.w};
-        const float cv[4] = {c.x, c.y, c.z, c.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) s[i * 4 + j] = fmaf(av[i], cv[j], s[i * 4 + j]);
-      }
-    } else {
-      const int r = sub >> 2, c = sub & 3;
-      for (int gg = slice * 16; gg < slice * 16 + 16; ++gg) s[0] = fmaf(sm.u.t.g[gg][r], sm.u.t.x[gg][c], s[0]);
+    __syncwarp();
+#pragma unroll 4
+    for (int g = 0; g < 32; ++g) {
+      const float2 a = *reinterpret_cast<const float2*>(&wg[g][r0]);
+      const float4 c = *reinterpret_cast<const float4*>(&wx[g][c0]);
+      s[0] = fmaf(a.x, c.x, s[0]);
+      s[1] = fmaf(a.x, c.y, s[1]);
+      s[2] = fmaf(a.x, c.z, s[2]);
+      s[3] = fmaf(a.x, c.w, s[3]);
+      s[4] = fmaf(a.y, c.x, s[4]);
+      s[5] = fmaf(a.y, c.y, s[5]);
+      s[6] = fmaf(a.y, c.z, s[6]);
+      s[7] = fmaf(a.y, c.w, s[7]);
     }
+    __syncwarp();
     if ((++tiles & 3) == 0) {
 #pragma unroll
-      for (int i = 0; i < NS; ++i) {
+      for (int i = 0; i < 8; ++i) {
         acc[i] += (double)s[i];
         s[i] = 0.f;
       }
     }
-    __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < NS; ++i) acc[i] += (double)s[i];
-}
-
-// write the block's dP partial (sum over slices) to grad_partial[slot]
-template <int K>
-__device__ void store_partial(double* __restrict__ dst, BatchSmem& sm) {
-  const int tid = threadIdx.x;
-  const double* acc = sm.acc[tid];
-  const int sub = tid & 15, slice = tid >> 4;
-  if (K == 16) {
-    const int rb = (sub >> 2) * 4, cb = (sub & 3) * 4;
+  for (int i = 0; i < 8; ++i) acc[i] += (double)s[i];
+  __syncthreads();  // every warp is done with the tile: reuse it for the sums
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 2; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) sm.u.red[slice][(rb + i) * 16 + cb + j] = acc[i * 4 + j];
-  } else {
-    sm.u.red[slice][sub] = acc[0];
-  }
+    for (int j = 0; j < 4; ++j) sm.u.red[warp][(r0 + i) * 16 + c0 + j] = acc[i * 4 + j];
   __syncthreads();
-  for (int e = tid; e < K * K; e += blockDim.x) {
-    double s = 0.0;
-    for (int sl = 0; sl < kSlices; ++sl) s += sm.u.red[sl][e];
-    dst[e] = s;
+  for (int e = threadIdx.x; e < K * K; e += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < nwarps; ++w) t += sm.u.red[w][e];
+    dst[e] = t;
   }
   __syncthreads();
 }
@@ -492,11 +470,7 @@ __device__ void process(const qsgb_batch_program& p, const qsgb_batch_item& it, 
       } else if (geo.k == 4) {
         adjoint1_vec(in.x, in.g, geo, it.beg, it.end, sm.P, sm.Pi, sm, p.grad_partial + (int64_t)it.slot * 256);
       } else {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) sm.acc[threadIdx.x][i] = 0.0;
-        double* dst = p.grad_partial + (int64_t)it.slot * 256;
-        adjoint_groups<16>(in.x, in.g, geo, it.beg, it.end, sm);
-        store_partial<16>(dst, sm);
+        adjoint2_warp(in.x, in.g, geo, it.beg, it.end, sm, p.grad_partial + (int64_t)it.slot * 256);
       }
       __syncthreads();
       break;
