@@ -541,7 +541,8 @@ def run_circuit_configs():
 def run_grad_config():
     """10 qubits, 40 layers, 249 physical parameters: one gradient step
     (forward, KL loss, adjoint with checkpoints every 8 layers) in FP64 and
-    with FP32 storage."""
+    with FP32 storage, unit by unit and with each CZ absorbing its qubits'
+    rotations."""
     import torch
     from quantumsim_gb300 import fitting
     m = fitting.NoisyCircuitModel()
@@ -549,16 +550,18 @@ def run_grad_config():
     out = {'params': m.n_params, 'qubits': m.n, 'layers': m.n_layers,
            'checkpoint_every': 8}
     for name, dtype in (('f64', torch.float64), ('f32', torch.float32)):
-        ts = []
-        for rep in range(3):
-            p = m.params()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            loss = m.loss(p, target, dtype=dtype, checkpoint_every=8)
-            loss.backward()
-            torch.cuda.synchronize()
-            ts.append(time.perf_counter() - t0)
-        out[name + '_step_s'] = min(ts[1:])
+        for fuse in (False, True):
+            ts = []
+            for rep in range(3):
+                p = m.params()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                loss = m.loss(p, target, dtype=dtype, checkpoint_every=8,
+                              fuse=fuse)
+                loss.backward()
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            out[name + ('_fused' if fuse else '') + '_step_s'] = min(ts[1:])
     return out
 
 

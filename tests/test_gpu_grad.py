@@ -126,3 +126,22 @@ def test_model_full_size_249_parameters():
     np.testing.assert_allclose(g64, gref, rtol=1e-8, atol=1e-12)
     scale = gref.abs().max()
     assert float((g32 - gref).abs().max() / scale) < 1e-4
+
+
+def test_model_fused_layers_full_size():
+    """The 249-parameter model with each CZ absorbing its qubits' rotations
+    (6 applications per layer instead of 15): GPU adjoint gradients against
+    the unfused float64 torch.einsum reference."""
+    m = fitting.NoisyCircuitModel()
+    target = m.probabilities(m.perturbed(), backend='gb300').detach()
+    names = list(m.init)
+    res = {}
+    for backend, fuse in (('gb300', True), ('einsum', False)):
+        p = m.params()
+        loss = m.loss(p, target, backend=backend, fuse=fuse,
+                      checkpoint_every=8)
+        loss.backward()
+        res[backend] = (loss.item(), _flat([p[k].grad for k in names]))
+    assert res['gb300'][0] == pytest.approx(res['einsum'][0], rel=1e-10)
+    np.testing.assert_allclose(res['gb300'][1], res['einsum'][1], rtol=1e-8,
+                               atol=1e-12)

@@ -218,3 +218,23 @@ def test_reference_geometry_has_no_partial_blocks_for_qubits():
             _, dims, grid, block, _, _ = ref_gpu.geometry(shape, pshape, qs)
             assert dims[-1] % (block[0] * block[1] * block[2]) == 0
             assert grid * block[0] * block[1] * block[2] == dims[-1]
+
+
+def test_fused_model_layers_equal_unfused_on_host():
+    """The differentiable model with each CZ absorbing its qubits' rotations
+    gives the same probabilities and parameter gradients as unit by unit
+    (float64 torch.einsum backend on the host)."""
+    import torch
+    from quantumsim_gb300 import fitting
+    m = fitting.NoisyCircuitModel(n_qubits=5, n_layers=6, n_groups=3, seed=4)
+    target = m.probabilities(m.perturbed(), backend='einsum').detach()
+    res = {}
+    for fuse in (False, True):
+        p = m.params()
+        loss = m.loss(p, target, backend='einsum', fuse=fuse)
+        loss.backward()
+        res[fuse] = (float(loss.detach()), torch.cat([p[k].grad.reshape(-1)
+                                             for k in m.init]))
+    assert res[True][0] == pytest.approx(res[False][0], rel=1e-12)
+    np.testing.assert_allclose(res[True][1], res[False][1], rtol=1e-9,
+                               atol=1e-14)
