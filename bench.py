@@ -444,6 +444,7 @@ def run_qutrit_config():
         tr = s.trace()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+    x_unfused = s.to_pv()
     rng = np.random.default_rng(5)
     s = qg.PauliVectorGB300([bases.general(3)] * 8, force=True)
     nbytes = 2 * 9 ** 8 * 8
@@ -452,6 +453,37 @@ def run_qutrit_config():
            'circuit_s': dt, 'ptm_apps': n_ptm, 'apps_per_s': n_ptm / dt,
            'renorm_trace': traces[0] if traces else None,
            'final_trace': tr}
+    # the same circuit with the PTM runs between the basis reductions fused
+    from quantumsim_gb300 import circuit as qc
+    segments, seg = [], []
+    for op in ops:
+        if op[0] == 'ptm':
+            seg.append((op[1], op[2]))
+        else:
+            if seg:
+                segments.append(qc.FusedCircuit(seg))
+                seg = []
+            segments.append(op)
+    if seg:
+        segments.append(qc.FusedCircuit(seg))
+    for rep in range(2):
+        s = qg.PauliVectorGB300([bases.general(3)] * 8, force=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for item in segments:
+            if isinstance(item, qc.FusedCircuit):
+                item(s)
+            else:
+                workloads.run(s, [item])
+        tr_f = s.trace()
+        torch.cuda.synchronize()
+        dt_f = time.perf_counter() - t0
+    res['fused_circuit_s'] = dt_f
+    res['fused_passes'] = sum(c.n_passes for c in segments
+                              if isinstance(c, qc.FusedCircuit))
+    res['fused_final_trace'] = tr_f
+    res['fused_max_abs_diff'] = float(np.abs(s.to_pv() - x_unfused).max())
+    s = qg.PauliVectorGB300([bases.general(3)] * 8, force=True)
     for name, ptm, qs in (('9x9_q4', workloads.qutrit_1q(rng), (4,)),
                           ('81x81_q2_q5', workloads.qutrit_2q(rng), (2, 5)),
                           ('81x81_q7_q6', workloads.qutrit_2q(rng), (7, 6))):

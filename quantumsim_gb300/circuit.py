@@ -17,10 +17,10 @@ HBM traffic whatever the PTM, so merging units saves passes:
   between, become their product.
 
 A merge is made only when the time model says the merged PTM is cheaper
-than the two passes: an application costs
-``max(1 / R_MEM, 1 / R_BASE + terms_per_row / R_TERMS)`` per byte streamed,
-fitted to the specialised FP64 kernels on GB300 (denser rows take more
-float-float arithmetic per element).  PTM products are formed in
+than the two passes: an application's time per byte streamed is
+interpolated from rates measured on GB300 for the specialised FP64 kernels,
+by PTM size and non-zero terms per row (denser rows take more float-float
+arithmetic per element, and the 81x81 kernels degrade fastest).  PTM products are formed in
 FP64 on the host; the fused result differs from unit-by-unit application by
 rounding only.
 
@@ -42,14 +42,26 @@ launch instead of one host call per unit.
 import numpy as np
 import torch
 
-# GB300, specialised FP64 kernels, 14 qubits: sparse PTMs stream at
-# ~6.4 TB/s; denser rows take 1/R_BASE + t/R_TERMS seconds per byte for t
-# terms per row.  Fitted to measured two-qubit PTMs (GB/s): CZ between two
-# rotations, 4.38 terms/row 5245, 6.12 terms/row 3984, 11.25 terms/row
-# 2458, 12.25 terms/row 2107; dense 16x16 1650.
-R_MEM = 6.4e12
-R_BASE = 25.0e12
-R_TERMS = 28.8e12
+# Measured application rates of the specialised FP64 kernels on GB300
+# (TB/s of the vector streamed in and out) against non-zero terms per PTM
+# row, per PTM size K (product of the qudits' Pauli dims); 14 qubits or 8
+# qutrits:
+#   K = 4:  noisy rotation 2.5 terms/row 5.8; two rotations 3.75 5.0
+#   K = 9:  qutrit rotation 2.56 5.5; two rotations 2.78 5.2
+#   K = 16: noisy CZ 1.56 6.4; CZ after a rotation 2.19 6.3; CZ between
+#           rotations 4.38 5.2, 6.12 4.0, 11.25 2.46; dense 16 1.65
+#   K = 81: leakage CZ 2.14 4.7; after one rotation 5.16 2.5; between
+#           rotations 12.26 0.80 -- the 81x81 kernels lose registers and
+#           instruction cache quickly, so merging into them rarely pays.
+# Between points 1/rate is interpolated linearly in the terms per row;
+# beyond the last point it continues along the last segment.
+_RATES = {
+    4: [(1.0, 7.0), (2.5, 5.8), (3.75, 5.0)],
+    9: [(1.0, 6.5), (2.56, 5.5), (2.78, 5.2)],
+    16: [(1.56, 6.4), (2.19, 6.3), (4.38, 5.2), (6.12, 4.0), (11.25, 2.46),
+         (16.0, 1.65)],
+    81: [(1.0, 5.0), (2.14, 4.7), (5.16, 2.5), (12.26, 0.80)],
+}
 
 
 def terms_per_row(m):
@@ -60,9 +72,28 @@ def terms_per_row(m):
     return float((a > amax * 2.0 ** -52).sum()) / max(1, m.shape[0])
 
 
+# PTMs with more non-zero terms than this are not specialised at run time
+# (the library's limit) and run on the slower generic kernel: never merge
+# into one.
+MAX_SPECIALISED_TERMS = 1024
+
+
 def pass_cost(m):
-    """Relative time of one application of the square PTM matrix m."""
-    return max(1.0 / R_MEM, 1.0 / R_BASE + terms_per_row(m) / R_TERMS)
+    """Relative time (seconds per TB streamed) of one application of the
+    square PTM matrix m."""
+    k = m.shape[0]
+    t = terms_per_row(m)
+    if t * k > MAX_SPECIALISED_TERMS:
+        return float('inf')
+    pts = _RATES[min(_RATES, key=lambda kk: abs(kk - k))]
+    inv = [(tt, 1.0 / r) for tt, r in pts]
+    if t <= inv[0][0]:
+        return inv[0][1]
+    for (t0, c0), (t1, c1) in zip(inv, inv[1:]):
+        if t <= t1:
+            return c0 + (c1 - c0) * (t - t0) / (t1 - t0)
+    (t0, c0), (t1, c1) = inv[-2], inv[-1]
+    return c1 + (c1 - c0) * (t - t1) / (t1 - t0)
 
 
 class _Unit:
@@ -118,7 +149,8 @@ def plan(units):
     last = {}  # qudit -> index in `out` of the last unit touching it
 
     def gain(merged, parts):
-        return pass_cost(merged) < sum(pass_cost(p) for p in parts)
+        c = pass_cost(merged)
+        return c != float('inf') and c < sum(pass_cost(p) for p in parts)
 
     for ptm, qudits in units:
         u = _Unit(ptm, qudits)
