@@ -675,6 +675,30 @@ def run_profile_qutrits(args):
     print(json.dumps({'profile_case': 'qutrits', 'trace': s.trace()}))
 
 
+def run_profile_circuit(args):
+    """The fused 14-qubit noisy circuit (1050 units, 337 passes) applied
+    once to the |0..0> state, then the partial trace; for an ncu launch
+    list (gpu__time_duration only: one pass per launch).  Prints the terms
+    per row of every fused pass, in launch order."""
+    import numpy as np
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads, circuit as qc
+    ops, keep = workloads.config1_circuit(seed=1)
+    circ = qc.FusedCircuit([(p, qs) for _, p, qs in ops])
+    s = qg.PauliVectorGB300([bases.general(2)] * 14, force=True)
+    circ(s)
+    s.partial_trace(*keep)
+    torch.cuda.synchronize()
+    terms = [round(qc.terms_per_row(p.reshape(int(np.sqrt(p.size)), -1)), 2)
+             for p, _ in circ.fused]
+    print(json.dumps({'profile_case': 'circuit', 'passes': len(terms),
+                      'terms_per_row': terms,
+                      'qudits': [list(q) for _, q in circ.fused]}))
+
+
 def run_profile_batched(args):
     """Workload for ncu captures of the batched kernel: 16 circuits of 11 and
     12 qubits (0.9 GB of FP32 state, 2.6 GB with adjoint and checkpoints),
@@ -724,13 +748,14 @@ def main():
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', nargs='?', const='apply',
-                    choices=['apply', 'qutrits', 'batched'],
+                    choices=['apply', 'qutrits', 'batched', 'circuit'],
                     help='run a small ncu profiling workload and exit')
     ap.add_argument('--profile-qubits', type=int, default=12)
     args = ap.parse_args()
     if args.profile_case:
         {'apply': run_profile_case, 'qutrits': run_profile_qutrits,
-         'batched': run_profile_batched}[args.profile_case](args)
+         'batched': run_profile_batched,
+         'circuit': run_profile_circuit}[args.profile_case](args)
         return
     if args.warmup < 3 and args.impl == 'gb300':
         print('warning: fewer than 3 warm-up steps', file=sys.stderr)
