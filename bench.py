@@ -344,6 +344,17 @@ def run_gb300(args):
             per_target['arith_{}_2q_dense_3_7'.format(arith)] = _time_app(
                 s, dense, (3, 7), bytes_per_app)
         s._arith_key, s._arith = 'auto', qops_arith('auto')
+        # FP32 storage (FP32 arithmetic): half the bytes per application
+        s32 = qg.PauliVectorGB300([bases.general(2)] * N_QUBITS, force=True,
+                                  dtype=np.float32, device=dev)
+        s32._data.copy_(s._data.float())
+        b32 = bytes_per_app // 2
+        per_target['f32_2q_cz_3_7'] = _time_app(s32, cz, (3, 7), b32)
+        per_target['f32_2q_cz_12_13'] = _time_app(s32, cz, (12, 13), b32)
+        per_target['f32_1q_q5'] = _time_app(s32, r1, (5,), b32)
+        per_target['f32_1q_q13'] = _time_app(s32, r1, (13,), b32)
+        per_target['f32_2q_dense_3_7'] = _time_app(s32, dense, (3, 7), b32)
+        del s32
 
     # ---- end to end through the public API (host PTMs, trace read back)
     e2e_steps = [workloads.config1_2q_batch(50000 + 1000 * rank + i,
