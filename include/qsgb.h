@@ -29,7 +29,7 @@ extern "C" {
 #define QSGB_OK 0
 #define QSGB_ERR_INVALID 1     /* bad argument (shape, pointer, flag) */
 #define QSGB_ERR_CUDA 2        /* a CUDA runtime call failed */
-#define QSGB_ERR_UNSUPPORTED 3 /* valid request this build does not serve */
+#define QSGB_ERR_UNSUPPORTED 3 /* valid request the library does not serve */
 #define QSGB_ERR_SCRATCH 4     /* caller scratch buffer too small */
 
 /* ---- device status bits (written into *dev_status) ---- */
