@@ -142,6 +142,8 @@ class BatchedSimulator:
         self.n_inst = len(specs)
         dev = self.device
         # ---- per-instance buffers
+        if any(not 1 <= s.n <= 15 for s in specs):
+            raise ValueError('batched instances have 1 to 15 qubits')
         self.sizes = [4 ** s.n for s in specs]
         self.n_ckpt = [max(0, (s.depth - 1) // checkpoint_every)
                        for s in specs]

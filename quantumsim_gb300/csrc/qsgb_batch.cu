@@ -110,37 +110,23 @@ __device__ __forceinline__ int64_t group_base(const Geo& g, int64_t gi) {
   return (x << (g.lz + g.ly + 4)) + (y << (g.lz + 2)) + z;
 }
 
+// (32-bit: instances have at most 15 qubits, so an offset inside a group
+// stays below 3 * 4^14; fewer registers than 64-bit addresses per input)
 template <int K>
-__device__ __forceinline__ int64_t in_offset(const Geo& g, int k) {
-  if (K == 4) return (int64_t)k << g.lz;
-  return ((int64_t)(k >> 2) << (g.lz + g.ly + 2)) + ((int64_t)(k & 3) << g.lz);
+__device__ __forceinline__ int in_offset(const Geo& g, int k) {
+  if (K == 4) return k << g.lz;
+  return ((k >> 2) << (g.lz + g.ly + 2)) + ((k & 3) << g.lz);
 }
 
 // ---------------------------------------------------------------- items
-template <int K>
-__device__ void apply_groups(float* __restrict__ x, const Geo& geo, int64_t beg, int64_t end, const float* P) {
-  for (int64_t gi = beg + threadIdx.x; gi < end; gi += blockDim.x) {
-    const int64_t b = group_base(geo, gi);
-    float v[K], y[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = x[b + in_offset<K>(geo, k)];
-#pragma unroll
-    for (int r = 0; r < K; ++r) {
-      float a = 0.f;
-#pragma unroll
-      for (int k = 0; k < K; ++k) a = fmaf(P[r * K + k], v[k], a);
-      y[r] = a;
-    }
-#pragma unroll
-    for (int r = 0; r < K; ++r) x[b + in_offset<K>(geo, r)] = y[r];
-  }
-}
-
 // Vectorised in-place apply.  Z >= 4: a thread takes V consecutive groups
 // (z .. z+V-1, 16- or 8-byte accesses per input); Z == 1: the K inputs of a
 // group along the less significant qubit are contiguous (16-byte accesses).
+// The per-op bodies are not inlined into the kernel: each gets its own
+// register allocation under the kernel's 128-register cap, so one op's
+// pressure does not spill into the others.
 template <int K>
-__device__ void apply_vec(float* __restrict__ x, const Geo& geo, int64_t beg, int64_t end, const float* P) {
+__device__ __noinline__ void apply_vec(float* __restrict__ x, const Geo& geo, int64_t beg, int64_t end, const float* P) {
   if (geo.lz >= 2) {
     constexpr int V = 4;
     for (int64_t gi = beg + (int64_t)threadIdx.x * V; gi < end; gi += (int64_t)blockDim.x * V) {
@@ -157,7 +143,7 @@ __device__ void apply_vec(float* __restrict__ x, const Geo& geo, int64_t beg, in
           v[k][0] = t.x; v[k][1] = t.y;
         }
       }
-#pragma unroll 2
+#pragma unroll 1
       for (int r = 0; r < K; ++r) {
         float y[V];
 #pragma unroll
@@ -203,7 +189,7 @@ __device__ void apply_vec(float* __restrict__ x, const Geo& geo, int64_t beg, in
 // dP[r][k] = sum g_out[r] x_in[k] accumulated in FP32 registers, folded to
 // FP64 every 16 groups, reduced over the block and written to dst (16
 // doubles).
-__device__ void adjoint1_vec(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
+__device__ __noinline__ void adjoint1_vec(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
                              int64_t end, const float* P, const float* Pi, BatchSmem& sm, double* __restrict__ dst) {
   float acc[16];
   double* accd = sm.acc[threadIdx.x];  // FP64 running sums live in shared memory
@@ -315,7 +301,7 @@ __device__ void adjoint1_vec(float* __restrict__ x, float* __restrict__ gv, cons
 // sums in shared memory;
 // at the end the warps' blocks are summed in a fixed order and written to
 // dst (256 doubles).
-__device__ void adjoint2_warp(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
+__device__ __noinline__ void adjoint2_warp(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
                               int64_t end, BatchSmem& sm, double* __restrict__ dst) {
   constexpr int K = 16;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -403,7 +389,7 @@ __device__ void adjoint2_warp(float* __restrict__ x, float* __restrict__ gv, con
   __syncthreads();
 }
 
-__device__ void loss_item(const qsgb_batch_program& p, const qsgb_batch_instance& in, int inst, BatchSmem& sm) {
+__device__ __noinline__ void loss_item(const qsgb_batch_program& p, const qsgb_batch_instance& in, int inst, BatchSmem& sm) {
   const int n = in.n_qubits;
   const int64_t D = 1ll << n;
   double part = 0.0;
