@@ -389,6 +389,7 @@ def run_gb300(args):
         extra['qutrit_8q'] = run_qutrit_config()
         extra['grad_10q'] = run_grad_config()
         extra.update(run_circuit_configs())
+        extra['ops'] = run_ops_config()
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -578,6 +579,67 @@ def run_circuit_configs():
                     'a line matching)',
         'units': f0.n_units, 'fused_passes': f0.n_passes,
         'seconds': times}
+    return out
+
+
+def run_ops_config():
+    """The non-apply operations of the backend, on resident states: on the
+    14-qubit FP64 vector diagonal, trace, meas_prob, partial_trace (keep 4)
+    and renormalize; on the 8-qutrit vector reduce_basis (9 -> 3, the
+    computational subbasis) and project.  Host wall time per call with a
+    device synchronisation, averaged over repetitions (diagonal and
+    partial_trace leave their result on the device)."""
+    import numpy as np
+    import torch
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases
+
+    def per_call(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    out = {}
+    n = N_QUBITS
+    s = qg.PauliVectorGB300([bases.general(2)] * n, force=True)
+    s._data.copy_(torch.rand_like(s._data) * 2.0 ** -14)
+    nbytes = 2 * 4 ** n * 8
+    out['diagonal_us'] = per_call(lambda: s.diagonal(get_data=False), 50) * 1e6
+    out['trace_us'] = per_call(s.trace, 50) * 1e6
+    out['meas_prob_us'] = per_call(lambda: s.meas_prob(5), 50) * 1e6
+    out['partial_trace_keep4_us'] = per_call(
+        lambda: s.partial_trace(0, 3, 5, 7), 20) * 1e6
+    t = per_call(s.renormalize, 10)
+    out['renormalize_ms'] = t * 1e3
+    out['renormalize_gbs'] = nbytes / t / 1e9
+    del s
+    g3 = bases.general(3)
+    comp = [g3.computational_basis_indices[i] for i in range(3)]
+
+    def reduce():
+        q = qg.PauliVectorGB300([g3] * 8, force=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q.reduce_basis(3, comp)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        q.project(5, 1)
+        torch.cuda.synchronize()
+        return t1 - t0, time.perf_counter() - t1
+    reduce()
+    tr, tp = min(reduce() for _ in range(5))
+    n_red = 9 ** 7 * 3  # entries kept by reduce_basis
+    out['reduce_basis_9to3_ms'] = tr * 1e3
+    out['reduce_basis_gbs'] = 2 * n_red * 8 / tr / 1e9
+    out['project_ms'] = tp * 1e3
+    out['workload'] = ('14 qubits FP64 (diagonal, trace, meas_prob, '
+                       'partial_trace keeping 4, renormalize); 8 qutrits '
+                       'FP64 (reduce_basis 9 -> 3 on one qutrit, then '
+                       'project another)')
     return out
 
 

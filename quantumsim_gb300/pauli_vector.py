@@ -78,10 +78,27 @@ class _PtmCache:
 _PTM_CACHE = _PtmCache()
 
 
+_PLAN_CACHE = {}
+
+
 def _diag_plan(bases):
     """Gather plan for diagonal(): per qudit, for each Hilbert index i the
     Pauli index x whose computational_basis_vectors row is exactly e_x, or
-    -1 for an all-zero row.  None if some row is neither."""
+    -1 for an all-zero row.  None if some row is neither.  Cached by the
+    identity of the basis objects (the cache keeps them alive, so an id is
+    never reused while its entry exists)."""
+    key = tuple(id(b) for b in bases)
+    hit = _PLAN_CACHE.get(key)
+    if hit is not None:
+        return hit[1]
+    plan = _diag_plan_of(bases)
+    if len(_PLAN_CACHE) > 256:
+        _PLAN_CACHE.clear()
+    _PLAN_CACHE[key] = (tuple(bases), plan)
+    return plan
+
+
+def _diag_plan_of(bases):
     idx_off, idx = [0], []
     for b in bases:
         cbv = np.asarray(b.computational_basis_vectors)
