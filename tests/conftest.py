@@ -49,12 +49,13 @@ def golden_bases(data, ids):
                        list(data['basis{}_labels'.format(i)])) for i in ids]
 
 
-def assert_close_dot(actual, expected, absref, rtol=RTOL_F64):
+def assert_close_dot(actual, expected, absref, rtol=RTOL_F64, atol=0.0):
     """Per-entry forward-error check of a contraction: |a - e| <= rtol *
-    (sum_k |P_rk| |x_k|), the natural scale of a dot product whose terms may
-    cancel (`absref` = the same contraction applied to |P| and |x|)."""
+    (sum_k |P_rk| |x_k|) + atol, the natural scale of a dot product whose
+    terms may cancel (`absref` = the same contraction applied to |P| and
+    |x|)."""
     actual, expected = np.asarray(actual), np.asarray(expected)
-    bound = rtol * np.asarray(absref) + 1e-300
+    bound = rtol * np.asarray(absref) + atol + 1e-300
     err = np.abs(actual - expected)
     worst = np.max(err / bound) if err.size else 0.0
     assert worst <= 1.0, 'max error / bound = {:.3g}'.format(worst)

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import assert_close_dot
+from conftest import ATOL_F64, assert_close_dot
 from oracle import pauli_vector_np as O
 import quantumsim_gb300 as qg
 from quantumsim_gb300 import bases as B
@@ -76,8 +76,9 @@ def test_graph_replay_equals_eager(dtype):
 def test_reference_operations_fused_on_gpu():
     """Units extracted from quantumsim operations (golden fixtures: an
     uncompiled chain, the chain on permuted qubits, compiled, compiled into
-    reduced bases) run fused on the GPU and reproduce the reference's
-    output."""
+    reduced bases, and a FinalizedCircuit applied to a State with `@`, whose
+    qubits start in one-element subbases) run fused on the GPU and reproduce
+    the reference's output."""
     import json
     import os
     d = np.load(os.path.join(os.path.dirname(__file__), 'golden',
@@ -87,9 +88,16 @@ def test_reference_operations_fused_on_gpu():
         units = [(d['c{}_u{}'.format(i, j)], tuple(qs))
                  for j, qs in enumerate(m['unit_qudits'])]
         x_in, x_out = d['c{}_in'.format(i)], d['c{}_out'.format(i)]
+        bases = [B.general(2) if d == 4 else B.general(2).subbasis([0])
+                 for d in m['dims_in']]
         for fuse in (False, True):
-            s = qg.PauliVectorGB300([B.general(2)] * 3, x_in)
+            s = qg.PauliVectorGB300(bases, x_in)
             C.FusedCircuit(units, fuse=fuse)(s)
             assert list(s._data.shape) == m['dims_out']
+            # absolute floor as in the golden checks: the kernels drop PTM
+            # entries below 2^-52 of the largest (the ~1e-17 residue of the
+            # complex arithmetic that built them), which leaves entries made
+            # only of such residue at 0 instead of ~1e-17
             assert_close_dot(s.to_pv(), x_out,
-                             _seq(np.abs(x_in), units, True) * 8)
+                             _seq(np.abs(x_in), units, True) * 8,
+                             atol=ATOL_F64)
