@@ -116,6 +116,23 @@ int qsgb_apply_ptm2(const void* in, void* out, const double* ptm,
                     unsigned* dev_status, void* stream);
 
 /*
+ * Compile ahead of time the kernel that qsgb_apply_ptm2 (or, with d0_out =
+ * d0_in = dim_x = 1, qsgb_apply_ptm1) would specialise at run time to this
+ * host PTM (QSGB_PTM_HOST required) and geometry, for tensors aligned as
+ * device allocators return them; nothing is launched and no tensor is
+ * touched.  Safe to call from several host threads at once, which compile
+ * in parallel: a circuit's distinct sparsity patterns can be prepared
+ * together instead of one by one at first use.  QSGB_OK when the kernel is
+ * ready, QSGB_ERR_UNSUPPORTED when the call would not use a specialised
+ * kernel (nothing to prepare).
+ * No counterpart in the reference (PyCUDA compiles its one kernel once).
+ */
+int qsgb_prepare_ptm2(const double* ptm, int64_t d0_out, int64_t d1_out,
+                      int64_t d0_in, int64_t d1_in, int64_t dim_x,
+                      int64_t dim_y, int64_t dim_z, int ptm_flags, int dtype,
+                      int arith);
+
+/*
  * Multi-axis take ("multitake"): out = in[np.ix_(idx_0, ..., idx_{n-1})].
  * Replaces: quantumsim/pauli_vectors/primitives.cu:100-130 (multitake, used by
  * cuda.py:279-345 diagonal()).  Index lists are CSR-like as in cuda.py:307-313

@@ -39,6 +39,8 @@ one vector into a CUDA graph (a static input and output buffer), so a
 circuit that is run many times on states of one shape costs one graph
 launch instead of one host call per unit.
 """
+import os
+
 import numpy as np
 import torch
 
@@ -245,6 +247,7 @@ class FusedCircuit:
                       for p, q in units]
         self.fused = plan(self.units) if fuse else list(self.units)
         self.bases_out = bases_out
+        self._prepared = set()
 
     @classmethod
     def from_operation(cls, operation, bases, *qubits, fuse=True):
@@ -261,8 +264,34 @@ class FusedCircuit:
     def n_passes(self):
         return len(self.fused)
 
+    def prepare(self, shape, dtype=torch.float64, arith=0, threads=None):
+        """Compile the specialised kernels of every fused PTM for a vector of
+        `shape` and `dtype` ahead of time, on `threads` host threads at
+        once (default: the host's cores, at most 32).  The library compiles
+        each sparsity pattern once per process (and caches it on disk), so
+        this only moves the work of the first application forward and
+        spreads it over the cores."""
+        from concurrent.futures import ThreadPoolExecutor
+        from . import ops
+        jobs, shape = [], tuple(shape)
+        for ptm, qudits in self.fused:
+            jobs.append((shape, ptm, qudits))
+            shape = tuple(ops.apply_geometry(shape, list(qudits),
+                                             ptm.shape)[0])
+        n = threads or min(32, os.cpu_count() or 1)
+        with ThreadPoolExecutor(max_workers=n) as pool:
+            list(pool.map(lambda j: ops.prepare_ptm(j[0], dtype, j[1], j[2],
+                                                    arith), jobs))
+        self._prepared.add((tuple(jobs[0][0]) if jobs else shape, dtype,
+                            arith))
+
     def __call__(self, pv):
-        """Apply the circuit to a PauliVectorGB300 (in place)."""
+        """Apply the circuit to a PauliVectorGB300 (in place).  The first
+        call for a vector shape compiles the circuit's kernels in parallel
+        (see prepare)."""
+        key = (tuple(pv._data.shape), pv._data.dtype, pv._arith)
+        if key not in self._prepared:
+            self.prepare(*key)
         for ptm, qudits in self.fused:
             pv.apply_ptm(ptm, *qudits)
         if self.bases_out is not None:

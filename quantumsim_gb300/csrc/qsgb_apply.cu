@@ -567,8 +567,10 @@ int launch_apply(ApplyParams& p, cudaStream_t stream) {
 // run-time specialised kernel (qsgb_jit.cu)
 // ---------------------------------------------------------------------------
 // Returns QSGB_ERR_UNSUPPORTED when the specialised path does not apply.
+// prepare_only: compile (or fetch) the kernel, launch nothing.
 int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_in, int64_t db_in, int64_t Z,
-            int flags, int dtype, int arith, bool pair, ApplyParams& p, cudaStream_t stream) {
+            int flags, int dtype, int arith, bool pair, ApplyParams& p, cudaStream_t stream,
+            bool prepare_only = false) {
   if (!(flags & QSGB_PTM_HOST) || (flags & QSGB_PTM_NOJIT) || !jit::available()) return QSGB_ERR_UNSUPPORTED;
   // Z == 1: the db inputs (outputs) of a group along the less significant
   // target are contiguous; move them with 2- or 4-wide vector accesses
@@ -605,6 +607,7 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
                         Z == 1, contiguous, vwidth(db_in, p.in), vwidth(db_out, p.out), spec, coef))
       return QSGB_ERR_UNSUPPORTED;
   }
+  if (prepare_only) return jit::prepare(spec);
   const int NL = pair ? 2 : 1;
   jit::Geometry g;
   g.in = p.in;
@@ -624,9 +627,11 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
   return jit::launch(spec, g, coef.data(), stream);
 }
 
+// prepare_only: validate, then compile the specialised kernel the call would
+// launch (for tensors aligned as allocators give them), and launch nothing.
 int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, int64_t db_out, int64_t da_in,
                  int64_t db_in, int64_t X, int64_t Y, int64_t Z, int flags, int dtype, int arith,
-                 int64_t max_terms, unsigned* status, void* stream) {
+                 int64_t max_terms, unsigned* status, void* stream, bool prepare_only = false) {
   if (!in || !out || !ptm) return QSGB_ERR_INVALID;
   if (in == out) return QSGB_ERR_INVALID;
   if (da_out < 1 || db_out < 1 || da_in < 1 || db_in < 1 || X < 1 || Y < 1 || Z < 1) return QSGB_ERR_INVALID;
@@ -670,8 +675,8 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
   // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)
-  const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s);
-  if (js != QSGB_ERR_UNSUPPORTED) return js;
+  const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s, prepare_only);
+  if (js != QSGB_ERR_UNSUPPORTED || prepare_only) return js;
   // 2. generic kernel; a host PTM travels inside its launch parameters
   if (flags & QSGB_PTM_HOST) {
     if (kin * kout > kMaxInline) return QSGB_ERR_UNSUPPORTED;
@@ -717,4 +722,15 @@ extern "C" int qsgb_apply_ptm2(const void* in, void* out, const double* ptm, int
                                void* stream) {
   return qsgb::apply_common(in, out, ptm, d0_out, d1_out, d0_in, d1_in, dim_x, dim_y, dim_z, ptm_flags, dtype,
                             arith, max_terms, dev_status, stream);
+}
+
+extern "C" int qsgb_prepare_ptm2(const double* ptm, int64_t d0_out, int64_t d1_out, int64_t d0_in, int64_t d1_in,
+                                 int64_t dim_x, int64_t dim_y, int64_t dim_z, int ptm_flags, int dtype, int arith) {
+  if (!(ptm_flags & QSGB_PTM_HOST)) return QSGB_ERR_INVALID;
+  // stand-in tensor addresses with the 256-byte alignment of the allocators
+  // (never dereferenced: nothing is launched)
+  const void* in = reinterpret_cast<const void*>(uintptr_t(256));
+  void* out = reinterpret_cast<void*>(uintptr_t(512));
+  return qsgb::apply_common(in, out, ptm, d0_out, d1_out, d0_in, d1_in, dim_x, dim_y, dim_z, ptm_flags, dtype,
+                            arith, 0, nullptr, nullptr, true);
 }

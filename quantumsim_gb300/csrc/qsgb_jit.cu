@@ -849,6 +849,11 @@ int kernel_for(const Spec& s, cudaKernel_t* k, std::string* src_out) {
   return QSGB_OK;
 }
 
+int prepare(const Spec& s) {
+  cudaKernel_t kern;
+  return kernel_for(s, &kern, nullptr);
+}
+
 int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t stream) {
   cudaKernel_t kern;
   const int st = kernel_for(s, &kern, nullptr);

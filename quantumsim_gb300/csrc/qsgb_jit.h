@@ -58,6 +58,8 @@ int kernel_for(const Spec& s, cudaKernel_t* k, std::string* src_out);
 // coef: one double per term in row order (dp: value; df: hi/lo float words;
 // f32: float bits in the low word).
 int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t stream);
+// Compile (or fetch from the caches) the kernel of `s` without launching it.
+int prepare(const Spec& s);
 
 }  // namespace jit
 }  // namespace qsgb

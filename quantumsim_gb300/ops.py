@@ -412,6 +412,30 @@ def scale_by_inverse_(pv: torch.Tensor, denom: torch.Tensor,
     L.check(status, 'qsgb_scale_by_inverse')
 
 
+def prepare_ptm(shape, dtype, ptm, qudits, arith, transpose=False):
+    """Compile ahead of time the specialised kernel that
+    ``torch.ops.qsgb.apply_ptm`` would use for this host PTM (numpy float64)
+    on a Pauli-vector tensor of `shape` and `dtype`; returns the shape of the
+    result.  Releases the GIL while compiling, so threads compile in
+    parallel.  A PTM served by the generic kernel needs nothing."""
+    ptm = np.ascontiguousarray(ptm, dtype=np.float64)
+    new_shape, (X, Y, Z), (dao, dbo, dai, dbi), swapped = apply_geometry(
+        tuple(shape), list(qudits), ptm.shape, transpose)
+    if math.prod(new_shape) == 0:
+        return new_shape
+    flags = L.PTM_HOST | (L.PTM_SWAPPED if swapped else 0) | (
+        L.PTM_TRANSPOSED if transpose else 0)
+    code = L.F64 if dtype == torch.float64 else L.F32
+    if len(qudits) == 1:
+        dao, dai, X = 1, 1, 1
+    st = L.load().qsgb_prepare_ptm2(
+        ctypes.c_void_p(ptm.ctypes.data), dao, dbo, dai, dbi, X, Y, Z, flags,
+        code, arith)
+    if st not in (L.OK, L.ERR_UNSUPPORTED):
+        L.check(st, 'qsgb_prepare_ptm2')
+    return new_shape
+
+
 def nnz_terms(ptm, arith):
     """Number of PTM entries the kernel keeps (same rule as the device):
     exact zeros are dropped for native FP64, otherwise entries with

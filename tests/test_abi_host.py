@@ -79,6 +79,10 @@ def test_argument_errors_rejected_on_host(lib):
     assert lib.qsgb_apply_ptm2(one, two, two, 9, 9, 9, 9, 1, 1, 1,
                                L.PTM_HOST | L.PTM_NOJIT, L.F64, 0, 0, null,
                                null) == L.ERR_UNSUPPORTED
+    # ahead-of-time preparation needs a host PTM (flags checked before
+    # anything is read)
+    assert lib.qsgb_prepare_ptm2(two, 4, 4, 4, 4, 1, 1, 1, 0, L.F64,
+                                 0) == L.ERR_INVALID
     # gathers
     assert lib.qsgb_take_axis(one, one, L.F64, 1, 4, 1, L.i32_array([0]), 1,
                               null) == L.ERR_INVALID

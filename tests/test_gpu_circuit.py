@@ -101,3 +101,26 @@ def test_reference_operations_fused_on_gpu():
             assert_close_dot(s.to_pv(), x_out,
                              _seq(np.abs(x_in), units, True) * 8,
                              atol=ATOL_F64)
+
+
+def test_parallel_preparation_then_apply():
+    """Kernels compiled ahead of time on several host threads
+    (FusedCircuit.prepare -> qsgb_prepare_ptm2) serve the applications:
+    results equal the unfused oracle, for FP64 and FP32 vectors."""
+    rng = np.random.default_rng(14)
+    units = [(p, qs) for _, p, qs in workloads.config1_circuit(
+        seed=21, n_qubits=7, n_layers=4, n_2q=3)[0]]
+    circ = C.FusedCircuit(units)
+    for dtype in (torch.float64, torch.float32):
+        circ.prepare((4,) * 7, dtype, 0, threads=8)
+        pv0 = rng.standard_normal((4,) * 7) / 128
+        s = qg.PauliVectorGB300([B.general(2)] * 7, pv0,
+                                dtype=np.float64 if dtype == torch.float64
+                                else np.float32)
+        circ(s)
+        ref = _seq(pv0, units)
+        if dtype == torch.float64:
+            assert_close_dot(s.to_pv(), ref, _seq(np.abs(pv0), units, True) * 8)
+        else:
+            np.testing.assert_allclose(s.to_pv(), ref, rtol=0,
+                                       atol=1e-5 * np.abs(ref).max())
