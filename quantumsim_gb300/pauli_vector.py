@@ -288,8 +288,26 @@ class PauliVectorGB300(_Base):
                 ops.nnz_terms(m, L.ARITH_DF64), False)
         return data.reshape(-1)
 
-    def diagonal(self, *, get_data=True):
+    def diagonal(self, *, get_data=True, target_array=None, flatten=True):
+        """Probabilities of the computational basis states, length
+        prod(dim_hilbert) (quantumsim/pauli_vectors/numpy.py:66-80).
+        `get_data=False` returns the float64 CUDA tensor.  As in the
+        reference's GPU backend (quantumsim/pauli_vectors/cuda.py:279-345),
+        `target_array` is an already allocated CUDA tensor that receives the
+        values (ValueError when too small), and `flatten=False` shapes the
+        result as dim_hilbert."""
         diag = self._diagonal_device()
+        if target_array is not None:
+            n = diag.numel()
+            if target_array.numel() < n:
+                raise ValueError(
+                    'Size of `target_array` is too small ({}).\n'
+                    'Should be at least {}.'.format(target_array.numel(), n))
+            view = target_array.reshape(-1)[:n]
+            view.copy_(diag)
+            diag = view
+        if not flatten:
+            diag = diag.reshape(tuple(self.dim_hilbert))
         if not get_data:
             return diag
         ops.check_device_status(self._device)

@@ -471,3 +471,25 @@ def test_14_qubit_properties():
     a = x.data
     b = s.data
     assert torch.equal(a, 2 * b)
+
+
+def test_diagonal_target_array_and_flatten():
+    """The reference GPU backend's diagonal() keywords: an allocated target
+    tensor receives the values, flatten=False shapes them as dim_hilbert."""
+    rng = np.random.default_rng(61)
+    bases = [B.general(2), B.general(3), B.general(2)]
+    pv = rand_pv(rng, (4, 9, 4))
+    s = GB(bases, pv)
+    ref = O.diagonal(pv, bases)
+    target = torch.zeros(40, dtype=torch.float64, device='cuda')
+    d = s.diagonal(get_data=False, target_array=target)
+    assert d.data_ptr() == target.data_ptr()
+    np.testing.assert_allclose(target[:12].cpu().numpy(), ref, rtol=0,
+                               atol=ATOL_PROB)
+    shaped = s.diagonal(flatten=False)
+    assert shaped.shape == (2, 3, 2)
+    np.testing.assert_allclose(shaped.reshape(-1), ref, rtol=0,
+                               atol=ATOL_PROB)
+    with pytest.raises(ValueError):
+        s.diagonal(target_array=torch.zeros(5, dtype=torch.float64,
+                                            device='cuda'))
