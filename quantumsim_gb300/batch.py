@@ -188,7 +188,11 @@ class BatchedSimulator:
         entry per instance; an entry covering `total` groups (or elements)
         becomes ceil(total / chunk) items with chunk = max(tile,
         ceil(total / max_items)) -- large ops are shared by many blocks, and
-        no op has more than `max_items` items."""
+        no op has more than `max_items` items.  `tile` is a multiple of 4:
+        the kernel takes 4 consecutive groups along z per access, and an
+        item boundary must not split them."""
+        if tile < 4 or tile % 4:
+            raise ValueError('tile must be a positive multiple of 4')
         ent = []  # (stage, op, inst, q0, q1, ptm or checkpoint, total)
         for i, s in enumerate(self.specs):
             size = self.sizes[i]

@@ -28,16 +28,21 @@ namespace {
 
 constexpr int kBatchBlock = 256;
 constexpr int kRedRows = kBatchBlock / 16;  // rows of the FP64 dP reduction buffer (>= warps)
+// floats per staged group in the adjoint tile: 16 values + 4 of padding, so
+// that 16-byte stores of consecutive lanes fall in distinct banks
+constexpr int kTileStride = 20;
 
 struct BatchSmem {
   float P[256];
+  float PT[256];  // P transposed (ADJOINT: g_in = P^T g_out)
   float Pi[256];
-  // adjoint tile: g_out and x_in per group, [group][16], one 32-group slice
-  // per warp; reused for the FP64 cross-warp sums of the dP partials
+  // adjoint tile: g_out and x_in per group, [group][kTileStride], one
+  // 32-group slice per warp; reused for the FP64 cross-warp sums of the dP
+  // partials
   union {
     struct {
-      float g[kBatchBlock][16];
-      float x[kBatchBlock][16];
+      float g[kBatchBlock][kTileStride];
+      float x[kBatchBlock][kTileStride];
     } t;
     double red[kRedRows][256];
   } u __attribute__((aligned(16)));
@@ -46,6 +51,25 @@ struct BatchSmem {
   int ok;
   double lsum[kBatchBlock / 32];
 };
+
+}  // namespace
+
+// The block's dynamic shared memory, at namespace scope so that the op
+// bodies (separate functions) address it as shared memory.
+extern __shared__ __align__(16) unsigned char batch_dsm[];
+
+namespace {
+
+__device__ __forceinline__ BatchSmem& smem() { return *reinterpret_cast<BatchSmem*>(batch_dsm); }
+
+// A zero the compiler cannot see through: shared-memory loads indexed with it
+// are scheduled within the loop iteration that obtains it instead of being
+// hoisted out of the loop (which would hold a whole 16 x 16 PTM in registers).
+__device__ __forceinline__ int opaque_zero() {
+  int z;
+  asm volatile("mov.b32 %0, 0;" : "=r"(z));
+  return z;
+}
 
 __device__ __forceinline__ volatile uint32_t* vol(uint32_t* p) { return p; }
 
@@ -294,22 +318,27 @@ __device__ __noinline__ void adjoint1_vec(float* __restrict__ x, float* __restri
 
 // Two-qubit ADJOINT with independent warps: each warp takes tiles of 32
 // consecutive groups (lane = group), computes x_in = P^-1 x_out and
-// g_in = P^T g_out, stages x_in and g_out of its tile in its own slice of
-// the shared tile, and after a __syncwarp each lane accumulates a 2 x 4
-// block of dP over the tile's 32 groups.  No block barrier inside the loop.
+// g_in = P^T g_out (rows of both as 16-byte shared loads), stages x_in and
+// g_out of its tile in its own slice of the shared tile (padded rows: no bank
+// conflicts), and after a __syncwarp each lane accumulates a 2 x 4 block of
+// dP over the tile's 32 groups.  When the pair includes the last qubit
+// (Z == 1) the inputs 4a .. 4a+3 of a group are contiguous and move as one
+// 16-byte access.  No block barrier inside the loop.
 // FP32 products are carried over 4 tiles, then folded into the thread's FP64
 // sums in shared memory;
 // at the end the warps' blocks are summed in a fixed order and written to
 // dst (256 doubles).
 __device__ __noinline__ void adjoint2_warp(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
-                              int64_t end, BatchSmem& sm, double* __restrict__ dst) {
+                              int64_t end, double* __restrict__ dst) {
   constexpr int K = 16;
+  BatchSmem& sm = smem();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
-  // this warp's slice of the tile: x_in and g_out of 32 groups, [group][16]
-  float(*wx)[16] = &sm.u.t.x[warp * 32];
-  float(*wg)[16] = &sm.u.t.g[warp * 32];
+  // this warp's slice of the tile: x_in and g_out of 32 groups
+  float(*wx)[kTileStride] = &sm.u.t.x[warp * 32];
+  float(*wg)[kTileStride] = &sm.u.t.g[warp * 32];
   const int r0 = 2 * (lane >> 2), c0 = 4 * (lane & 3);
+  const bool vec = geo.lz == 0;
   float s[8];
   double* acc = sm.acc[threadIdx.x];  // FP64 running sums in shared memory
 #pragma unroll
@@ -323,26 +352,60 @@ __device__ __noinline__ void adjoint2_warp(float* __restrict__ x, float* __restr
     if (gi < end) {
       const int64_t b = group_base(geo, gi);
       float xo[K], go[K];
+      if (vec) {
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        xo[k] = x[b + in_offset<K>(geo, k)];
-        go[k] = gv[b + in_offset<K>(geo, k)];
-      }
-#pragma unroll
-      for (int r = 0; r < K; ++r) {
-        float a = 0.f, c = 0.f;
+        for (int q = 0; q < K / 4; ++q) {
+          const float4 u = *reinterpret_cast<const float4*>(x + b + in_offset<K>(geo, 4 * q));
+          const float4 w = *reinterpret_cast<const float4*>(gv + b + in_offset<K>(geo, 4 * q));
+          xo[4 * q] = u.x; xo[4 * q + 1] = u.y; xo[4 * q + 2] = u.z; xo[4 * q + 3] = u.w;
+          go[4 * q] = w.x; go[4 * q + 1] = w.y; go[4 * q + 2] = w.z; go[4 * q + 3] = w.w;
+        }
+      } else {
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-          a = fmaf(sm.Pi[r * K + k], xo[k], a);
-          c = fmaf(sm.P[k * K + r], go[k], c);
+          xo[k] = x[b + in_offset<K>(geo, k)];
+          go[k] = gv[b + in_offset<K>(geo, k)];
         }
-        x[b + in_offset<K>(geo, r)] = a;
-        gv[b + in_offset<K>(geo, r)] = c;
-        wx[lane][r] = a;
       }
+      const int z0 = opaque_zero();
+      const float4* pi4 = reinterpret_cast<const float4*>(sm.Pi) + z0;
+      const float4* pt4 = reinterpret_cast<const float4*>(sm.PT) + z0;
 #pragma unroll
-      for (int k = 0; k < K; k += 4)
-        *reinterpret_cast<float4*>(&wg[lane][k]) = make_float4(go[k], go[k + 1], go[k + 2], go[k + 3]);
+      for (int rq = 0; rq < K / 4; ++rq) {
+        float a[4], c[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = 4 * rq + i;
+          float u = 0.f, w = 0.f;
+#pragma unroll
+          for (int q = 0; q < K / 4; ++q) {
+            const float4 pi = pi4[r * 4 + q], pt = pt4[r * 4 + q];
+            u = fmaf(pi.x, xo[4 * q], u);
+            u = fmaf(pi.y, xo[4 * q + 1], u);
+            u = fmaf(pi.z, xo[4 * q + 2], u);
+            u = fmaf(pi.w, xo[4 * q + 3], u);
+            w = fmaf(pt.x, go[4 * q], w);
+            w = fmaf(pt.y, go[4 * q + 1], w);
+            w = fmaf(pt.z, go[4 * q + 2], w);
+            w = fmaf(pt.w, go[4 * q + 3], w);
+          }
+          a[i] = u;
+          c[i] = w;
+        }
+        if (vec) {
+          *reinterpret_cast<float4*>(x + b + in_offset<K>(geo, 4 * rq)) = make_float4(a[0], a[1], a[2], a[3]);
+          *reinterpret_cast<float4*>(gv + b + in_offset<K>(geo, 4 * rq)) = make_float4(c[0], c[1], c[2], c[3]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            x[b + in_offset<K>(geo, 4 * rq + i)] = a[i];
+            gv[b + in_offset<K>(geo, 4 * rq + i)] = c[i];
+          }
+        }
+        *reinterpret_cast<float4*>(&wx[lane][4 * rq]) = make_float4(a[0], a[1], a[2], a[3]);
+        *reinterpret_cast<float4*>(&wg[lane][4 * rq]) =
+            make_float4(go[4 * rq], go[4 * rq + 1], go[4 * rq + 2], go[4 * rq + 3]);
+      }
     } else {
 #pragma unroll
       for (int k = 0; k < K; k += 4) {
@@ -444,8 +507,12 @@ __device__ void process(const qsgb_batch_program& p, const qsgb_batch_item& it, 
       const Geo geo = geometry(in.n_qubits, it.q0, it.q1);
       const int kk = geo.k * geo.k;
       for (int e = threadIdx.x; e < kk; e += blockDim.x) {
-        sm.P[e] = p.ptm[(int64_t)it.ptm * 256 + e];
-        if (it.op == QSGB_BOP_ADJOINT) sm.Pi[e] = p.ptm_inv[(int64_t)it.ptm * 256 + e];
+        const float v = p.ptm[(int64_t)it.ptm * 256 + e];
+        sm.P[e] = v;
+        if (it.op == QSGB_BOP_ADJOINT) {
+          sm.PT[(e % geo.k) * geo.k + e / geo.k] = v;
+          sm.Pi[e] = p.ptm_inv[(int64_t)it.ptm * 256 + e];
+        }
       }
       __syncthreads();
       if (it.op == QSGB_BOP_APPLY) {
@@ -456,7 +523,7 @@ __device__ void process(const qsgb_batch_program& p, const qsgb_batch_item& it, 
       } else if (geo.k == 4) {
         adjoint1_vec(in.x, in.g, geo, it.beg, it.end, sm.P, sm.Pi, sm, p.grad_partial + (int64_t)it.slot * 256);
       } else {
-        adjoint2_warp(in.x, in.g, geo, it.beg, it.end, sm, p.grad_partial + (int64_t)it.slot * 256);
+        adjoint2_warp(in.x, in.g, geo, it.beg, it.end, p.grad_partial + (int64_t)it.slot * 256);
       }
       __syncthreads();
       break;
