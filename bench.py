@@ -804,6 +804,37 @@ def run_profile_batched(args):
                       'achieved_gbs': sim.algorithmic_bytes() / ms / 1e6}))
 
 
+def run_profile_adjoint2(args):
+    """Workload for ncu captures of the batched two-qubit adjoint: 16
+    circuits of 12 qubits, each 12 CZs on the pair `--profile-pair` (default
+    5,6), forward + adjoint as one plain launch per step, 2 steps (3.2 GB on
+    the device with adjoint and checkpoint buffers)."""
+    import math
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    from quantumsim_gb300 import batch as BT
+    from quantumsim_gb300 import ptm as P
+    q0, q1 = (int(v) for v in args.profile_pair.split(','))
+    cz = P.cphase(math.pi).reshape(16, 16).double()
+
+    class PairSpec(BT.CircuitSpec):
+        def ops(self):
+            return [(0, (q0, q1))] * 12
+
+    specs = [PairSpec(12, 1, i) for i in range(16)]
+    uniform = [torch.full((2 ** 12,), 1.0 / 2 ** 12, dtype=torch.float64)
+               for _ in specs]
+    sim = BT.BatchedSimulator(specs, uniform, checkpoint_every=8, tile=8192)
+    sim.set_ptms([[cz] * 12 for _ in specs])
+    for _ in range(2):
+        sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    sim.check()
+    print(json.dumps({'profile_case': 'adjoint2', 'pair': [q0, q1],
+                      'loss0': float(sim.results()[1][0])}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
     ap.add_argument('--gpus', type=int, default=1)
@@ -821,13 +852,16 @@ def main():
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', nargs='?', const='apply',
-                    choices=['apply', 'qutrits', 'batched', 'circuit'],
+                    choices=['apply', 'qutrits', 'batched', 'circuit',
+                             'adjoint2'],
                     help='run a small ncu profiling workload and exit')
     ap.add_argument('--profile-qubits', type=int, default=12)
+    ap.add_argument('--profile-pair', default='5,6',
+                    help='qubit pair of the adjoint2 profiling workload')
     args = ap.parse_args()
     if args.profile_case:
         {'apply': run_profile_case, 'qutrits': run_profile_qutrits,
-         'batched': run_profile_batched,
+         'batched': run_profile_batched, 'adjoint2': run_profile_adjoint2,
          'circuit': run_profile_circuit}[args.profile_case](args)
         return
     if args.warmup < 3 and args.impl == 'gb300':
