@@ -97,3 +97,43 @@ def test_batched_tiles_and_autotune_give_same_results():
     for gi_b, gi_c in zip(g_b, g_c):
         for b, c in zip(gi_b, gi_c):
             assert torch.equal(b, c)
+
+
+def test_grid_barrier_wait_expires_and_context_survives():
+    """Every grid barrier polls a bounded number of times.  A barrier that no
+    block can complete (its arrival counter starts past the grid size, a
+    flag nothing will set) ends after the spin limit: the kernel reports
+    QSGB_DEV_TIMEOUT, all blocks return, and the next normal step on the same
+    context gives the same results as before."""
+    import ctypes
+
+    from quantumsim_gb300 import _lib as L
+
+    ns = [5, 4, 6]
+    specs, targets, ptms = _setup(ns, depth=4, every=2, seed=21)
+    sim = BT.BatchedSimulator(specs, targets, checkpoint_every=2, tile=256)
+    sim.set_ptms(ptms)
+    sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    probs0, loss0, _ = [x for x in sim.results()]
+    probs0 = [p.clone() for p in probs0]
+    loss0 = loss0.clone()
+
+    sim.work.zero_()
+    sim.work[sim.n_stages] = 1 << 30  # barrier arrival counter
+    st = sim.lib.qsgb_batch_run(
+        ctypes.byref(sim.prog), sim.max_grid, BT.BLOCK, 1,
+        ctypes.c_void_p(sim.status.data_ptr()), 20000,
+        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    L.check(st, 'qsgb_batch_run')
+    torch.cuda.synchronize()
+    assert int(sim.status.item()) & L.DEV_TIMEOUT
+    with pytest.raises(RuntimeError, match='device status'):
+        sim.check()  # reports and clears the status
+
+    sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    probs1, loss1, _ = sim.results()
+    for a, b in zip(probs0, probs1):
+        assert torch.equal(a, b)
+    assert torch.equal(loss0, loss1)
