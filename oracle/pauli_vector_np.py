@@ -96,6 +96,29 @@ def renormalize(pv, bases):
     return pv, tr
 
 
+PAULI = {
+    'I': np.array([[1, 0], [0, 1]], dtype=complex),
+    'X': np.array([[0, 1], [1, 0]], dtype=complex),
+    'Y': np.array([[0, -1j], [1j, 0]], dtype=complex),
+    'Z': np.array([[1, 0], [0, -1]], dtype=complex),
+}
+
+
+def exp_value(pv, bases, operator):
+    """Expectation value of a Pauli string, one letter per qubit
+    (quantumsim/states/state.py:43-83): the contraction of sigma_q[a, b],
+    the Pauli vector and each basis' vectors[k, b, a].  Complex, as numpy's
+    einsum of complex arrays returns it."""
+    n = len(bases)
+    args = []
+    for i, ch in enumerate(operator):
+        args += [PAULI[ch.upper()], [i, n + i]]
+    args += [pv, [2 * n + i for i in range(n)]]
+    for i, b in enumerate(bases):
+        args += [b.vectors, [2 * n + i, n + i, i]]
+    return np.einsum(*args, optimize=True)
+
+
 def reduce_basis(pv, qubit, indices):
     """Basis reduction as the selection PTM eye(d)[indices] applied to
     `qubit` (quantumsim/operations/operation.py:549-551 with a rectangular

@@ -39,6 +39,15 @@ import torch
 from . import _lib as L
 from . import ops
 
+# Pauli matrices of the operator strings of exp_value
+# (quantumsim/algebra/tools.py:4-13)
+_PAULI = {
+    'I': np.array([[1, 0], [0, 1]], dtype=complex),
+    'X': np.array([[0, 1], [1, 0]], dtype=complex),
+    'Y': np.array([[0, -1j], [1j, 0]], dtype=complex),
+    'Z': np.array([[1, 0], [0, -1]], dtype=complex),
+}
+
 try:  # subclass the reference ABC when the quantumsim package is present
     with warnings.catch_warnings():
         warnings.simplefilter('ignore')
@@ -355,6 +364,43 @@ class PauliVectorGB300(_Base):
         return tr
 
     # ------------------------------------------------------------ new API
+    def exp_value(self, operator):
+        """Expectation value tr(rho O) of a Pauli string `operator` (one of
+        I, X, Y, Z per qubit, any case), computed on the device.
+
+        The reference contracts the host copy of the Pauli vector with
+        sigma_q[a, b] and each basis' vectors[k, b, a]
+        (quantumsim/states/state.py:43-83).  For a string that contraction is
+        sum_k pv[k] prod_q w_q[k_q] with w_q[k] = tr(sigma_q P_k): the
+        weighted full contraction of the partial-trace kernel with no qudit
+        kept (FP64 accumulation).  Same ValueErrors as the reference; the
+        value is returned as a float (the reference's einsum returns the
+        same number as a complex with zero imaginary part).  Dense operator
+        arrays are left to the reference's host contraction."""
+        if not isinstance(operator, str):
+            raise NotImplementedError(
+                'exp_value on the device takes Pauli strings; dense operators '
+                'are contracted on the host by State.exp_value')
+        n = self.n_qubits
+        if n != len(operator):
+            raise ValueError("operator string must have the same length "
+                             "as number of qubits in the state")
+        try:
+            sigmas = [_PAULI[ch.upper()] for ch in operator]
+        except KeyError as ex:
+            raise ValueError("operator string must contain only I, X, "
+                             "Y or Z") from ex
+        weights = []
+        for s, b in zip(sigmas, self.bases):
+            if b.dim_hilbert != 2:
+                raise ValueError('Pauli strings act on qubits; qudit basis '
+                                 'of dimension {}'.format(b.dim_hilbert))
+            w = np.einsum('ab,kba->k', s, np.asarray(b.vectors))
+            weights.extend(float(v) for v in np.real(w))
+        out = torch.ops.qsgb.partial_trace(self._data, [0] * n, weights)
+        ops.check_device_status(self._device)
+        return float(out.item())
+
     def reduce_basis(self, qubit, indices):
         """Keep only the Pauli elements `indices` of `qubit`'s basis
         (e.g. 9 -> 3 with the computational subbasis of a qutrit) and

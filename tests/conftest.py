@@ -39,6 +39,23 @@ def golden():
     return data
 
 
+EXP_GOLDEN = os.path.join(ROOT, 'tests', 'golden', 'exp_value_golden.npz')
+
+
+def exp_value_cases():
+    """(name, Pauli vector, bases, operator strings, reference values) of
+    the State.exp_value fixtures."""
+    from quantumsim_gb300.bases import PauliBasis
+    data = np.load(EXP_GOLDEN, allow_pickle=False)
+    out = []
+    for i, c in enumerate(json.loads(str(data['meta']))):
+        bases = [PauliBasis(data['c{}_b{}_vectors'.format(i, q)], labels)
+                 for q, labels in enumerate(c['labels'])]
+        out.append((c['name'], data['c{}_pv'.format(i)], bases, c['ops'],
+                    data['c{}_val'.format(i)]))
+    return out
+
+
 def golden_cases(data):
     return json.loads(str(data['manifest']))
 

@@ -493,3 +493,36 @@ def test_diagonal_target_array_and_flatten():
     with pytest.raises(ValueError):
         s.diagonal(target_array=torch.zeros(5, dtype=torch.float64,
                                             device='cuda'))
+
+
+def test_exp_value_matches_reference_fixtures():
+    """Pauli-string expectation values on the device against the
+    reference's State.exp_value (full bases, reshuffled subbases, a circuit
+    run from State's one-element starting bases, the starting state)."""
+    from conftest import exp_value_cases
+    for name, pv, bases, ops, vals in exp_value_cases():
+        s = GB(bases, pv.copy())
+        for op, v in zip(ops, vals):
+            assert s.exp_value(op) == pytest.approx(float(v.real), abs=1e-13), \
+                (name, op)
+
+
+def test_exp_value_large_state_storage_types_and_errors():
+    rng = np.random.default_rng(62)
+    n = 10
+    bases = [B.general(2)] * n
+    pv = rand_pv(rng, (4,) * n)
+    s = GB(bases, pv)
+    s32 = GB(bases, pv.astype(np.float32), dtype=np.float32)
+    for op in ['XYZIZYXIIZ', 'IIIIIIIIII', 'ZZZZZZZZZZ', 'xyzixyzixy']:
+        ref = float(O.exp_value(pv, bases, op).real)
+        assert s.exp_value(op) == pytest.approx(ref, rel=1e-12, abs=1e-13)
+        ref32 = float(O.exp_value(pv.astype(np.float32).astype(np.float64),
+                                  bases, op).real)
+        assert s32.exp_value(op) == pytest.approx(ref32, rel=1e-6, abs=1e-7)
+    with pytest.raises(ValueError, match='same length'):
+        s.exp_value('XX')
+    with pytest.raises(ValueError, match='only I, X'):
+        s.exp_value('XXXXXXXXXA')
+    with pytest.raises(NotImplementedError):
+        s.exp_value(np.eye(2 ** n))

@@ -238,3 +238,13 @@ def test_fused_model_layers_equal_unfused_on_host():
     assert res[True][0] == pytest.approx(res[False][0], rel=1e-12)
     np.testing.assert_allclose(res[True][1], res[False][1], rtol=1e-9,
                                atol=1e-14)
+
+
+def test_oracle_exp_value_matches_reference_fixtures():
+    """The oracle's Pauli-string expectation values against
+    State.exp_value of the reference (quantumsim/states/state.py:43-83)."""
+    from conftest import exp_value_cases
+    for name, pv, bases, ops, vals in exp_value_cases():
+        for op, v in zip(ops, vals):
+            np.testing.assert_allclose(O.exp_value(pv, bases, op), v,
+                                       rtol=0, atol=1e-14, err_msg=name)
