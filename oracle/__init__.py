@@ -1,4 +1,4 @@
-"""Checkers of the density-matrix hot path (test infrastructure only).
+"""Oracles of the density-matrix hot path (test infrastructure only).
 
 ``oracle/pauli_vector_np.py``: the CPU oracle.  ``oracle/ref_gpu.py``: the
 reference's own CUDA kernel, compiled from the reference source tree by

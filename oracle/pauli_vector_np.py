@@ -1,7 +1,7 @@
 """CPU oracle of the density-matrix hot path -- TEST INFRASTRUCTURE ONLY.
 
 A plain-numpy restatement of the reference backend ``PauliVectorNumpy``
-(quantumsim/pauli_vectors/numpy.py) used as the checker for the GB300
+(quantumsim/pauli_vectors/numpy.py), the oracle of the GB300
 kernels: only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
 leg of ``bench.py`` may import it.  The product (``quantumsim_gb300``) never
 calls it.

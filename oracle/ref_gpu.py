@@ -1,4 +1,4 @@
-"""The reference's own GPU kernel as a second checker and as the reference
+"""The reference's own GPU kernel as a second oracle and as the reference
 arm's GPU timing -- test infrastructure, never part of the product.
 
 ``oracle/_ref/primitives_sm103a.cubin`` is quantumsim's

@@ -4,7 +4,7 @@
 // linkage as PyCUDA's SourceModule compiles it, for sm_103a.  The result,
 // oracle/_ref/primitives_sm103a.cubin, is test and reference-arm
 // infrastructure only: the parity tests use the reference kernel as a second
-// checker and bench.py's reference arm times it; the product never loads it.
+// oracle and bench.py's reference arm times it; the product never loads it.
 extern "C" {
 #include QSGB_REF_PRIMITIVES
 }

@@ -1,5 +1,5 @@
 """The reference's own GPU kernel (quantumsim/pauli_vectors/primitives.cu,
-compiled unchanged for sm_103a into oracle/_ref) as a second checker: on the
+compiled unchanged for sm_103a into oracle/_ref) as a second oracle: on the
 same inputs it agrees with the GB300 kernels and with the oracle, for
 one-qubit PTMs at every position and two-qubit PTMs on every ordered pair
 (the reference's transposition for qubit0 > qubit1 included)."""
