@@ -9,15 +9,22 @@ KL(target || prob) and dL/dP for every PTM of its circuit.
 
 Circuits are the CPU-runnable workload family: per layer a noisy rotation on
 every qubit (rotation, then amplitude + phase damping over 20 ns) and CZs on
-a line matching.  The device program is built once per circuit structure:
+a line matching.  Ops are grouped into units first (`plan_units`): a CZ
+absorbs the rotations before it on its two qubits, so a layer of n rotations
+and ~n/2 CZs costs ~n/2 passes over the state instead of ~3n/2.  The device
+program is built once per circuit structure:
 
     stage 0              INIT  (|0..0>)
-    stages ...           APPLY of op j of every instance (instances aligned
-                         by op index), SAVE at every `checkpoint_every` layers
+    stages ...           APPLY of unit j of every instance (instances aligned
+                         by unit index), SAVE at every `checkpoint_every`
+                         layers
                          ZERO_G, LOSS
-    stages ...           ADJOINT of the ops in reverse, RESTORE at the saved
-                         layers (drift refresh)
-    last stage           GRADSUM per PTM
+    stages ...           ADJOINT of the units in reverse, RESTORE at the
+                         saved layers (drift refresh)
+    last stage           GRADSUM per unit PTM
+
+after which batched 16 x 16 contractions turn the units' gradients into
+dL/dP of every original op.
 
 Each op on a large instance is split into tiles of `tile` groups, so blocks
 share big instances while small ones take one item.  ``autotune()`` times the
@@ -129,11 +136,61 @@ def target_probabilities(spec, seed):
     return diagonal_diff(x, [_bases.general(2)] * spec.n).detach()
 
 
+def plan_units(ops, fuse=True):
+    """Group a circuit's ops into the units the kernel applies.
+
+    ops: [(layer, qubits)] in application order.  With `fuse`, a two-qubit
+    op absorbs the one-qubit ops still pending on its two qubits in the same
+    layer: the unit's PTM is F = C (R_a (x) R_b), a dense 16 x 16 PTM like any
+    two-qubit PTM of the kernel, so the unit costs one pass where the three
+    ops cost three.  One-qubit ops that meet no two-qubit op in their layer
+    stay single units.  A pending op is only delayed past ops on other
+    qubits, and every layer ends with its own units, so checkpoints still
+    fall between layers.
+
+    Returns [(layer, qubits, members)]: members = (j,) for a one-qubit unit
+    (qubits = (q,)), (j_c, j_a, j_b) for a two-qubit unit (qubits = (a, b)
+    sorted; j_a / j_b = -1 where no one-qubit op was absorbed)."""
+    units = []
+    pending = {}
+    layer = None
+
+    def flush():
+        for q, j in sorted(pending.items(), key=lambda t: t[1]):
+            units.append((ops[j][0], (q,), (j,)))
+        pending.clear()
+
+    for j, (l, qs) in enumerate(ops):
+        if l != layer:
+            flush()
+            layer = l
+        if len(qs) == 1:
+            q = qs[0]
+            if not fuse:
+                units.append((l, (q,), (j,)))
+                continue
+            if q in pending:
+                units.append((l, (q,), (pending.pop(q),)))
+            pending[q] = j
+        else:
+            a, b = min(qs), max(qs)
+            ja = pending.pop(a, -1)
+            jb = pending.pop(b, -1)
+            units.append((l, (a, b), (j, ja, jb)))
+    flush()
+    return units
+
+
 class BatchedSimulator:
-    """Forward + adjoint of many circuits in one persistent launch."""
+    """Forward + adjoint of many circuits in one persistent launch.
+
+    With `fuse` (default) each two-qubit op absorbs the one-qubit ops before
+    it on its qubits (`plan_units`); `results()` still returns dL/dP for
+    every original op: step() maps the units' gradients back with batched
+    16 x 16 contractions on the same stream (inside the CUDA graph)."""
 
     def __init__(self, specs, targets, checkpoint_every=8, tile=None,
-                 device=None, cooperative=True):
+                 device=None, cooperative=True, fuse=True):
         self.lib = L.load()
         self.device = torch.device(device or 'cuda')
         self.specs = specs
@@ -166,14 +223,24 @@ class BatchedSimulator:
                                 int(self.diag_off[i]))
         self.inst_dev = torch.frombuffer(bytearray(bytes(inst)),
                                          dtype=torch.uint8).to(dev)
-        # ---- PTM pool: one slot per op of every instance
-        self.op_base = np.cumsum([0] + [len(s.ops()) for s in specs])
-        self.n_ptm = int(self.op_base[-1])
+        # ---- units (fused ops) and the PTM pool: one slot per unit
+        self.fuse = fuse
+        self.ops = [s.ops() for s in specs]
+        self.units = [plan_units(o, fuse) for o in self.ops]
+        self.op_base = np.cumsum([0] + [len(o) for o in self.ops])
+        self.n_ops = int(self.op_base[-1])
+        self.unit_base = np.cumsum([0] + [len(u) for u in self.units])
+        self.n_ptm = int(self.unit_base[-1])
+        self._index_units()
         self.ptm = torch.zeros(self.n_ptm, 256, dtype=torch.float32,
                                device=dev)
         self.ptm_inv = torch.zeros_like(self.ptm)
         self.grad = torch.zeros(self.n_ptm, 256, dtype=torch.float64,
                                 device=dev)
+        # dL/dP per original op (the units' gradients mapped back)
+        self.op_grad = torch.zeros(self.n_ops, 256, dtype=torch.float64,
+                                   device=dev)
+        self._factors = None
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.max_grid = self.lib.qsgb_batch_max_grid(BLOCK)
         if self.max_grid < 1:
@@ -196,11 +263,11 @@ class BatchedSimulator:
         ent = []  # (stage, op, inst, q0, q1, ptm or checkpoint, total)
         for i, s in enumerate(self.specs):
             size = self.sizes[i]
-            ops = s.ops()
+            ops = [(l, qs) for l, qs, _ in self.units[i]]
             layer_of = [l for l, _ in ops]
             seq = [(BOP_INIT, -1, -1, 0, size)]
             for j, (l, qs) in enumerate(ops):
-                pidx = int(self.op_base[i]) + j
+                pidx = int(self.unit_base[i]) + j
                 q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
                 seq.append((BOP_APPLY, q0, q1, pidx,
                             size // (4 if q1 < 0 else 16)))
@@ -213,7 +280,7 @@ class BatchedSimulator:
             seq.append((BOP_LOSS, -1, -1, 0, 1))
             for j in reversed(range(len(ops))):
                 l, qs = ops[j]
-                pidx = int(self.op_base[i]) + j
+                pidx = int(self.unit_base[i]) + j
                 q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
                 seq.append((BOP_ADJOINT, q0, q1, pidx,
                             size // (4 if q1 < 0 else 16)))
@@ -292,44 +359,110 @@ class BatchedSimulator:
 
     def algorithmic_bytes(self):
         """HBM bytes one step must move with FP32 vectors of N entries:
-        APPLY reads and writes the state (8 N), ADJOINT reads x_out and g_out
-        and writes x_in and g_in (16 N), SAVE and RESTORE copy it (8 N each),
-        INIT and ZERO_G write it (4 N each), LOSS reads the 2^n diagonal
-        entries.  PTMs, dP partials and their sums are negligible."""
+        APPLY of a unit reads and writes the state (8 N), ADJOINT reads x_out
+        and g_out and writes x_in and g_in (16 N), SAVE and RESTORE copy it
+        (8 N each), INIT and ZERO_G write it (4 N each), LOSS reads the 2^n
+        diagonal entries.  PTMs, dP partials and their sums are
+        negligible."""
         total = 0
         for i, s in enumerate(self.specs):
-            n_ops = len(s.ops())
-            total += self.sizes[i] * (24 * n_ops + 16 * self.n_ckpt[i] + 8) \
+            n_units = len(self.units[i])
+            total += self.sizes[i] * (24 * n_units + 16 * self.n_ckpt[i] + 8) \
                 + 4 * 2 ** s.n
         return total
+
+    def _index_units(self):
+        """Flat index arrays of the units: slot and op of every one-qubit
+        unit; slot, C op, R_a op and R_b op (-1: none) of every two-qubit
+        unit."""
+        one_slot, one_op, two_slot, two_ops = [], [], [], []
+        for i, units in enumerate(self.units):
+            ub, ob = int(self.unit_base[i]), int(self.op_base[i])
+            for u, (_, qs, mem) in enumerate(units):
+                if len(qs) == 1:
+                    one_slot.append(ub + u)
+                    one_op.append(ob + mem[0])
+                else:
+                    two_slot.append(ub + u)
+                    two_ops.append([ob + m if m >= 0 else -1 for m in mem])
+        dev = self.device
+        as_idx = (lambda v: torch.as_tensor(np.asarray(v, dtype=np.int64),
+                                            device=dev))
+        self._one_slot, self._one_op = as_idx(one_slot), as_idx(one_op)
+        two = np.asarray(two_ops, dtype=np.int64).reshape(-1, 3)
+        self._two_slot = as_idx(two_slot)
+        self._two_c = as_idx(two[:, 0])
+        self._two_has = [two[:, 1] >= 0, two[:, 2] >= 0]
+        self._two_r = [as_idx(two[:, 1][two[:, 1] >= 0]),
+                       as_idx(two[:, 2][two[:, 2] >= 0])]
+        self._two_r_sel = [as_idx(np.nonzero(h)[0]) for h in self._two_has]
+        self._two_np = two
 
     # ------------------------------------------------------------ PTMs
     def set_ptms(self, ptms_per_instance):
         """ptms_per_instance[i][j]: (K, K) float64 PTM of op j of instance i
-        (any device).  Builds the FP32 pool of P and P^-1 on the GPU (the
-        inverses are computed on the host in FP64)."""
-        flat = [p.reshape(p.shape[0], -1) if p.dim() == 2 else
-                p.reshape(16, 16) for ps in ptms_per_instance for p in ps]
+        (two-qubit ones (16, 16) or (4, 4, 4, 4) in sorted qubit order; any
+        device).  Builds the units' PTMs (F = C (R_a (x) R_b) for fused
+        units) and their inverses in FP64 on the host, and stores them in
+        FP32 on the GPU; keeps C, R_a, R_b and R_a (x) R_b (FP64, GPU) for
+        mapping the gradients back."""
+        flat = [p.detach().to('cpu', torch.float64).reshape(
+                    (4, 4) if p.numel() == 16 else (16, 16))
+                for ps in ptms_per_instance for p in ps]
+        if len(flat) != self.n_ops:
+            raise ValueError('expected {} PTMs, got {}'.format(self.n_ops,
+                                                              len(flat)))
         dev = self.device
-        one = [k for k, p in enumerate(flat) if p.shape[0] == 4]
-        two = [k for k, p in enumerate(flat) if p.shape[0] == 16]
-        for idx, K in ((one, 4), (two, 16)):
-            if not idx:
+        eye4 = torch.eye(4, dtype=torch.float64)
+        one = torch.stack([flat[j] for j in self._one_op.tolist()]) \
+            if len(self._one_op) else torch.zeros(0, 4, 4,
+                                                  dtype=torch.float64)
+        two = self._two_np
+        if len(two):
+            c = torch.stack([flat[j] for j in two[:, 0]])
+            ra = torch.stack([flat[j] if j >= 0 else eye4 for j in two[:, 1]])
+            rb = torch.stack([flat[j] if j >= 0 else eye4 for j in two[:, 2]])
+            kr = torch.einsum('uac,ubd->uabcd', ra, rb).reshape(-1, 16, 16)
+            f = torch.bmm(c, kr)
+        else:
+            c = ra = rb = kr = f = torch.zeros(0, 16, 16, dtype=torch.float64)
+        for slots, m, K in ((self._one_slot, one, 4), (self._two_slot, f, 16)):
+            if not len(slots):
                 continue
             # inverted on the host in float64: the matrices are tiny, and
             # this keeps the device free of the solver libraries
-            m = torch.stack([flat[k].detach().to('cpu', torch.float64)
-                             for k in idx])
-            inv = torch.linalg.inv(m).to(dev)
-            m = m.to(dev)
-            pool = torch.zeros(len(idx), 256, dtype=torch.float64,
-                               device=dev)
+            inv = torch.linalg.inv(m)
+            pool = torch.zeros(len(slots), 256, dtype=torch.float64)
             ipool = torch.zeros_like(pool)
-            pool[:, :K * K] = m.reshape(len(idx), -1)
-            ipool[:, :K * K] = inv.reshape(len(idx), -1)
-            sel = torch.as_tensor(idx, device=dev)
-            self.ptm[sel] = pool.float()
-            self.ptm_inv[sel] = ipool.float()
+            pool[:, :K * K] = m.reshape(len(slots), -1)
+            ipool[:, :K * K] = inv.reshape(len(slots), -1)
+            self.ptm[slots] = pool.to(dev).float()
+            self.ptm_inv[slots] = ipool.to(dev).float()
+        self._factors = tuple(t.to(dev) for t in (c, ra, rb, kr))
+
+    def _map_gradients(self):
+        """dL/dP of every original op from the units' dL/dF (device, on the
+        current stream): one-qubit units copy; for F = C K with
+        K = R_a (x) R_b, dL/dC = G K^T and, with H = C^T G viewed as
+        [a', b', a, b], dL/dR_a = sum H R_b[b', b], dL/dR_b = sum H R_a[a', a]."""
+        og = self.op_grad
+        if len(self._one_slot):
+            og[self._one_op] = self.grad[self._one_slot]
+        if len(self._two_slot):
+            c, ra, rb, kr = self._factors
+            g = self.grad[self._two_slot].view(-1, 16, 16)
+            og[self._two_c] = torch.bmm(g, kr.transpose(1, 2)).reshape(-1, 256)
+            h = torch.bmm(c.transpose(1, 2), g).view(-1, 4, 4, 4, 4)
+            for side in (0, 1):
+                sel = self._two_r_sel[side]
+                if not len(sel):
+                    continue
+                hs = h[sel]
+                if side == 0:
+                    d = torch.einsum('uxyzw,uyw->uxz', hs, rb[sel])
+                else:
+                    d = torch.einsum('uxyzw,uxz->uyw', hs, ra[sel])
+                og[self._two_r[side], :16] = d.reshape(-1, 16)
 
     # ------------------------------------------------------------ run
     def _launch(self, grid):
@@ -342,19 +475,26 @@ class BatchedSimulator:
         L.check(st, 'qsgb_batch_run')
 
     def step(self, grid=None, use_graph=True):
-        """One forward + adjoint of every instance (asynchronous)."""
+        """One forward + adjoint of every instance, and the per-op gradients
+        (asynchronous)."""
+        if self._factors is None:
+            raise RuntimeError('set_ptms() before step()')
         grid = grid or self.max_grid
+
+        def run():
+            self._launch(grid)
+            self._map_gradients()
         if use_graph:
             if self.graph is None:
-                self._launch(grid)  # warm-up outside capture
+                run()  # warm-up outside capture
                 torch.cuda.synchronize(self.device)
                 g = torch.cuda.CUDAGraph()
                 with torch.cuda.graph(g):
-                    self._launch(grid)
+                    run()
                 self.graph = g
             self.graph.replay()
         else:
-            self._launch(grid)
+            run()
 
     def check(self):
         val = int(self.status.item())
@@ -369,11 +509,11 @@ class BatchedSimulator:
         probs = [self.prob[self.diag_off[i]:self.diag_off[i + 1]]
                  for i in range(self.n_inst)]
         grads = []
-        for i, s in enumerate(self.specs):
+        for i, ops in enumerate(self.ops):
             gi = []
-            for j, (_, qs) in enumerate(s.ops()):
+            for j, (_, qs) in enumerate(ops):
                 K = 4 if len(qs) == 1 else 16
-                gi.append(self.grad[int(self.op_base[i]) + j, :K * K]
+                gi.append(self.op_grad[int(self.op_base[i]) + j, :K * K]
                           .view(K, K))
             grads.append(gi)
         return probs, self.loss, grads
@@ -381,8 +521,8 @@ class BatchedSimulator:
     # ------------------------------------------------------------ autotune
     def _cache_key(self):
         sig = sorted(s.n for s in self.specs)
-        return '{}:{}:{}'.format(len(sig), sum(4 ** n for n in sig),
-                                 self.max_grid)
+        return '{}:{}:{}:{}'.format(len(sig), sum(4 ** n for n in sig),
+                                    self.max_grid, self.n_ptm)
 
     @staticmethod
     def _cache_path():
@@ -546,6 +686,12 @@ def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
         'f64_checked_instances': len(list(idx)),
         'tile': sim.tile, 'autotune_ms': tuned,
         'stages': sim.n_stages, 'items': sim.n_items,
+        'ops': sim.n_ops, 'units': sim.n_ptm,
+        'fusion': 'each CZ absorbs the rotations before it on its qubits '
+                  '(F = C (R_a x R_b)); per-op gradients mapped back in the '
+                  'same graph',
         'program_build_s': build_s,
         'launches_per_step': 1, 'cuda_graph': True,
+        'graph_contents': 'the persistent batch kernel, then batched-GEMM '
+                          'gradient mapping (torch) on the same stream',
     }

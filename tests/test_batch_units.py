@@ -1,0 +1,85 @@
+"""Host-side planning of the batched kernel's units (no GPU): a two-qubit op
+absorbs the one-qubit ops pending on its qubits within a layer.  Applying
+the units' PTMs F = C (R_a (x) R_b) with the oracle reproduces the ops
+applied one by one."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import pauli_vector_np as O
+from quantumsim_gb300 import batch as BT
+
+
+def _apply_ops(x, ops, mats):
+    for (l, qs), m in zip(ops, mats):
+        x = O.apply_ptm(x, m if len(qs) == 1 else m.reshape(4, 4, 4, 4),
+                        *sorted(qs))
+    return x
+
+
+@pytest.mark.parametrize('n,depth,seed', [(5, 4, 0), (6, 3, 1), (4, 5, 2),
+                                          (1, 2, 3), (2, 3, 4)])
+def test_units_reproduce_ops(n, depth, seed):
+    spec = BT.CircuitSpec(n, depth, seed)
+    ops = spec.ops()
+    mats = [p.numpy() for p in BT.instance_ptms(spec)]
+    # a generic (non-symmetric) two-qubit PTM exposes any ordering slip
+    rng = np.random.default_rng(seed)
+    mats = [m if m.shape == (4, 4) else rng.standard_normal((16, 16))
+            for m in mats]
+    units = BT.plan_units(ops)
+    # every op exactly once; layers contiguous and in order
+    used = sorted(j for _, _, mem in units for j in mem if j >= 0)
+    assert used == list(range(len(ops)))
+    layers = [l for l, _, _ in units]
+    assert layers == sorted(layers)
+    eye = np.eye(4)
+    unit_ops, unit_mats = [], []
+    for l, qs, mem in units:
+        if len(qs) == 1:
+            unit_ops.append((l, qs))
+            unit_mats.append(mats[mem[0]])
+        else:
+            assert qs[0] < qs[1]
+            ra = mats[mem[1]] if mem[1] >= 0 else eye
+            rb = mats[mem[2]] if mem[2] >= 0 else eye
+            unit_ops.append((l, qs))
+            unit_mats.append(mats[mem[0]] @ np.kron(ra, rb))
+    x = rng.standard_normal((4,) * n)
+    np.testing.assert_allclose(_apply_ops(x, unit_ops, unit_mats),
+                               _apply_ops(x, ops, mats), rtol=1e-12,
+                               atol=1e-12)
+    # unfused planning keeps one unit per op
+    assert [mem[0] for _, _, mem in BT.plan_units(ops, fuse=False)] == \
+        list(range(len(ops)))
+
+
+def test_units_fuse_most_one_qubit_ops():
+    """The line-matching circuits pair every qubit but one or two per layer:
+    about a third of the ops remain as units."""
+    spec = BT.CircuitSpec(12, 30, 0)
+    ops = spec.ops()
+    units = BT.plan_units(ops)
+    assert len(units) < 0.45 * len(ops)
+
+
+def test_gradient_mapping_matches_autograd():
+    """The rule step() applies to a fused unit's gradient: for F = C K with
+    K = R_a (x) R_b and any loss of F, dL/dC = G K^T and dL/dR_a, dL/dR_b
+    from H = C^T G, against torch autograd in float64."""
+    rng = np.random.default_rng(9)
+    c = torch.tensor(rng.standard_normal((16, 16)), requires_grad=True)
+    ra = torch.tensor(rng.standard_normal((4, 4)), requires_grad=True)
+    rb = torch.tensor(rng.standard_normal((4, 4)), requires_grad=True)
+    w = torch.tensor(rng.standard_normal((16, 16)))
+    f = c @ torch.kron(ra, rb)
+    loss = (w * f).sum() + (f ** 2).sum()
+    loss.backward()
+    g = (w + 2 * f).detach()
+    kr = torch.einsum('ac,bd->abcd', ra, rb).reshape(16, 16).detach()
+    np.testing.assert_allclose(g @ kr.T, c.grad, rtol=1e-12, atol=1e-12)
+    h = (c.detach().T @ g).view(4, 4, 4, 4)
+    np.testing.assert_allclose(torch.einsum('xyzw,yw->xz', h, rb.detach()),
+                               ra.grad, rtol=1e-12, atol=1e-11)
+    np.testing.assert_allclose(torch.einsum('xyzw,xz->yw', h, ra.detach()),
+                               rb.grad, rtol=1e-12, atol=1e-11)
