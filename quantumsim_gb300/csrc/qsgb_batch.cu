@@ -28,21 +28,23 @@ namespace {
 
 constexpr int kBatchBlock = 256;
 constexpr int kRedRows = kBatchBlock / 16;  // rows of the FP64 dP reduction buffer (>= warps)
-// floats per staged group in the adjoint tile: 16 values + 4 of padding, so
-// that 16-byte stores of consecutive lanes fall in distinct banks
-constexpr int kTileStride = 20;
+// floats per row of a warp's 16 x 32 adjoint tiles: 32 groups + 8 of
+// padding, so that the fragment loads and 8-byte stores of the two-qubit
+// ADJOINT fall in distinct banks
+constexpr int kAdjStride = 40;
+constexpr int kWarps = kBatchBlock / 32;
 
 struct BatchSmem {
   float P[256];
   float PT[256];  // P transposed (ADJOINT: g_in = P^T g_out)
   float Pi[256];
-  // adjoint tile: g_out and x_in per group, [group][kTileStride], one
-  // 32-group slice per warp; reused for the FP64 cross-warp sums of the dP
-  // partials
+  // two-qubit ADJOINT tiles, one pair per warp: x (X_out, then X_in) and g
+  // (G_out, then G_in), 16 rows of kAdjStride floats; reused for the FP64
+  // cross-warp sums of the dP partials
   union {
     struct {
-      float g[kBatchBlock][kTileStride];
-      float x[kBatchBlock][kTileStride];
+      float g[kWarps][16 * kAdjStride];
+      float x[kWarps][16 * kAdjStride];
     } t;
     double red[kRedRows][256];
   } u __attribute__((aligned(16)));
@@ -61,15 +63,6 @@ extern __shared__ __align__(16) unsigned char batch_dsm[];
 namespace {
 
 __device__ __forceinline__ BatchSmem& smem() { return *reinterpret_cast<BatchSmem*>(batch_dsm); }
-
-// A zero the compiler cannot see through: shared-memory loads indexed with it
-// are scheduled within the loop iteration that obtains it instead of being
-// hoisted out of the loop (which would hold a whole 16 x 16 PTM in registers).
-__device__ __forceinline__ int opaque_zero() {
-  int z;
-  asm volatile("mov.b32 %0, 0;" : "=r"(z));
-  return z;
-}
 
 __device__ __forceinline__ volatile uint32_t* vol(uint32_t* p) { return p; }
 
@@ -316,43 +309,98 @@ __device__ __noinline__ void adjoint1_vec(float* __restrict__ x, float* __restri
   __syncthreads();
 }
 
-// Two-qubit ADJOINT with independent warps: each warp takes tiles of 32
-// consecutive groups (lane = group), computes x_in = P^-1 x_out and
-// g_in = P^T g_out (rows of both as 16-byte shared loads), stages x_in and
-// g_out of its tile in its own slice of the shared tile (padded rows: no bank
-// conflicts), and after a __syncwarp each lane accumulates a 2 x 4 block of
-// dP over the tile's 32 groups.  When the pair includes the last qubit
-// (Z == 1) the inputs 4a .. 4a+3 of a group are contiguous and move as one
-// 16-byte access.  No block barrier inside the loop.
-// FP32 products are carried over 4 tiles, then folded into the thread's FP64
-// sums in shared memory;
-// at the end the warps' blocks are summed in a fixed order and written to
-// dst (256 doubles).
+// ---- warp-level tensor-core helpers (mma.sync m16n8k8, TF32 operands)
+// The FP32 value x is carried as hi + lo, both TF32 (cvt.rna keeps the top
+// 11 significant bits): hi = tf32(x), lo = tf32(x - hi).  A product is taken
+// as A_lo B_hi + A_hi B_lo + A_hi B_hi (the lo * lo term is below the
+// representation error of the split, ~2^-22 relative), accumulated in FP32.
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  hi = to_tf32(x);
+  lo = to_tf32(x - __uint_as_float(hi));
+}
+
+// d += a * b for one m16n8k8 tile: a = 16 x 8 (row-major fragment a0..a3),
+// b = 8 x 8 (column fragment b0, b1), d = 16 x 8 FP32
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// d += A B with A given as split fragments (ah, al) and B as FP32 values
+__device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4], float b0,
+                                     float b1) {
+  uint32_t bh0, bl0, bh1, bl1;
+  split_tf32(b0, bh0, bl0);
+  split_tf32(b1, bh1, bl1);
+  mma_tf32(d, al, bh0, bh1);
+  mma_tf32(d, ah, bl0, bl1);
+  mma_tf32(d, ah, bh0, bh1);
+}
+
+// Two-qubit ADJOINT on the warp-level tensor cores.  A warp takes tiles of 32
+// consecutive groups; lane l loads group t0 + l (coalesced across lanes) and
+// stages its x_out and g_out as column l of two 16 x 32 tiles in its own
+// slice of shared memory ([k][group], rows of kAdjStride floats).  Per tile:
+//   X_in = P^-1 X_out and G_in = P^T G_out   (M 16, N 32, K 16: 8 mma each)
+//   dP  += G_out X_in^T                      (M 16, N 16, K 32: 8 mma)
+// each mma in 3xTF32 (24 per product).  X_in and G_in go back through the
+// tiles ([r][group]) to the lanes that own the groups and to global memory.
+// The dP fragments are carried in FP32 over 4 tiles, then folded into the
+// thread's FP64 sums in shared memory; at the end the warps' sums are added
+// in a fixed order and written to dst (256 doubles).
 __device__ __noinline__ void adjoint2_warp(float* __restrict__ x, float* __restrict__ gv, const Geo& geo, int64_t beg,
-                              int64_t end, double* __restrict__ dst) {
+                                           int64_t end, double* __restrict__ dst) {
   constexpr int K = 16;
+  constexpr int S = kAdjStride;
   BatchSmem& sm = smem();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
-  // this warp's slice of the tile: x_in and g_out of 32 groups
-  float(*wx)[kTileStride] = &sm.u.t.x[warp * 32];
-  float(*wg)[kTileStride] = &sm.u.t.g[warp * 32];
-  const int r0 = 2 * (lane >> 2), c0 = 4 * (lane & 3);
+  const int gid = lane >> 2, tig = lane & 3;
+  float* ta = sm.u.t.x[warp];  // X_out, then X_in
+  float* tb = sm.u.t.g[warp];  // G_out, then G_in
   const bool vec = geo.lz == 0;
-  float s[8];
+  // A fragments of P^-1 and P^T (two k-steps each), split into TF32 hi / lo
+  uint32_t pih[2][4], pil[2][4], pth[2][4], ptl[2][4];
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks) {
+    const int c = 8 * ks + tig;
+    const float vi[4] = {sm.Pi[gid * K + c], sm.Pi[(gid + 8) * K + c], sm.Pi[gid * K + c + 4],
+                         sm.Pi[(gid + 8) * K + c + 4]};
+    const float vt[4] = {sm.PT[gid * K + c], sm.PT[(gid + 8) * K + c], sm.PT[gid * K + c + 4],
+                         sm.PT[(gid + 8) * K + c + 4]};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      split_tf32(vi[i], pih[ks][i], pil[ks][i]);
+      split_tf32(vt[i], pth[ks][i], ptl[ks][i]);
+    }
+  }
+  float dp[2][4];  // dP fragments: rows gid, gid + 8; columns 8 nb + 2 tig (+1)
+#pragma unroll
+  for (int nb = 0; nb < 2; ++nb)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dp[nb][i] = 0.f;
   double* acc = sm.acc[threadIdx.x];  // FP64 running sums in shared memory
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    s[i] = 0.f;
-    acc[i] = 0.0;
-  }
+  for (int i = 0; i < 8; ++i) acc[i] = 0.0;
   int tiles = 0;
   for (int64_t t0 = beg + (int64_t)warp * 32; t0 < end; t0 += (int64_t)nwarps * 32) {
     const int64_t gi = t0 + lane;
-    if (gi < end) {
-      const int64_t b = group_base(geo, gi);
+    const bool have = gi < end;
+    const int64_t b = have ? group_base(geo, gi) : 0;
+    {
       float xo[K], go[K];
-      if (vec) {
+      if (!have) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) xo[k] = go[k] = 0.f;
+      } else if (vec) {
 #pragma unroll
         for (int q = 0; q < K / 4; ++q) {
           const float4 u = *reinterpret_cast<const float4*>(x + b + in_offset<K>(geo, 4 * q));
@@ -367,82 +415,102 @@ __device__ __noinline__ void adjoint2_warp(float* __restrict__ x, float* __restr
           go[k] = gv[b + in_offset<K>(geo, k)];
         }
       }
-      const int z0 = opaque_zero();
-      const float4* pi4 = reinterpret_cast<const float4*>(sm.Pi) + z0;
-      const float4* pt4 = reinterpret_cast<const float4*>(sm.PT) + z0;
 #pragma unroll
-      for (int rq = 0; rq < K / 4; ++rq) {
-        float a[4], c[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int r = 4 * rq + i;
-          float u = 0.f, w = 0.f;
-#pragma unroll
-          for (int q = 0; q < K / 4; ++q) {
-            const float4 pi = pi4[r * 4 + q], pt = pt4[r * 4 + q];
-            u = fmaf(pi.x, xo[4 * q], u);
-            u = fmaf(pi.y, xo[4 * q + 1], u);
-            u = fmaf(pi.z, xo[4 * q + 2], u);
-            u = fmaf(pi.w, xo[4 * q + 3], u);
-            w = fmaf(pt.x, go[4 * q], w);
-            w = fmaf(pt.y, go[4 * q + 1], w);
-            w = fmaf(pt.z, go[4 * q + 2], w);
-            w = fmaf(pt.w, go[4 * q + 3], w);
-          }
-          a[i] = u;
-          c[i] = w;
-        }
-        if (vec) {
-          *reinterpret_cast<float4*>(x + b + in_offset<K>(geo, 4 * rq)) = make_float4(a[0], a[1], a[2], a[3]);
-          *reinterpret_cast<float4*>(gv + b + in_offset<K>(geo, 4 * rq)) = make_float4(c[0], c[1], c[2], c[3]);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            x[b + in_offset<K>(geo, 4 * rq + i)] = a[i];
-            gv[b + in_offset<K>(geo, 4 * rq + i)] = c[i];
-          }
-        }
-        *reinterpret_cast<float4*>(&wx[lane][4 * rq]) = make_float4(a[0], a[1], a[2], a[3]);
-        *reinterpret_cast<float4*>(&wg[lane][4 * rq]) =
-            make_float4(go[4 * rq], go[4 * rq + 1], go[4 * rq + 2], go[4 * rq + 3]);
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < K; k += 4) {
-        *reinterpret_cast<float4*>(&wx[lane][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
-        *reinterpret_cast<float4*>(&wg[lane][k]) = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 0; k < K; ++k) {
+        ta[k * S + lane] = xo[k];
+        tb[k * S + lane] = go[k];
       }
     }
     __syncwarp();
-#pragma unroll 4
-    for (int g = 0; g < 32; ++g) {
-      const float2 a = *reinterpret_cast<const float2*>(&wg[g][r0]);
-      const float4 c = *reinterpret_cast<const float4*>(&wx[g][c0]);
-      s[0] = fmaf(a.x, c.x, s[0]);
-      s[1] = fmaf(a.x, c.y, s[1]);
-      s[2] = fmaf(a.x, c.z, s[2]);
-      s[3] = fmaf(a.x, c.w, s[3]);
-      s[4] = fmaf(a.y, c.x, s[4]);
-      s[5] = fmaf(a.y, c.y, s[5]);
-      s[6] = fmaf(a.y, c.z, s[6]);
-      s[7] = fmaf(a.y, c.w, s[7]);
+    // X_in = P^-1 X_out, G_in = P^T G_out: four n-tiles of 8 groups
+    float xi[4][4], gn[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) xi[nt][i] = gn[nt][i] = 0.f;
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks) {
+        const int r0 = (8 * ks + tig) * S + 8 * nt + gid;
+        mma3(xi[nt], pih[ks], pil[ks], ta[r0], ta[r0 + 4 * S]);
+        mma3(gn[nt], pth[ks], ptl[ks], tb[r0], tb[r0 + 4 * S]);
+      }
+    }
+    // dP A fragments: G_out[r][group] for the four k-steps over groups
+    float ga[4][4];
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const int c = 8 * ks + tig;
+      ga[ks][0] = tb[gid * S + c];
+      ga[ks][1] = tb[(gid + 8) * S + c];
+      ga[ks][2] = tb[gid * S + c + 4];
+      ga[ks][3] = tb[(gid + 8) * S + c + 4];
+    }
+    __syncwarp();
+    // X_in and G_in into the tiles as [r][group]
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const int c = 8 * nt + 2 * tig;
+      *reinterpret_cast<float2*>(&ta[gid * S + c]) = make_float2(xi[nt][0], xi[nt][1]);
+      *reinterpret_cast<float2*>(&ta[(gid + 8) * S + c]) = make_float2(xi[nt][2], xi[nt][3]);
+      *reinterpret_cast<float2*>(&tb[gid * S + c]) = make_float2(gn[nt][0], gn[nt][1]);
+      *reinterpret_cast<float2*>(&tb[(gid + 8) * S + c]) = make_float2(gn[nt][2], gn[nt][3]);
+    }
+    __syncwarp();
+    // this lane's group back to global memory
+    if (have) {
+      if (vec) {
+#pragma unroll
+        for (int q = 0; q < K / 4; ++q) {
+          *reinterpret_cast<float4*>(x + b + in_offset<K>(geo, 4 * q)) =
+              make_float4(ta[(4 * q) * S + lane], ta[(4 * q + 1) * S + lane], ta[(4 * q + 2) * S + lane],
+                          ta[(4 * q + 3) * S + lane]);
+          *reinterpret_cast<float4*>(gv + b + in_offset<K>(geo, 4 * q)) =
+              make_float4(tb[(4 * q) * S + lane], tb[(4 * q + 1) * S + lane], tb[(4 * q + 2) * S + lane],
+                          tb[(4 * q + 3) * S + lane]);
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+          x[b + in_offset<K>(geo, r)] = ta[r * S + lane];
+          gv[b + in_offset<K>(geo, r)] = tb[r * S + lane];
+        }
+      }
+    }
+    // dP += G_out X_in^T: B[group][k] = X_in[k][group]
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      uint32_t ah[4], al[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) split_tf32(ga[ks][i], ah[i], al[i]);
+#pragma unroll
+      for (int nb = 0; nb < 2; ++nb) {
+        const int r0 = (8 * nb + gid) * S + 8 * ks + tig;
+        mma3(dp[nb], ah, al, ta[r0], ta[r0 + 4]);
+      }
     }
     __syncwarp();
     if ((++tiles & 3) == 0) {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        acc[i] += (double)s[i];
-        s[i] = 0.f;
-      }
+      for (int nb = 0; nb < 2; ++nb)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          acc[nb * 4 + i] += (double)dp[nb][i];
+          dp[nb][i] = 0.f;
+        }
     }
   }
 #pragma unroll
-  for (int i = 0; i < 8; ++i) acc[i] += (double)s[i];
+  for (int nb = 0; nb < 2; ++nb)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[nb * 4 + i] += (double)dp[nb][i];
   __syncthreads();  // every warp is done with the tile: reuse it for the sums
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int nb = 0; nb < 2; ++nb)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) sm.u.red[warp][(r0 + i) * 16 + c0 + j] = acc[i * 4 + j];
+    for (int i = 0; i < 4; ++i) {
+      const int r = gid + 8 * (i >> 1), k = 8 * nb + 2 * tig + (i & 1);
+      sm.u.red[warp][r * 16 + k] = acc[nb * 4 + i];
+    }
   __syncthreads();
   for (int e = threadIdx.x; e < K * K; e += blockDim.x) {
     double t = 0.0;
