@@ -83,3 +83,39 @@ def test_gradient_mapping_matches_autograd():
                                ra.grad, rtol=1e-12, atol=1e-11)
     np.testing.assert_allclose(torch.einsum('xyzw,xz->yw', h, ra.detach()),
                                rb.grad, rtol=1e-12, atol=1e-11)
+
+
+@pytest.mark.parametrize('seed', range(6))
+def test_units_reproduce_random_op_sequences(seed):
+    """Random layers of one- and two-qubit ops in any order: rotations after
+    a CZ, two CZs sharing a qubit, several rotations on one qubit, pairs in
+    either qubit order.  Applying the units equals applying the ops."""
+    rng = np.random.default_rng(100 + seed)
+    n = int(rng.integers(2, 6))
+    ops, mats = [], []
+    for layer in range(int(rng.integers(1, 4))):
+        for _ in range(int(rng.integers(1, 9))):
+            if rng.random() < 0.5:
+                ops.append((layer, (int(rng.integers(n)),)))
+                mats.append(rng.standard_normal((4, 4)))
+            else:
+                a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+                ops.append((layer, (a, b)))
+                mats.append(rng.standard_normal((16, 16)))
+    units = BT.plan_units(ops)
+    used = sorted(j for _, _, mem in units for j in mem if j >= 0)
+    assert used == list(range(len(ops)))
+    eye = np.eye(4)
+    unit_ops, unit_mats = [], []
+    for l, qs, mem in units:
+        unit_ops.append((l, qs))
+        if len(qs) == 1:
+            unit_mats.append(mats[mem[0]])
+        else:
+            ra = mats[mem[1]] if mem[1] >= 0 else eye
+            rb = mats[mem[2]] if mem[2] >= 0 else eye
+            unit_mats.append(mats[mem[0]] @ np.kron(ra, rb))
+    x = rng.standard_normal((4,) * n)
+    np.testing.assert_allclose(_apply_ops(x, unit_ops, unit_mats),
+                               _apply_ops(x, ops, mats), rtol=1e-11,
+                               atol=1e-11)
