@@ -137,3 +137,30 @@ def test_grid_barrier_wait_expires_and_context_survives():
     for a, b in zip(probs0, probs1):
         assert torch.equal(a, b)
     assert torch.equal(loss0, loss1)
+
+
+def test_fused_units_match_unfused_program():
+    """Units (a CZ absorbing the rotations before it) against one unit per
+    op: the same probabilities, losses and per-op gradients up to the FP32
+    rounding of the different products."""
+    ns = [5, 3, 6, 4]
+    specs, targets, ptms = _setup(ns, depth=6, every=2, seed=31)
+    out = []
+    for fuse in (True, False):
+        sim = BT.BatchedSimulator(specs, targets, checkpoint_every=2,
+                                  tile=128, fuse=fuse)
+        sim.set_ptms(ptms)
+        sim.step(use_graph=True)
+        torch.cuda.synchronize()
+        p, l, g = sim.results()
+        out.append(([t.clone() for t in p], l.clone(),
+                    [[t.clone() for t in gi] for gi in g], sim.n_ptm))
+    (pf, lf, gf, nf), (pu, lu, gu, nu) = out
+    assert nf < nu
+    for a, b in zip(pf, pu):
+        assert float((a - b).abs().max()) < 1e-6
+    np.testing.assert_allclose(lf.cpu(), lu.cpu(), rtol=1e-4, atol=1e-8)
+    for gi_f, gi_u in zip(gf, gu):
+        scale = max(float(t.abs().max()) for t in gi_u)
+        for a, b in zip(gi_f, gi_u):
+            assert float((a - b).abs().max()) < 1e-4 * scale
