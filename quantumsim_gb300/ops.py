@@ -100,7 +100,22 @@ def check_device_status(device):
     """Raise if a kernel reported a device-side problem since the last check
     (synchronises the device's current stream)."""
     st = status_tensor(device)
-    val = int(st.item())
+    _raise_status(st, int(st.item()))
+
+
+def fetch_checked(t):
+    """Host (numpy, float64) copy of the small device tensor `t`, read in the
+    same device-to-host copy as the status word: one synchronisation where
+    ``check_device_status`` followed by a read takes two.  Raises like
+    ``check_device_status``."""
+    st = status_tensor(t.device)
+    both = torch.cat([t.reshape(-1).to(torch.float64),
+                      st.to(torch.float64)]).cpu().numpy()
+    _raise_status(st, int(both[-1]))
+    return both[:-1]
+
+
+def _raise_status(st, val):
     if val:
         st.zero_()
         reasons = []

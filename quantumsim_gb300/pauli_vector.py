@@ -315,28 +315,23 @@ class PauliVectorGB300(_Base):
             view = target_array.reshape(-1)[:n]
             view.copy_(diag)
             diag = view
-        if not flatten:
-            diag = diag.reshape(tuple(self.dim_hilbert))
         if not get_data:
-            return diag
-        ops.check_device_status(self._device)
-        return diag.cpu().numpy()
+            return diag if flatten else diag.reshape(tuple(self.dim_hilbert))
+        out = ops.fetch_checked(diag)
+        return out if flatten else out.reshape(tuple(self.dim_hilbert))
 
     def _trace_device(self):
         diag = self._diagonal_device()
         return torch.ops.qsgb.marginals(diag, [diag.numel()], -1)
 
     def trace(self):
-        tr = self._trace_device()
-        ops.check_device_status(self._device)
-        return float(tr.item())
+        return float(ops.fetch_checked(self._trace_device())[0])
 
     def meas_prob(self, qubit):
         self._validate_qubit(qubit, 'qubit')
         diag = self._diagonal_device()
         probs = torch.ops.qsgb.marginals(diag, list(self.dim_hilbert), qubit)
-        ops.check_device_status(self._device)
-        return probs.cpu().numpy()
+        return ops.fetch_checked(probs)
 
     def partial_trace(self, *qubits):
         for q in qubits:
@@ -398,8 +393,7 @@ class PauliVectorGB300(_Base):
             w = np.einsum('ab,kba->k', s, np.asarray(b.vectors))
             weights.extend(float(v) for v in np.real(w))
         out = torch.ops.qsgb.partial_trace(self._data, [0] * n, weights)
-        ops.check_device_status(self._device)
-        return float(out.item())
+        return float(ops.fetch_checked(out)[0])
 
     def reduce_basis(self, qubit, indices):
         """Keep only the Pauli elements `indices` of `qubit`'s basis
