@@ -13,7 +13,11 @@
 // are invertible and well conditioned), while the adjoint state moves back
 // through P^T; the host refreshes the state from checkpoints every few
 // layers.  One ADJOINT item therefore reads x_out and g_out once, writes x_in
-// and g_in, and accumulates its share of dL/dP = sum g_out (x) x_in.
+// and g_in, and accumulates its share of dL/dP = sum g_out (x) x_in.  The
+// two-qubit ADJOINT does its three small products per 32-group warp tile on
+// the warp-level tensor cores (mma.sync m16n8k8, TF32 operands split hi/lo);
+// every other body runs on the FP32 pipes.  An op here is whatever the host
+// planned as a unit (a CZ may carry the rotations before it).
 //
 // Every grid barrier polls a bounded number of times; on expiry the kernel
 // flags QSGB_DEV_TIMEOUT and all blocks return.
