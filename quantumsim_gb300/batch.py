@@ -136,6 +136,24 @@ def target_probabilities(spec, seed):
     return diagonal_diff(x, [_bases.general(2)] * spec.n).detach()
 
 
+def validate_ops(ops, n, depth, what='circuit'):
+    """Raise ValueError unless every op acts on one qubit or two distinct
+    qubits in [0, n) and the layers are non-decreasing within [0, depth)."""
+    prev = 0
+    for j, (layer, qs) in enumerate(ops):
+        qs = tuple(qs)
+        if len(qs) not in (1, 2) or any(
+                not (isinstance(q, (int, np.integer)) and 0 <= q < n)
+                for q in qs) or len(set(qs)) != len(qs):
+            raise ValueError('{}: op {} acts on {}; ops take one qubit or two '
+                             'distinct qubits in [0, {})'.format(what, j, qs,
+                                                                  n))
+        if not 0 <= layer < depth or layer < prev:
+            raise ValueError('{}: op {} has layer {}; layers run in order '
+                             'within [0, {})'.format(what, j, layer, depth))
+        prev = layer
+
+
 def plan_units(ops, fuse=True):
     """Group a circuit's ops into the units the kernel applies.
 
@@ -191,6 +209,14 @@ class BatchedSimulator:
 
     def __init__(self, specs, targets, checkpoint_every=8, tile=None,
                  device=None, cooperative=True, fuse=True):
+        # ---- structure checks, before anything reaches the device: the
+        # kernel's group geometry assumes valid, distinct target qubits
+        if any(not 1 <= s.n <= 15 for s in specs):
+            raise ValueError('batched instances have 1 to 15 qubits')
+        if checkpoint_every < 1:
+            raise ValueError('checkpoint_every must be at least 1')
+        for i, s in enumerate(specs):
+            validate_ops(s.ops(), s.n, s.depth, 'instance {}'.format(i))
         self.lib = L.load()
         self.device = torch.device(device or 'cuda')
         self.specs = specs
@@ -199,8 +225,6 @@ class BatchedSimulator:
         self.n_inst = len(specs)
         dev = self.device
         # ---- per-instance buffers
-        if any(not 1 <= s.n <= 15 for s in specs):
-            raise ValueError('batched instances have 1 to 15 qubits')
         self.sizes = [4 ** s.n for s in specs]
         self.n_ckpt = [max(0, (s.depth - 1) // checkpoint_every)
                        for s in specs]

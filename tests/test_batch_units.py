@@ -119,3 +119,22 @@ def test_units_reproduce_random_op_sequences(seed):
     np.testing.assert_allclose(_apply_ops(x, unit_ops, unit_mats),
                                _apply_ops(x, ops, mats), rtol=1e-11,
                                atol=1e-11)
+
+
+@pytest.mark.parametrize('ops,msg', [
+    ([(0, (5,))], 'acts on'),                 # qubit out of range
+    ([(0, (-1,))], 'acts on'),
+    ([(0, (2, 2))], 'acts on'),               # repeated qubit
+    ([(0, (0, 1, 2))], 'acts on'),            # three qubits
+    ([(1, (0,)), (0, (1,))], 'layer'),        # layers out of order
+    ([(7, (0,))], 'layer'),                   # layer past the depth
+])
+def test_malformed_structures_are_rejected_on_the_host(ops, msg):
+    """Bad target qubits or layers raise ValueError before any device
+    memory is touched (the kernel's group geometry assumes valid targets)."""
+    spec = BT.CircuitSpec(4, 3, 0)
+    spec.ops = lambda o=ops: o
+    with pytest.raises(ValueError, match=msg):
+        BT.BatchedSimulator([spec], [torch.ones(16) / 16], device='cpu')
+    # the valid structure passes the check
+    BT.validate_ops(BT.CircuitSpec(4, 3, 0).ops(), 4, 3)
