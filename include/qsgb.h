@@ -35,7 +35,9 @@ extern "C" {
 /* ---- device status bits (written into *dev_status) ---- */
 #define QSGB_DEV_RANGE 1u      /* df64 arithmetic saw |x| >= 2^128, inf or nan */
 #define QSGB_DEV_TIMEOUT 2u    /* a bounded device-side wait gave up */
-#define QSGB_DEV_BADITEM 4u    /* batched work queue met a malformed item */
+#define QSGB_DEV_BADITEM 4u    /* batched work queue met a malformed item
+                                  (unknown op, targets outside its instance,
+                                  range past its vector); it was skipped */
 
 /* ---- storage element types ---- */
 #define QSGB_F64 0
@@ -276,7 +278,8 @@ typedef struct {
 
 typedef struct {
   int32_t op;         /* QSGB_BOP_* */
-  int32_t inst;       /* instance index */
+  int32_t inst;       /* instance index, below the number of instances (the
+                         device cannot check it: the program carries no count) */
   int32_t q0, q1;     /* target qubits, q0 < q1; q1 = -1 for one qubit */
   int32_t ptm;        /* PTM index (APPLY/ADJOINT/GRADSUM) or checkpoint slot */
   int32_t slot;       /* gradient partial slot (ADJOINT) */

@@ -555,6 +555,29 @@ __device__ __noinline__ void loss_item(const qsgb_batch_program& p, const qsgb_b
   __syncthreads();
 }
 
+// An item's fields against its instance: a known op, targets inside the
+// instance (two distinct, ordered qubits for two-qubit ops), ranges inside
+// the vector (in groups for APPLY / ADJOINT), a non-negative PTM or
+// checkpoint index.  Malformed items are skipped and reported as
+// QSGB_DEV_BADITEM instead of being allowed to address memory they do not
+// own.  (The instance index itself is trusted: the program does not carry
+// the instance count.)
+__device__ __forceinline__ bool item_ok(const qsgb_batch_program& p, const qsgb_batch_item& it) {
+  if (it.op < QSGB_BOP_INIT || it.op > QSGB_BOP_GRADSUM || it.inst < 0) return false;
+  if (it.op == QSGB_BOP_GRADSUM) return it.beg >= 0 && it.end >= it.beg && it.ptm >= 0;
+  const qsgb_batch_instance in = p.instances[it.inst];
+  const int n = in.n_qubits;
+  if (n < 1 || n > 15 || in.size != (1ll << (2 * n))) return false;
+  if (it.op == QSGB_BOP_LOSS) return true;
+  if (it.beg < 0 || it.ptm < 0) return false;
+  if (it.op == QSGB_BOP_APPLY || it.op == QSGB_BOP_ADJOINT) {
+    if (it.q0 < 0 || it.q0 >= n) return false;
+    if (it.q1 >= 0 && (it.q1 <= it.q0 || it.q1 >= n)) return false;
+    return it.end <= (in.size >> (it.q1 < 0 ? 2 : 4));
+  }
+  return it.end <= in.size;
+}
+
 __device__ void process(const qsgb_batch_program& p, const qsgb_batch_item& it, BatchSmem& sm) {
   const qsgb_batch_instance in = p.instances[it.inst];
   switch (it.op) {
@@ -632,7 +655,7 @@ __global__ void __launch_bounds__(kBatchBlock, 2) batch_kernel(const __grid_cons
       const int i = sm.item;
       if (i >= end) break;
       const qsgb_batch_item it = p.items[i];
-      if (it.op < QSGB_BOP_INIT || it.op > QSGB_BOP_GRADSUM || it.inst < 0) {
+      if (!item_ok(p, it)) {
         if (threadIdx.x == 0 && status) atomicOr(status, QSGB_DEV_BADITEM);
         continue;
       }
