@@ -278,8 +278,7 @@ typedef struct {
 
 typedef struct {
   int32_t op;         /* QSGB_BOP_* */
-  int32_t inst;       /* instance index, below the number of instances (the
-                         device cannot check it: the program carries no count) */
+  int32_t inst;       /* instance index, below the program's n_instances */
   int32_t q0, q1;     /* target qubits, q0 < q1; q1 = -1 for one qubit */
   int32_t ptm;        /* PTM index (APPLY/ADJOINT/GRADSUM) or checkpoint slot */
   int32_t slot;       /* gradient partial slot (ADJOINT) */
@@ -291,6 +290,8 @@ typedef struct {
   const qsgb_batch_item* items;         /* device */
   const int32_t* stage_begin;           /* device, n_stages + 1 item offsets */
   int32_t n_stages;
+  int32_t n_instances;     /* entries of `instances`; items must index below it
+                              (ABI version 2; fills what was padding) */
   uint32_t* work;          /* device, n_stages + 3 words, ZERO before each run */
   const float* ptm;        /* device, n_ptm x 256: P (sorted qubit order,
                               row-major out x in; 4x4 in the first 16) */

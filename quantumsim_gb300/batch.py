@@ -63,7 +63,7 @@ class _Instance(ctypes.Structure):
 class _Program(ctypes.Structure):
     _fields_ = [('instances', ctypes.c_void_p), ('items', ctypes.c_void_p),
                 ('stage_begin', ctypes.c_void_p), ('n_stages', ctypes.c_int32),
-                ('work', ctypes.c_void_p), ('ptm', ctypes.c_void_p),
+                ('n_instances', ctypes.c_int32), ('work', ctypes.c_void_p), ('ptm', ctypes.c_void_p),
                 ('ptm_inv', ctypes.c_void_p),
                 ('grad_partial', ctypes.c_void_p), ('grad', ctypes.c_void_p),
                 ('target', ctypes.c_void_p), ('prob', ctypes.c_void_p),
@@ -368,6 +368,7 @@ class BatchedSimulator:
         prog.items = self.items_dev.data_ptr()
         prog.stage_begin = self.stage_dev.data_ptr()
         prog.n_stages = self.n_stages
+        prog.n_instances = self.n_inst
         prog.work = self.work.data_ptr()
         prog.ptm = self.ptm.data_ptr()
         prog.ptm_inv = self.ptm_inv.data_ptr()

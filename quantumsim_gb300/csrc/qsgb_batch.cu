@@ -558,12 +558,11 @@ __device__ __noinline__ void loss_item(const qsgb_batch_program& p, const qsgb_b
 // An item's fields against its instance: a known op, targets inside the
 // instance (two distinct, ordered qubits for two-qubit ops), ranges inside
 // the vector (in groups for APPLY / ADJOINT), a non-negative PTM or
-// checkpoint index.  Malformed items are skipped and reported as
-// QSGB_DEV_BADITEM instead of being allowed to address memory they do not
-// own.  (The instance index itself is trusted: the program does not carry
-// the instance count.)
+// checkpoint index, an instance below the program's count.  Malformed items
+// are skipped and reported as QSGB_DEV_BADITEM instead of being allowed to
+// address memory they do not own.
 __device__ __forceinline__ bool item_ok(const qsgb_batch_program& p, const qsgb_batch_item& it) {
-  if (it.op < QSGB_BOP_INIT || it.op > QSGB_BOP_GRADSUM || it.inst < 0) return false;
+  if (it.op < QSGB_BOP_INIT || it.op > QSGB_BOP_GRADSUM || it.inst < 0 || it.inst >= p.n_instances) return false;
   if (it.op == QSGB_BOP_GRADSUM) return it.beg >= 0 && it.end >= it.beg && it.ptm >= 0;
   const qsgb_batch_instance in = p.instances[it.inst];
   const int n = in.n_qubits;
@@ -693,7 +692,8 @@ extern "C" int qsgb_batch_run(const qsgb_batch_program* prog, int grid, int bloc
                               unsigned* dev_status, int64_t spin_limit, void* stream) {
   if (!prog || !prog->instances || !prog->items || !prog->stage_begin || !prog->work || !prog->ptm)
     return QSGB_ERR_INVALID;
-  if (block != qsgb::kBatchBlock || grid < 1 || prog->n_stages < 1 || spin_limit < 1) return QSGB_ERR_INVALID;
+  if (block != qsgb::kBatchBlock || grid < 1 || prog->n_stages < 1 || prog->n_instances < 1 || spin_limit < 1)
+    return QSGB_ERR_INVALID;
   const int maxg = qsgb_batch_max_grid(block);
   if (maxg < 1) return QSGB_ERR_CUDA;
   if (grid > maxg) return QSGB_ERR_INVALID;  // every block must be resident for the barriers

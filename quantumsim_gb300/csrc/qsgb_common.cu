@@ -24,7 +24,7 @@ int launch_status() {
 
 }  // namespace qsgb
 
-extern "C" int qsgb_abi_version(void) { return 1; }
+extern "C" int qsgb_abi_version(void) { return 2; }
 
 extern "C" const char* qsgb_status_string(int status) {
   switch (status) {

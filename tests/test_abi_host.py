@@ -43,7 +43,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.qsgb_abi_version() >= 1
+    assert lib.qsgb_abi_version() >= 2
     assert lib.qsgb_jit_available() in (0, 1)
     assert lib.qsgb_status_string(0) == b'ok'
     assert b'invalid' in lib.qsgb_status_string(1)
@@ -174,3 +174,15 @@ def test_registered_into_reference_namespace_when_available():
     assert qpv.PauliVectorGB300 is qg.PauliVectorGB300
     from quantumsim.pauli_vectors.pauli_vector import PauliVectorBase
     assert issubclass(qg.PauliVectorGB300, PauliVectorBase)
+
+
+def test_batch_program_layout_matches_the_header():
+    """The ctypes mirror of qsgb_batch_program follows C layout rules on
+    64-bit hosts: n_instances (ABI 2) sits in what was the padding after
+    n_stages, so the pointer fields keep their offsets."""
+    from quantumsim_gb300 import batch as BT
+    P = BT._Program
+    assert P.n_stages.offset == 24 and P.n_instances.offset == 28
+    assert P.work.offset == 32 and ctypes.sizeof(P) == 96
+    assert ctypes.sizeof(BT._Instance) == 40
+    assert BT._ITEM_DTYPE.itemsize == 40

@@ -164,3 +164,40 @@ def test_fused_units_match_unfused_program():
         scale = max(float(t.abs().max()) for t in gi_u)
         for a, b in zip(gi_f, gi_u):
             assert float((a - b).abs().max()) < 1e-4 * scale
+
+
+@pytest.mark.parametrize('field,value', [('inst', None), ('q1', 'q0'),
+                                         ('end', 'past')])
+def test_malformed_items_are_skipped_and_reported(field, value):
+    """The kernel checks every item against its instance before touching
+    memory: an instance index at the count, a second target equal to the
+    first, a range past the vector.  Each is skipped with QSGB_DEV_BADITEM,
+    and the context then gives the same results as before."""
+    from quantumsim_gb300 import _lib as L
+
+    specs, targets, ptms = _setup([4, 5], depth=2, every=2, seed=41)
+    sim = BT.BatchedSimulator(specs, targets, checkpoint_every=2, tile=64)
+    sim.set_ptms(ptms)
+    sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    p0 = [p.clone() for p in sim.results()[0]]
+    good = sim.items_dev.clone()
+    items = good.cpu().numpy().view(BT._ITEM_DTYPE).copy()
+    j = int(np.nonzero((items['op'] == BT.BOP_APPLY) & (items['q1'] >= 0))[0][0])
+    if field == 'inst':
+        items['inst'][j] = sim.n_inst
+    elif field == 'q1':
+        items['q1'][j] = items['q0'][j]
+    else:
+        items['end'][j] = items['end'][j] + 4 ** 8
+    sim.items_dev.copy_(torch.from_numpy(items.view(np.uint8).copy()))
+    sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    assert int(sim.status.item()) & L.DEV_BADITEM
+    with pytest.raises(RuntimeError, match='device status'):
+        sim.check()
+    sim.items_dev.copy_(good)
+    sim.step(use_graph=False)
+    torch.cuda.synchronize()
+    for a, b in zip(p0, sim.results()[0]):
+        assert torch.equal(a, b)
