@@ -726,13 +726,15 @@ int Spec::n_coef() const {
 // How many inputs the generated loads run ahead of their first use.  Items
 // of up to 36 values (16x16 pairs, 9x9) load everything first and compute
 // rows in natural order; larger ones (81x81) go component by component with
-// loads 8 inputs ahead, which keeps them near 80 registers instead of 255.
-// Measured on GB300 (GB/s, 14 qubits / 8 qutrits): everything first gives
-// noisy CZ 6354 and 81x81 on (2, 5) 2477; components with lookahead 8 give
-// 6326 and 4863; lookahead 16 to 255 lose up to 18 % on the CZ pair kernel.
-// On the 81x81 leakage CZ on (2, 5) of 8 qutrits, lookahead 8 / 12 / 16 /
-// 24 / 32 / 81 gave 4972 / 4405 / 4871 / 4728 / 3262 / 2812 GB/s.
-int lookahead_for(int kin, bool pair) { return kin * (pair ? 2 : 1) <= 36 ? kin : 8; }
+// loads a few inputs ahead, which keeps them near 80-100 registers instead
+// of 255.  Measured on GB300 (GB/s, 14 qubits / 8 qutrits): everything first
+// gives noisy CZ 6354 and 81x81 on (2, 5) 2477; components with lookahead 8
+// give 6326 and 4863; lookahead 16 to 255 lose up to 18 % on the CZ pair
+// kernel.  On the 81x81 leakage CZ of 8 qutrits ((2, 5), (0, 1), (3, 4)),
+// lookahead 4 / 6 / 8 / 9 / 10 / 11 / 12 / 16 / 32 / 81 gave about
+// 4400 / 4830 / 5000 / 5190 / 5230 / 5250 / 4400 / 4870 / 3260 / 2810 GB/s:
+// 9 to 11 is a plateau before a cliff at 12.
+int lookahead_for(int kin, bool pair) { return kin * (pair ? 2 : 1) <= 36 ? kin : 10; }
 
 bool make_spec(const double* ptm_host, int da_out, int db_out, int da_in, int db_in, int layout, int dtype,
                int arith, bool pair, bool z1, bool contiguous, int vin, int vout, Spec& spec,
