@@ -199,6 +199,90 @@ def plan_units(ops, fuse=True):
     return units
 
 
+def build_program(units, unit_base, sizes, depths, every, tile,
+                  max_items=64):
+    """Host part of the device program, in numpy: (items, stage_begin,
+    n_slots).
+
+    Every unit is one stage entry per instance; an entry covering `total`
+    groups (or elements) becomes ceil(total / chunk) items with chunk =
+    max(tile, ceil(total / max_items)) -- large ops are shared by many
+    blocks, and no op has more than `max_items` items.  `tile` is a multiple
+    of 4: the kernel takes 4 consecutive groups along z per access, and an
+    item boundary must not split them.  Stages per instance: INIT, APPLY of
+    every unit (SAVE after every `every`-th layer), ZERO_G, LOSS, ADJOINT of
+    the units in reverse (RESTORE at the saved layers); a last stage holds
+    one GRADSUM item per unit over the dP slots of its ADJOINT items."""
+    if tile < 4 or tile % 4:
+        raise ValueError('tile must be a positive multiple of 4')
+    ent = []  # (stage, op, inst, q0, q1, ptm or checkpoint, total)
+    for i, (unit_list, size, depth) in enumerate(zip(units, sizes, depths)):
+        ops = [(l, qs) for l, qs, _ in unit_list]
+        layer_of = [l for l, _ in ops]
+        seq = [(BOP_INIT, -1, -1, 0, size)]
+        for j, (l, qs) in enumerate(ops):
+            pidx = int(unit_base[i]) + j
+            q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
+            seq.append((BOP_APPLY, q0, q1, pidx,
+                        size // (4 if q1 < 0 else 16)))
+            last_of_layer = j + 1 == len(ops) or layer_of[j + 1] != l
+            if last_of_layer and (l + 1) % every == 0 and l + 1 < depth:
+                seq.append((BOP_SAVE, -1, -1, (l + 1) // every - 1, size))
+        seq.append((BOP_ZERO_G, -1, -1, 0, size))
+        seq.append((BOP_LOSS, -1, -1, 0, 1))
+        for j in reversed(range(len(ops))):
+            l, qs = ops[j]
+            pidx = int(unit_base[i]) + j
+            q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
+            seq.append((BOP_ADJOINT, q0, q1, pidx,
+                        size // (4 if q1 < 0 else 16)))
+            first_of_layer = j == 0 or layer_of[j - 1] != l
+            if first_of_layer and l > 0 and l % every == 0:
+                seq.append((BOP_RESTORE, -1, -1, l // every - 1, size))
+        for k, (op, q0, q1, pp, total) in enumerate(seq):
+            ent.append((k, op, i, q0, q1, pp, total))
+    e = np.array(ent, dtype=np.int64)
+    stage, op, inst, q0, q1, pp, total = e.T
+    is_loss = op == BOP_LOSS
+    chunk = np.where(is_loss, 1, np.maximum(tile, -(-total // max_items)))
+    n_items = -(-total // chunk)
+    # one dP partial slot per ADJOINT item
+    adj = op == BOP_ADJOINT
+    slot_base = np.zeros(len(e), dtype=np.int64)
+    slot_base[adj] = np.cumsum(np.concatenate([[0], n_items[adj][:-1]]))
+    n_slots = int(n_items[adj].sum())
+    # expand entries into items
+    rep = np.repeat(np.arange(len(e)), n_items)
+    first = np.repeat(np.cumsum(n_items) - n_items, n_items)
+    j = np.arange(len(rep)) - first
+    beg = j * chunk[rep]
+    end_ = np.minimum(total[rep], beg + chunk[rep])
+    items = np.zeros(len(rep), dtype=_ITEM_DTYPE)
+    items['op'] = op[rep]
+    items['inst'] = inst[rep]
+    items['q0'] = q0[rep]
+    items['q1'] = q1[rep]
+    items['ptm'] = pp[rep]
+    items['slot'] = np.where(adj[rep], slot_base[rep] + j, 0)
+    items['beg'] = np.where(is_loss[rep], 0, beg)
+    items['end'] = np.where(is_loss[rep], 0, end_)
+    st = stage[rep]
+    n_main = int(st.max()) + 1
+    # last stage: GRADSUM per PTM over the slots of its ADJOINT items
+    gitems = np.zeros(int(adj.sum()), dtype=_ITEM_DTYPE)
+    gitems['op'] = BOP_GRADSUM
+    gitems['ptm'] = pp[adj]
+    gitems['q1'] = -1
+    gitems['beg'] = slot_base[adj]
+    gitems['end'] = slot_base[adj] + n_items[adj]
+    order = np.argsort(st, kind='stable')
+    items = np.concatenate([items[order], gitems])
+    counts = np.concatenate([np.bincount(st, minlength=n_main),
+                             [len(gitems)]])
+    begin = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    return items, begin, n_slots
+
+
 class BatchedSimulator:
     """Forward + adjoint of many circuits in one persistent launch.
 
@@ -275,84 +359,12 @@ class BatchedSimulator:
 
     # ------------------------------------------------------------ program
     def _build_program(self, tile, max_items=64):
-        """Device program for the current circuits.  Every op is one stage
-        entry per instance; an entry covering `total` groups (or elements)
-        becomes ceil(total / chunk) items with chunk = max(tile,
-        ceil(total / max_items)) -- large ops are shared by many blocks, and
-        no op has more than `max_items` items.  `tile` is a multiple of 4:
-        the kernel takes 4 consecutive groups along z per access, and an
-        item boundary must not split them."""
-        if tile < 4 or tile % 4:
-            raise ValueError('tile must be a positive multiple of 4')
-        ent = []  # (stage, op, inst, q0, q1, ptm or checkpoint, total)
-        for i, s in enumerate(self.specs):
-            size = self.sizes[i]
-            ops = [(l, qs) for l, qs, _ in self.units[i]]
-            layer_of = [l for l, _ in ops]
-            seq = [(BOP_INIT, -1, -1, 0, size)]
-            for j, (l, qs) in enumerate(ops):
-                pidx = int(self.unit_base[i]) + j
-                q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
-                seq.append((BOP_APPLY, q0, q1, pidx,
-                            size // (4 if q1 < 0 else 16)))
-                last_of_layer = j + 1 == len(ops) or layer_of[j + 1] != l
-                if last_of_layer and (l + 1) % self.every == 0 and \
-                        l + 1 < s.depth:
-                    seq.append((BOP_SAVE, -1, -1, (l + 1) // self.every - 1,
-                                size))
-            seq.append((BOP_ZERO_G, -1, -1, 0, size))
-            seq.append((BOP_LOSS, -1, -1, 0, 1))
-            for j in reversed(range(len(ops))):
-                l, qs = ops[j]
-                pidx = int(self.unit_base[i]) + j
-                q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
-                seq.append((BOP_ADJOINT, q0, q1, pidx,
-                            size // (4 if q1 < 0 else 16)))
-                first_of_layer = j == 0 or layer_of[j - 1] != l
-                if first_of_layer and l > 0 and l % self.every == 0:
-                    seq.append((BOP_RESTORE, -1, -1, l // self.every - 1,
-                                size))
-            for k, (op, q0, q1, pp, total) in enumerate(seq):
-                ent.append((k, op, i, q0, q1, pp, total))
-        e = np.array(ent, dtype=np.int64)
-        stage, op, inst, q0, q1, pp, total = e.T
-        is_loss = op == BOP_LOSS
-        chunk = np.where(is_loss, 1, np.maximum(tile, -(-total // max_items)))
-        n_items = -(-total // chunk)
-        # one dP partial slot per ADJOINT item
-        adj = op == BOP_ADJOINT
-        slot_base = np.zeros(len(e), dtype=np.int64)
-        slot_base[adj] = np.cumsum(np.concatenate([[0], n_items[adj][:-1]]))
-        n_slots = int(n_items[adj].sum())
-        # expand entries into items
-        rep = np.repeat(np.arange(len(e)), n_items)
-        first = np.repeat(np.cumsum(n_items) - n_items, n_items)
-        j = np.arange(len(rep)) - first
-        beg = j * chunk[rep]
-        end_ = np.minimum(total[rep], beg + chunk[rep])
-        items = np.zeros(len(rep), dtype=_ITEM_DTYPE)
-        items['op'] = op[rep]
-        items['inst'] = inst[rep]
-        items['q0'] = q0[rep]
-        items['q1'] = q1[rep]
-        items['ptm'] = pp[rep]
-        items['slot'] = np.where(adj[rep], slot_base[rep] + j, 0)
-        items['beg'] = np.where(is_loss[rep], 0, beg)
-        items['end'] = np.where(is_loss[rep], 0, end_)
-        st = stage[rep]
-        n_main = int(st.max()) + 1
-        # last stage: GRADSUM per PTM over the slots of its ADJOINT items
-        gitems = np.zeros(int(adj.sum()), dtype=_ITEM_DTYPE)
-        gitems['op'] = BOP_GRADSUM
-        gitems['ptm'] = pp[adj]
-        gitems['q1'] = -1
-        gitems['beg'] = slot_base[adj]
-        gitems['end'] = slot_base[adj] + n_items[adj]
-        order = np.argsort(st, kind='stable')
-        items = np.concatenate([items[order], gitems])
-        counts = np.concatenate([np.bincount(st, minlength=n_main),
-                                 [len(gitems)]])
-        begin = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+        """Device program for the current circuits (`build_program` on the
+        host, then uploaded)."""
+        items, begin, n_slots = build_program(
+            self.units, self.unit_base, self.sizes,
+            [s.depth for s in self.specs], self.every, tile, max_items)
+        n_main = len(begin) - 2
         dev = self.device
         self.n_stages = n_main + 1
         self.n_items = len(items)

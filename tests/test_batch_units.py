@@ -138,3 +138,69 @@ def test_malformed_structures_are_rejected_on_the_host(ops, msg):
         BT.BatchedSimulator([spec], [torch.ones(16) / 16], device='cpu')
     # the valid structure passes the check
     BT.validate_ops(BT.CircuitSpec(4, 3, 0).ops(), 4, 3)
+
+
+@pytest.mark.parametrize('fuse', [True, False])
+@pytest.mark.parametrize('tile', [4, 64, 8192])
+def test_program_invariants(fuse, tile):
+    """What the batch kernel relies on: every stage entry's items cover its
+    range exactly once with boundaries on multiples of 4, one entry per
+    instance per stage, the per-instance stage sequence INIT, APPLY (units
+    in order, SAVE between layers), ZERO_G, LOSS, ADJOINT (units in reverse,
+    RESTORE), every dP slot written by exactly one ADJOINT item and summed
+    by exactly one GRADSUM item of its unit."""
+    shapes = [(4, 5), (7, 3), (2, 4), (9, 2), (1, 3), (6, 8)]
+    specs = [BT.CircuitSpec(n, d, i) for i, (n, d) in enumerate(shapes)]
+    every = 2
+    units = [BT.plan_units(s.ops(), fuse) for s in specs]
+    ubase = np.cumsum([0] + [len(u) for u in units])
+    sizes = [4 ** s.n for s in specs]
+    items, begin, n_slots = BT.build_program(
+        units, ubase, sizes, [s.depth for s in specs], every, tile)
+    assert begin[0] == 0 and begin[-1] == len(items)
+    assert np.all(np.diff(begin) >= 0)
+    last = items[begin[-2]:]
+    assert np.all(last['op'] == BT.BOP_GRADSUM)
+    assert not np.any(items[:begin[-2]]['op'] == BT.BOP_GRADSUM)
+    seqs = {i: [] for i in range(len(specs))}
+    for s in range(len(begin) - 2):
+        stage = items[begin[s]:begin[s + 1]]
+        for i in np.unique(stage['inst']):
+            it = np.sort(stage[stage['inst'] == i], order='beg')
+            assert len(set(it['op'])) == 1 and len(set(it['ptm'])) == 1
+            op, pp = int(it['op'][0]), int(it['ptm'][0])
+            assert len(it) <= 64
+            if op == BT.BOP_LOSS:
+                assert len(it) == 1
+            else:
+                if op in (BT.BOP_APPLY, BT.BOP_ADJOINT):
+                    total = sizes[i] // (4 if it['q1'][0] < 0 else 16)
+                    _, qs, _ = units[i][pp - ubase[i]]
+                    assert (it['q0'][0], it['q1'][0]) == \
+                        ((qs[0], -1) if len(qs) == 1 else qs)
+                else:
+                    total = sizes[i]
+                assert it['beg'][0] == 0 and it['end'][-1] == total
+                assert np.all(it['beg'][1:] == it['end'][:-1])
+                assert np.all(it['beg'] % 4 == 0)
+                assert np.all((it['end'] % 4 == 0) | (it['end'] == total))
+            seqs[int(i)].append((op, pp))
+    for i, seq in seqs.items():
+        n_u = len(units[i])
+        ops = [o for o, _ in seq]
+        assert ops[0] == BT.BOP_INIT
+        k_loss = ops.index(BT.BOP_LOSS)
+        assert ops[k_loss - 1] == BT.BOP_ZERO_G
+        fwd = [p for o, p in seq[:k_loss] if o == BT.BOP_APPLY]
+        bwd = [p for o, p in seq[k_loss:] if o == BT.BOP_ADJOINT]
+        assert fwd == list(range(ubase[i], ubase[i] + n_u))
+        assert bwd == fwd[::-1]
+        n_ckpt = max(0, (specs[i].depth - 1) // every)
+        assert ops.count(BT.BOP_SAVE) == n_ckpt
+        assert ops.count(BT.BOP_RESTORE) == n_ckpt
+    adj = items[items['op'] == BT.BOP_ADJOINT]
+    assert sorted(adj['slot']) == list(range(n_slots))
+    for g in last:
+        mine = adj[adj['ptm'] == g['ptm']]
+        assert sorted(mine['slot']) == list(range(g['beg'], g['end']))
+    assert sorted(last['ptm']) == list(range(int(ubase[-1])))
