@@ -574,26 +574,31 @@ __device__ __forceinline__ bool item_ok(const qsgb_batch_program& p, const qsgb_
     if (it.q1 >= 0 && (it.q1 <= it.q0 || it.q1 >= n)) return false;
     return it.end <= (in.size >> (it.q1 < 0 ? 2 : 4));
   }
-  return it.end <= in.size;
+  return it.end <= in.size && (it.beg & 3) == 0 && (it.end & 3) == 0;
 }
 
 __device__ void process(const qsgb_batch_program& p, const qsgb_batch_item& it, BatchSmem& sm) {
   const qsgb_batch_instance in = p.instances[it.inst];
   switch (it.op) {
+    // element ranges start and end on multiples of 4 (item_ok): 16-byte accesses
     case QSGB_BOP_INIT:
-      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) in.x[e] = (e == 0) ? 1.f : 0.f;
+      for (int64_t e = it.beg + 4 * (int64_t)threadIdx.x; e < it.end; e += 4 * (int64_t)blockDim.x)
+        *reinterpret_cast<float4*>(in.x + e) = make_float4(e == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
       break;
     case QSGB_BOP_ZERO_G:
-      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) in.g[e] = 0.f;
+      for (int64_t e = it.beg + 4 * (int64_t)threadIdx.x; e < it.end; e += 4 * (int64_t)blockDim.x)
+        *reinterpret_cast<float4*>(in.g + e) = make_float4(0.f, 0.f, 0.f, 0.f);
       break;
     case QSGB_BOP_SAVE: {
       float* dst = in.ckpt + (int64_t)it.ptm * in.size;
-      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) dst[e] = in.x[e];
+      for (int64_t e = it.beg + 4 * (int64_t)threadIdx.x; e < it.end; e += 4 * (int64_t)blockDim.x)
+        *reinterpret_cast<float4*>(dst + e) = *reinterpret_cast<const float4*>(in.x + e);
       break;
     }
     case QSGB_BOP_RESTORE: {
       const float* src = in.ckpt + (int64_t)it.ptm * in.size;
-      for (int64_t e = it.beg + threadIdx.x; e < it.end; e += blockDim.x) in.x[e] = src[e];
+      for (int64_t e = it.beg + 4 * (int64_t)threadIdx.x; e < it.end; e += 4 * (int64_t)blockDim.x)
+        *reinterpret_cast<float4*>(in.x + e) = *reinterpret_cast<const float4*>(src + e);
       break;
     }
     case QSGB_BOP_APPLY:
