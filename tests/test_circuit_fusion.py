@@ -166,3 +166,62 @@ def test_units_of_matches_reference_when_available():
     finally:
         for p in (os.path.join(here, '_stubs'), ref, here):
             sys.path.remove(p)
+
+
+def _random_units(rng):
+    """A random unit list over 2-4 qudits of dims 4 (qubit, full basis) or 9
+    (qutrit): sparse physical PTMs on single qudits and on ordered pairs,
+    and now and then a rectangular basis reduction (a barrier that changes
+    the qudit's dimension)."""
+    n = int(rng.integers(2, 5))
+    dims = [int(rng.choice([4, 4, 9])) for _ in range(n)]
+    t1, t2 = workloads.coherence_times(rng, n)
+    units = []
+    for _ in range(int(rng.integers(3, 15))):
+        u = rng.random()
+        if u < 0.45:
+            q = int(rng.integers(n))
+            if dims[q] == 4:
+                units.append((workloads.noisy_1q(rng, t1[q], t2[q]), (q,)))
+            elif dims[q] == 9:
+                units.append((workloads.qutrit_1q(rng), (q,)))
+            else:
+                units.append((rng.standard_normal((dims[q], dims[q])), (q,)))
+        elif u < 0.9:
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            if dims[a] == dims[b] == 4:
+                ptm = workloads.noisy_cz(rng, (a, b), t1, t2)
+            elif dims[a] == dims[b] == 9:
+                ptm = workloads.qutrit_2q(rng)
+            else:
+                ptm = rng.standard_normal((dims[a], dims[b], dims[a], dims[b]))
+                ptm *= rng.random(ptm.shape) < 0.15
+            units.append((ptm, (a, b)))
+        else:
+            q = int(rng.integers(n))
+            keep = sorted(int(v) for v in rng.choice(
+                dims[q], int(rng.integers(1, dims[q])), replace=False))
+            units.append((np.eye(dims[q])[keep], (q,)))
+            dims[q] = len(keep)
+    return units, n
+
+
+def test_plan_random_unit_sequences():
+    """Random unit lists: the fused plan applied by the oracle equals the
+    units applied one by one (rectangular units act as barriers)."""
+    for seed in range(24):
+        rng = np.random.default_rng(300 + seed)
+        units, n = _random_units(rng)
+        shape = []
+        for q in range(n):
+            first = [u for u in units if q in u[1]]
+            d = 4
+            if first:
+                ptm, qs = first[0]
+                d = ptm.shape[len(qs) + qs.index(q)]
+            shape.append(d)
+        pv = _rand_pv(rng, tuple(shape))
+        fused = C.plan(units)
+        assert len(fused) <= len(units)
+        assert_close_dot(_apply_all(pv, fused), _apply_all(pv, units),
+                         _abs_all(np.abs(pv), units) * 16 + 1e-300)
