@@ -186,3 +186,26 @@ def test_batch_program_layout_matches_the_header():
     assert P.work.offset == 32 and ctypes.sizeof(P) == 96
     assert ctypes.sizeof(BT._Instance) == 40
     assert BT._ITEM_DTYPE.itemsize == 40
+
+
+def test_plain_c_host_binds_the_library(lib, tmp_path):
+    """A C program (tests/c_host/abi_smoke.c) compiled with gcc against
+    include/qsgb.h and linked to libqsgb.so: the binding a C, cgo, JNI or
+    N-API host would make.  It checks the ABI version, the status strings
+    and host-side argument errors, none of which needs a GPU."""
+    import shutil
+    import subprocess
+    gcc = shutil.which('gcc')
+    if gcc is None:
+        pytest.skip('gcc not available')
+    libdir = os.path.dirname(L.library_path())
+    exe = str(tmp_path / 'abi_smoke')
+    build = subprocess.run(
+        [gcc, '-std=c99', '-Wall', '-Werror', '-I', os.path.join(ROOT, 'include'),
+         os.path.join(ROOT, 'tests', 'c_host', 'abi_smoke.c'), '-L', libdir,
+         '-lqsgb', '-Wl,-rpath,' + libdir, '-o', exe],
+        capture_output=True, text=True)
+    assert build.returncode == 0, build.stderr
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
+    assert 'argument checks ok' in run.stdout
