@@ -42,10 +42,10 @@ sys.path.insert(0, ROOT)
 
 N_QUBITS = 14
 APPS_PER_STEP = 7
-# DRAM bytes (read + write) of one 14-qubit noisy-CZ launch, from the ncu
-# capture summarised in profiles/apply_jit_traffic_13q.md (13-qubit launch:
-# 536.9 MB read, 486.8 MB written; reads scale 4x, writes 4x minus the ~50 MB
-# still in L2 at kernel end)
+# DRAM bytes (read + write) of one 14-qubit noisy-CZ launch, scaled from an
+# ncu capture of the same kernel on 13 qubits (536.9 MB read, 486.8 MB
+# written per launch; reads scale 4x, writes 4x minus the ~50 MB still in L2
+# at kernel end)
 TRAFFIC_14Q = 4 * 536.9e6 + 4 * 536.9e6 - 50e6
 METRIC = ('2q-PTM apps/s & HBM GB/s (14q fp64); batched fp32 fwd+adjoint vs '
           'plain, err<1e-6')
@@ -636,6 +636,28 @@ def run_ops_config():
     out['reduce_basis_9to3_ms'] = tr * 1e3
     out['reduce_basis_gbs'] = 2 * n_red * 8 / tr / 1e9
     out['project_ms'] = tp * 1e3
+    # the take kernel alone (CUDA events on the launching stream, 20
+    # launches on resident tensors larger than L2): bytes = entries kept,
+    # read and written
+    q = qg.PauliVectorGB300([g3] * 8, force=True)
+    q._data.copy_(torch.rand_like(q._data))
+    red = torch.ops.qsgb.take_axis(q._data, 3, comp)
+    for name, x, axis, idx, n_keep in (
+            ('reduce_basis_9to3', q._data, 3, comp, n_red),
+            ('project_9to1', red, 5, [comp[1]], 9 ** 6 * 3)):
+        torch.ops.qsgb.take_axis(x, axis, idx)
+        stream = torch.cuda.current_stream()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(20):
+            torch.ops.qsgb.take_axis(x, axis, idx)
+        b.record(stream)
+        torch.cuda.synchronize()
+        dt = a.elapsed_time(b) / 1e3 / 20
+        out[name + '_kernel_us'] = dt * 1e6
+        out[name + '_kernel_gbs'] = 2 * n_keep * 8 / dt / 1e9
+    del q, red
     out['workload'] = ('14 qubits FP64 (diagonal, trace, meas_prob, '
                        'partial_trace keeping 4, renormalize); 8 qutrits '
                        'FP64 (reduce_basis 9 -> 3 on one qutrit, then '

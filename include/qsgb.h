@@ -33,7 +33,10 @@ extern "C" {
 #define QSGB_ERR_SCRATCH 4     /* caller scratch buffer too small */
 
 /* ---- device status bits (written into *dev_status) ---- */
-#define QSGB_DEV_RANGE 1u      /* df64 arithmetic saw |x| >= 2^128, inf or nan */
+#define QSGB_DEV_RANGE 1u      /* reserved: apply kernels no longer raise it --
+                                  float-float rows whose inputs or results
+                                  leave the float pair's range are computed
+                                  again in native FP64 by the kernel */
 #define QSGB_DEV_TIMEOUT 2u    /* a bounded device-side wait gave up */
 #define QSGB_DEV_BADITEM 4u    /* batched work queue met a malformed item
                                   (unknown op, targets outside its instance,
@@ -135,6 +138,22 @@ int qsgb_prepare_ptm2(const double* ptm, int64_t d0_out, int64_t d1_out,
                       int arith);
 
 /*
+ * Diagnostic: generate the CUDA source of the kernel that qsgb_prepare_ptm2
+ * would compile for this host PTM and geometry, and compile it with NVRTC
+ * for sm_103a without loading it -- no device is needed, so a build host can
+ * check the code generator.  The source text (NUL-terminated, truncated to
+ * src_bytes - 1 characters) is written to `src` when it is not NULL.
+ * QSGB_OK when it compiles, QSGB_ERR_CUDA on a compile error (the NVRTC log
+ * goes to stderr when the environment sets QSGB_JIT_VERBOSE),
+ * QSGB_ERR_UNSUPPORTED when no specialised kernel applies or NVRTC is
+ * missing.  No counterpart in the reference.
+ */
+int qsgb_jit_check_ptm2(const double* ptm, int64_t d0_out, int64_t d1_out,
+                        int64_t d0_in, int64_t d1_in, int64_t dim_x,
+                        int64_t dim_y, int64_t dim_z, int ptm_flags,
+                        int dtype, int arith, char* src, int64_t src_bytes);
+
+/*
  * Multi-axis take ("multitake"): out = in[np.ix_(idx_0, ..., idx_{n-1})].
  * Replaces: quantumsim/pauli_vectors/primitives.cu:100-130 (multitake, used by
  * cuda.py:279-345 diagonal()).  Index lists are CSR-like as in cuda.py:307-313
@@ -189,8 +208,16 @@ int qsgb_marginals(const double* diag, int ndim, const int64_t* shape,
  * no cudaMalloc, cudaFree or allocating library routine.
  *
  * - The first call on each device looks up the array's device address
- *   (cudaGetSymbolAddress) with that device current; make that first call
- *   before any stream capture on the device.
+ *   (cudaGetSymbolAddress) with that device current.  Under CUDA's default
+ *   lazy module loading that lookup also loads the library's device code
+ *   on the device, which is when the 128 KiB array is reserved: a program
+ *   whose pool has already taken every byte of device memory can see that
+ *   first call fail with QSGB_ERR_CUDA.  Make one warm-up call per device
+ *   at initialisation, before the pool takes its memory and before any
+ *   stream capture on the device.
+ * - The address is cached per device and CUDA context.  After
+ *   cudaDeviceReset, or in another context made current through the driver
+ *   API, the next call looks it up again (the same first-call rules apply).
  * - Requests needing more than qsgb_marginals_noalloc_max_scratch_bytes()
  *   of partial sums (chunks x outcomes > 16384 doubles) return
  *   QSGB_ERR_SCRATCH; up to 32 outcomes per axis always fit.

@@ -52,6 +52,9 @@ SIGNATURES = {
                                _i64, _c_void_p, _c_void_p]),
     'qsgb_prepare_ptm2': (_int, [_c_void_p, _i64, _i64, _i64, _i64, _i64,
                                  _i64, _i64, _int, _int, _int]),
+    'qsgb_jit_check_ptm2': (_int, [_c_void_p, _i64, _i64, _i64, _i64, _i64,
+                                   _i64, _i64, _int, _int, _int, _c_void_p,
+                                   _i64]),
     'qsgb_gather': (_int, [_c_void_p, _c_void_p, _int, _int, _int, _p_i64,
                            _p_i32, _p_i32, _c_void_p]),
     'qsgb_take_axis': (_int, [_c_void_p, _c_void_p, _int, _i64, _i64, _i64,

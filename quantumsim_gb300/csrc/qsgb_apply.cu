@@ -39,6 +39,8 @@
 #include "qsgb_common.cuh"
 #include "qsgb_jit.h"
 #include <cmath>
+#include <cstring>
+#include <string>
 #include <vector>
 
 namespace qsgb {
@@ -264,6 +266,9 @@ __device__ bool build_terms(const ApplyParams& p, const SmemLayout& L, unsigned 
   __syncthreads();
   const double thr =
       (p.arith == QSGB_ARITH_F64) ? 0.0 : red[32] * ((p.arith == QSGB_ARITH_F32) ? 0x1p-30 : 0x1p-52);
+  // float-float rows carry PTM entries as float pairs: a PTM whose largest
+  // entry is outside [2^-100, 2^100] is computed in native FP64 throughout
+  const bool all_dp = p.arith != QSGB_ARITH_F32 && !(red[32] >= 0x1p-100 && red[32] <= 0x1p100);
   for (int r = tid; r < p.kout; r += nthr) {
     int c = 0;
     for (int k = 0; k < p.kin; ++k) c += fabs(stage[r * p.kin + k]) > thr;
@@ -315,7 +320,7 @@ __device__ bool build_terms(const ApplyParams& p, const SmemLayout& L, unsigned 
         mode = kZero;
       else if (p.arith == QSGB_ARITH_F32)
         mode = kF32;
-      else if (p.arith == QSGB_ARITH_F64 || c == 1)
+      else if (p.arith == QSGB_ARITH_F64 || c == 1 || all_dp)
         mode = kDP;
       else if (p.arith == QSGB_ARITH_DF64)
         mode = kDF;
@@ -446,7 +451,6 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
     }
   };
 
-  unsigned bad = 0;
   uint64_t t = blockIdx.x;
   int b = 0;
   if (t < n_tiles) load_tile(t, 0);
@@ -491,6 +495,7 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
             }
           } else if (ri.mode == kDF) {
             float s[NL], c[NL];
+            unsigned fb = 0;  // the row needs native FP64 (input or result range)
             {
               const Term tm = terms[ri.beg];
               const float ph = __int_as_float(__double2hiint(tm.p));
@@ -499,7 +504,7 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
 #pragma unroll
               for (int l = 0; l < NL; ++l) {
                 float xh, xl;
-                split_f64((double)lane_of(xv, l), xh, xl, bad);
+                split_f64((double)lane_of(xv, l), xh, xl, fb);
                 df_mul(s[l], c[l], ph, pl, xh, xl);
               }
             }
@@ -511,12 +516,29 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
 #pragma unroll
               for (int l = 0; l < NL; ++l) {
                 float xh, xl;
-                split_f64((double)lane_of(xv, l), xh, xl, bad);
+                split_f64((double)lane_of(xv, l), xh, xl, fb);
                 df_fma(s[l], c[l], ph, pl, xh, xl);
               }
             }
 #pragma unroll
-            for (int l = 0; l < NL; ++l) acc[l] = df_to_double(s[l], c[l]);
+            for (int l = 0; l < NL; ++l) {
+              fb |= qsgb_df_suspect(s[l]);
+              acc[l] = df_to_double(s[l], c[l]);
+            }
+            if (fb) {
+              // outside the float-float range: the row again in native FP64
+              // (the term is carried as hi + lo, 48 significant bits)
+#pragma unroll
+              for (int l = 0; l < NL; ++l) acc[l] = 0.0;
+              for (int q = ri.beg; q < ri.end; ++q) {
+                const Term tm = terms[q];
+                const double cf = (double)__int_as_float(__double2hiint(tm.p)) +
+                                  (double)__int_as_float(__double2loint(tm.p));
+                const V xv = xb[tm.k * tile];
+#pragma unroll
+                for (int l = 0; l < NL; ++l) acc[l] = fma(cf, (double)lane_of(xv, l), acc[l]);
+              }
+            }
           }
           put(dst, acc);
         }
@@ -526,7 +548,6 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
     b ^= 1;
   }
   cp_async_wait<0>();
-  if (bad && p.status) atomicOr(p.status, QSGB_DEV_RANGE);
 }
 
 // row groups = min(Kout, 4) rounded down to a power of two; the remaining
@@ -568,9 +589,13 @@ int launch_apply(ApplyParams& p, cudaStream_t stream) {
 // ---------------------------------------------------------------------------
 // Returns QSGB_ERR_UNSUPPORTED when the specialised path does not apply.
 // prepare_only: compile (or fetch) the kernel, launch nothing.
+// mode: kLaunch, kPrepare (compile and load, launch nothing) or kCompileOnly
+// (generate and compile the source, no device needed; *src_out gets it).
+enum { kLaunch = 0, kPrepare = 1, kCompileOnly = 2 };
+
 int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_in, int64_t db_in, int64_t Z,
             int flags, int dtype, int arith, bool pair, ApplyParams& p, cudaStream_t stream,
-            bool prepare_only = false) {
+            int mode = kLaunch, std::string* src_out = nullptr) {
   if (!(flags & QSGB_PTM_HOST) || (flags & QSGB_PTM_NOJIT) || !jit::available()) return QSGB_ERR_UNSUPPORTED;
   // Z == 1: the db inputs (outputs) of a group along the less significant
   // target are contiguous; move them with 2- or 4-wide vector accesses
@@ -607,7 +632,8 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
                         Z == 1, contiguous, vwidth(db_in, p.in), vwidth(db_out, p.out), spec, coef))
       return QSGB_ERR_UNSUPPORTED;
   }
-  if (prepare_only) return jit::prepare(spec);
+  if (mode == kPrepare) return jit::prepare(spec);
+  if (mode == kCompileOnly) return jit::compile_only(spec, src_out);
   const int NL = pair ? 2 : 1;
   jit::Geometry g;
   g.in = p.in;
@@ -627,11 +653,13 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
   return jit::launch(spec, g, coef.data(), stream);
 }
 
-// prepare_only: validate, then compile the specialised kernel the call would
-// launch (for tensors aligned as allocators give them), and launch nothing.
+// mode kPrepare / kCompileOnly: validate, then compile the specialised
+// kernel the call would launch (for tensors aligned as allocators give
+// them), and launch nothing.
 int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, int64_t db_out, int64_t da_in,
                  int64_t db_in, int64_t X, int64_t Y, int64_t Z, int flags, int dtype, int arith,
-                 int64_t max_terms, unsigned* status, void* stream, bool prepare_only = false) {
+                 int64_t max_terms, unsigned* status, void* stream, int mode = kLaunch,
+                 std::string* src_out = nullptr) {
   if (!in || !out || !ptm) return QSGB_ERR_INVALID;
   if (in == out) return QSGB_ERR_INVALID;
   if (da_out < 1 || db_out < 1 || da_in < 1 || db_in < 1 || X < 1 || Y < 1 || Z < 1) return QSGB_ERR_INVALID;
@@ -675,8 +703,8 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
   // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)
-  const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s, prepare_only);
-  if (js != QSGB_ERR_UNSUPPORTED || prepare_only) return js;
+  const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s, mode, src_out);
+  if (js != QSGB_ERR_UNSUPPORTED || mode != kLaunch) return js;
   // 2. generic kernel; a host PTM travels inside its launch parameters
   if (flags & QSGB_PTM_HOST) {
     if (kin * kout > kMaxInline) return QSGB_ERR_UNSUPPORTED;
@@ -732,5 +760,22 @@ extern "C" int qsgb_prepare_ptm2(const double* ptm, int64_t d0_out, int64_t d1_o
   const void* in = reinterpret_cast<const void*>(uintptr_t(256));
   void* out = reinterpret_cast<void*>(uintptr_t(512));
   return qsgb::apply_common(in, out, ptm, d0_out, d1_out, d0_in, d1_in, dim_x, dim_y, dim_z, ptm_flags, dtype,
-                            arith, 0, nullptr, nullptr, true);
+                            arith, 0, nullptr, nullptr, qsgb::kPrepare);
+}
+
+extern "C" int qsgb_jit_check_ptm2(const double* ptm, int64_t d0_out, int64_t d1_out, int64_t d0_in, int64_t d1_in,
+                                   int64_t dim_x, int64_t dim_y, int64_t dim_z, int ptm_flags, int dtype, int arith,
+                                   char* src, int64_t src_bytes) {
+  if (!(ptm_flags & QSGB_PTM_HOST)) return QSGB_ERR_INVALID;
+  const void* in = reinterpret_cast<const void*>(uintptr_t(256));
+  void* out = reinterpret_cast<void*>(uintptr_t(512));
+  std::string text;
+  const int st = qsgb::apply_common(in, out, ptm, d0_out, d1_out, d0_in, d1_in, dim_x, dim_y, dim_z, ptm_flags,
+                                    dtype, arith, 0, nullptr, nullptr, qsgb::kCompileOnly, &text);
+  if (src && src_bytes > 0) {
+    const size_t n = std::min<size_t>(text.size(), (size_t)src_bytes - 1);
+    std::memcpy(src, text.data(), n);
+    src[n] = '\0';
+  }
+  return st;
 }

@@ -27,9 +27,10 @@ __device__ __forceinline__ qsgb_u64 qsgb_fdiv(qsgb_u64 n, qsgb_u64 m, int l) {
 // Split an IEEE double into hi + lo floats with integer operations only (the
 // FP64<->FP32 converters run on the slow FP64 pipe on GB300).  hi keeps the
 // top 24 significant bits (truncated), lo the next 23 bits, so hi + lo agrees
-// with x to 2^-47 relative.  |x| < 2^-126 flushes to 0, |x| in
-// [2^-126, 2^-102) keeps only hi; |x| >= 2^128, inf and nan set `bad` and
-// give nan.
+// with x to 2^-47 relative.  Inputs the float pair cannot carry to that
+// precision set `bad`: a non-zero |x| < 2^-102 (|x| < 2^-126 flushes to 0,
+// [2^-126, 2^-102) keeps only hi) and |x| >= 2^128, inf and nan (which give
+// nan).  Callers recompute the affected results in native FP64.
 __device__ __forceinline__ void qsgb_split_f64(double x, float& hi, float& lo, unsigned& bad) {
   const unsigned h = (unsigned)__double2hiint(x);
   const unsigned l = (unsigned)__double2loint(x);
@@ -46,7 +47,20 @@ __device__ __forceinline__ void qsgb_split_f64(double x, float& hi, float& lo, u
   const bool has_lo = e >= 920u;
   hi = in_range ? __uint_as_float(hb) : (e < 897u ? __uint_as_float(sgn) : __int_as_float(0x7fc00000));
   lo = (in_range && has_lo) ? lo_full : 0.0f;
-  bad |= (e > 1150u) ? 1u : 0u;
+  // e in [921, 1150] is 2^-102 <= |x| < 2^128; e == 0 with a zero
+  // mantissa is an exact zero, carried exactly
+  bad |= ((e - 921u) > 229u && ((h << 1) | l) != 0u) ? 1u : 0u;
+}
+
+// A float-float row result whose leading float s is outside the range where
+// the pair keeps 48 significant bits: 0 < |s| < 2^-70 (products whose error
+// terms may have fallen below the normal floats) or |s| >= 2^126 (near
+// overflow), inf or nan.  s == 0 is exact when every input of the row is
+// (inputs below 2^-102 are flagged by qsgb_split_f64).  Callers recompute
+// such rows in native FP64.
+__device__ __forceinline__ unsigned qsgb_df_suspect(float s) {
+  const unsigned b = __float_as_uint(s) & 0x7fffffffu;
+  return ((b - 1u) < 0x1c7fffffu || b >= 0x7e800000u) ? 1u : 0u;
 }
 
 // acc (s, c) += (ph + pl) * (xh + xl); pl*xl (2^-48 relative) is dropped.

@@ -168,6 +168,63 @@ std::string gen_source(const Spec& s) {
   std::snprintf(buf, sizeof buf, "struct P { H h; double c[%d]; };\n", std::max(1, s.n_coef()));
   src += buf;
   const char* V = s.pair ? (f32 ? "qv2f" : "qv2d") : scal;
+  // Float-float rows of an item whose inputs or results leave the range of
+  // the float pair (qsgb_split_f64, qsgb_df_suspect) are computed again in
+  // native FP64 from the input, which the kernel does not overwrite (it
+  // writes a separate output): a loop over tables of the pattern's terms,
+  // kept out of the unrolled hot path.
+  std::string fallback;
+  if (std::count(s.mode.begin(), s.mode.end(), (int)kModeDF) > 0) {
+    std::string tk, te, td;
+    int t = 0;
+    for (int r = 0; r < s.kout; ++r) {
+      for (int k : s.cols[r]) tk += std::to_string(k) + ",";
+      t += (int)s.cols[r].size();
+      te += std::to_string(t) + ",";
+      td += s.mode[r] == kModeDF ? "1," : "0,";
+    }
+    if (tk.empty()) tk = "0,";
+    src += "__constant__ unsigned short qfb_k[] = {" + tk + "};\n";
+    src += "__constant__ unsigned short qfb_end[] = {" + te + "};\n";
+    src += "__constant__ unsigned char qfb_df[] = {" + td + "};\n";
+    const bool staged = s.stage_warps > 0;
+    std::snprintf(buf, sizeof buf,
+                  "    if (fb%s) {\n"
+                  "      unsigned tq = 0;\n"
+                  "#pragma unroll 1\n"
+                  "      for (int r = 0; r < %d; ++r) {\n"
+                  "        const unsigned te = qfb_end[r];\n"
+                  "        if (!qfb_df[r]) { tq = te; continue; }\n"
+                  "        double a0 = 0.0, a1 = 0.0;\n"
+                  "#pragma unroll 1\n"
+                  "        for (; tq < te; ++tq) {\n"
+                  "          const unsigned k = qfb_k[tq];\n"
+                  "          const double cf = (double)QH(p.c[tq]) + (double)QL(p.c[tq]);\n"
+                  "          const V xv = in[bi + (qsgb_i64)(k / %du) * p.h.sai + (qsgb_i64)(k %% %du) * %s];\n"
+                  "%s"
+                  "        }\n"
+                  "%s"
+                  "      }\n"
+                  "    }\n",
+                  staged ? " && lane < nv" : "", s.kout, s.db_in, s.db_in, staged ? "1" : "p.h.sbi",
+                  s.pair ? "          a0 = fma(cf, xv.x, a0); a1 = fma(cf, xv.y, a1);\n"
+                         : "          a0 = fma(cf, xv, a0);\n",
+                  "");
+    fallback = buf;
+    // where the row's result goes
+    std::string store;
+    if (staged) {
+      std::snprintf(buf, sizeof buf, "        t[lane * %d + r] = a0; (void)a1;\n", std::max(s.kin, s.kout));
+      store = buf;
+    } else {
+      std::snprintf(buf, sizeof buf,
+                    "        { V yv; %s out[bo + (qsgb_i64)(r / %d) * p.h.sao + (qsgb_i64)(r %% %d) * p.h.sbo] = yv; }\n",
+                    s.pair ? "yv.x = a0; yv.y = a1;" : "yv = a0; (void)a1;", s.db_out, s.db_out);
+      store = buf;
+    }
+    const size_t at = fallback.rfind("      }\n    }\n");
+    fallback.insert(at, store);
+  }
   src += "#define QH(v) __int_as_float(__double2hiint(v))\n#define QL(v) __int_as_float(__double2loint(v))\n";
   // vector loads / stores along the less significant target when Z == 1
   {
@@ -207,7 +264,7 @@ std::string gen_source(const Spec& s) {
                   "  const V* __restrict__ in = (const V*)p.h.in;\n"
                   "  V* __restrict__ out = (V*)p.h.out;\n"
                   "  const unsigned tb = (unsigned)__cvta_generic_to_shared(t);\n"
-                  "  unsigned bad_all = 0;\n",
+                  "",
                   32 * s.stage_warps, scal, s.stage_warps, KS);
     src += buf;
     if (s.stage_bulk) {
@@ -238,7 +295,7 @@ std::string gen_source(const Spec& s) {
                   "      bi = (qsgb_i64)xx * p.h.sxi + (qsgb_i64)yy * p.h.syi;\n"
                   "      bo = (qsgb_i64)xx * p.h.sxo + (qsgb_i64)yy * p.h.syo;\n"
                   "    }\n"
-                  "    unsigned bad = 0;\n",
+                  "    unsigned fb = 0;  // the item needs native FP64 (input or result range)\n",
                   s.stage_warps, s.stage_warps);
     src += buf;
     if (s.stage_bulk) {
@@ -303,7 +360,6 @@ std::string gen_source(const Spec& s) {
                 "  typedef %s V;\n"
                 "  const V* __restrict__ in = (const V*)p.h.in;\n"
                 "  V* __restrict__ out = (V*)p.h.out;\n"
-                "  unsigned bad = 0;\n"
                 "  const qsgb_u64 stride = (qsgb_u64)gridDim.x * blockDim.x;\n"
                 "  for (qsgb_u64 it = (qsgb_u64)blockIdx.x * blockDim.x + threadIdx.x; it < p.h.n_items; it += "
                 "stride) {\n"
@@ -312,7 +368,8 @@ std::string gen_source(const Spec& s) {
                 "    const qsgb_u64 xx = qsgb_fdiv(t1, p.h.ym, (int)p.h.yl);\n"
                 "    const qsgb_u64 yy = t1 - xx * p.h.yd;\n"
                 "    const qsgb_i64 bi = (qsgb_i64)xx * p.h.sxi + (qsgb_i64)yy * p.h.syi + (qsgb_i64)zi;\n"
-                "    const qsgb_i64 bo = (qsgb_i64)xx * p.h.sxo + (qsgb_i64)yy * p.h.syo + (qsgb_i64)zi;\n",
+                "    const qsgb_i64 bo = (qsgb_i64)xx * p.h.sxo + (qsgb_i64)yy * p.h.syo + (qsgb_i64)zi;\n"
+                "    unsigned fb = 0;  // the item needs native FP64 (input or result range)\n",
                 V);
   src += buf;
   }
@@ -373,7 +430,7 @@ std::string gen_source(const Spec& s) {
     if (splitd[k]) return;
     splitd[k] = 1;
     for (int l = 0; l < NL; ++l) {
-      std::snprintf(buf, sizeof buf, "    float h%d_%d, l%d_%d; qsgb_split_f64(x%d%s, h%d_%d, l%d_%d, bad);\n", k, l, k,
+      std::snprintf(buf, sizeof buf, "    float h%d_%d, l%d_%d; qsgb_split_f64(x%d%s, h%d_%d, l%d_%d, fb);\n", k, l, k,
                     l, k, lanes[l], k, l, k, l);
       src += buf;
     }
@@ -451,6 +508,8 @@ std::string gen_source(const Spec& s) {
                         l, q, q, cols[j], l, cols[j], l);
           src += buf;
         }
+        std::snprintf(buf, sizeof buf, "      fb |= qsgb_df_suspect(s%d);\n", l);
+        src += buf;
         vals[l] = "qsgb_df_to_double(s" + std::to_string(l) + ", c" + std::to_string(l) + ")";
       }
     }
@@ -489,6 +548,7 @@ std::string gen_source(const Spec& s) {
     }
   }
   if (s.stage_warps) {
+    src += fallback;
     src += "    __syncwarp();\n";
     if (s.stage_bulk) {
       // generic-proxy tile writes -> visible to the bulk (async-proxy) store
@@ -519,15 +579,15 @@ std::string gen_source(const Spec& s) {
                   "    }\n"
                   "%s"
                   "    __syncwarp();\n"
-                  "    if (lane < nv) bad_all |= bad;\n"
                   "  }\n",
                   s.db_out, s.db_out, s.db_out, s.kout / s.db_out, s.db_out, s.db_out, s.db_out, KS, s.db_out,
                   s.stage_bulk ? "    }\n" : "");
     src += buf;
     if (s.stage_bulk) src += "  if (lane == 0) asm volatile(\"cp.async.bulk.wait_group 0;\" ::: \"memory\");\n";
-    src += "  if (bad_all && p.h.status) atomicOr(p.h.status, 1u);\n}\n";
+    src += "}\n";
   } else {
-    src += "  }\n  if (bad && p.h.status) atomicOr(p.h.status, 1u);\n}\n";
+    src += fallback;
+    src += "  }\n}\n";
   }
   return src;
 }
@@ -759,6 +819,9 @@ bool make_spec(const double* ptm_host, int da_out, int db_out, int da_in, int db
       M[(size_t)r * kin + k] = v;
       amax = std::max(amax, std::fabs(v));
     }
+  // float-float rows carry PTM entries as float pairs: a PTM whose largest
+  // entry is outside [2^-100, 2^100] is computed in native FP64 throughout
+  if (arith != QSGB_ARITH_F32 && !(amax >= 0x1p-100 && amax <= 0x1p100)) arith = QSGB_ARITH_F64;
   const double thr = arith == QSGB_ARITH_F64 ? 0.0 : amax * (arith == QSGB_ARITH_F32 ? 0x1p-30 : 0x1p-52);
   spec.kin = kin;
   spec.kout = kout;
@@ -856,6 +919,27 @@ int kernel_for(const Spec& s, cudaKernel_t* k, std::string* src_out) {
 int prepare(const Spec& s) {
   cudaKernel_t kern;
   return kernel_for(s, &kern, nullptr);
+}
+
+int compile_only(const Spec& s, std::string* src_out) {
+  if (s.n_coef() > kMaxCoef) return QSGB_ERR_UNSUPPORTED;
+  const std::string src = gen_source(s);
+  if (src_out) *src_out = src;
+  Nvrtc& n = nvrtc();
+  if (!n.ok) return QSGB_ERR_UNSUPPORTED;
+  nvrtcProgram prog;
+  if (n.create(&prog, src.c_str(), "qsgb_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) return QSGB_ERR_UNSUPPORTED;
+  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device"};
+  const nvrtcResult cr = n.compile(prog, 3, opts);
+  if (cr != NVRTC_SUCCESS && std::getenv("QSGB_JIT_VERBOSE")) {
+    size_t ls = 0;
+    n.log_size(prog, &ls);
+    std::string log(ls, '\0');
+    n.log(prog, &log[0]);
+    std::fprintf(stderr, "qsgb jit: compilation failed:\n%s\n", log.c_str());
+  }
+  n.destroy(&prog);
+  return cr == NVRTC_SUCCESS ? QSGB_OK : QSGB_ERR_CUDA;
 }
 
 int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t stream) {

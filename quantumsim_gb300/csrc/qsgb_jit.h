@@ -60,6 +60,10 @@ int kernel_for(const Spec& s, cudaKernel_t* k, std::string* src_out);
 int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t stream);
 // Compile (or fetch from the caches) the kernel of `s` without launching it.
 int prepare(const Spec& s);
+// Generate the source of `s` and compile it with NVRTC without loading it
+// (no device needed): QSGB_OK, QSGB_ERR_CUDA on a compile error,
+// QSGB_ERR_UNSUPPORTED without NVRTC.
+int compile_only(const Spec& s, std::string* src_out);
 
 }  // namespace jit
 }  // namespace qsgb

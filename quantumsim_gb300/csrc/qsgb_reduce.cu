@@ -61,27 +61,89 @@ __global__ void gather_kernel(const __grid_constant__ GatherParams p) {
 }
 
 // ---------------------------------------------------------------- take axis
+// out[o, j, :] = in[o, idx[j], :] for a tensor viewed as (outer, d_in,
+// inner): a copy of rows of `inner` contiguous elements, moved as raw bits
+// (bit-exact) in units V of 16 bytes when the row length and both tensors
+// allow it, else of one element.  Long rows are cut into tiles of
+// kTakeTile units; the row and source of a tile are found once per tile, and
+// each thread keeps kTakeUnroll loads in flight.  Short rows (the last
+// qudits) go unit by unit with the index arithmetic per unit.
+constexpr int kTakeBlock = 256;
+constexpr int kTakeUnroll = 4;
+constexpr uint64_t kTakeTile = (uint64_t)kTakeBlock * kTakeUnroll;
+
 struct TakeParams {
   const void* in;
   void* out;
-  uint64_t n_out;
-  FastDiv div_inner, div_dout;
-  int64_t d_in, inner;
+  uint64_t n_rows;         // outer * d_out
+  uint64_t row_v;          // units per row
+  uint64_t tiles_per_row;  // row mode
+  uint64_t n_units;        // unit mode: n_rows * row_v
+  FastDiv div_tpr, div_dout, div_rowv;
+  int64_t d_in;
   int idx[kMaxIdx];
 };
 
-template <typename T>
-__global__ void take_kernel(const __grid_constant__ TakeParams p) {
-  const T* __restrict__ in = static_cast<const T*>(p.in);
-  T* __restrict__ out = static_cast<T*>(p.out);
-  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < p.n_out;
-       e += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t t = fdiv(e, p.div_inner);
-    const uint64_t i = e - t * p.inner;
+template <typename V>
+__global__ void __launch_bounds__(kTakeBlock) take_rows_kernel(const __grid_constant__ TakeParams p) {
+  const V* __restrict__ in = static_cast<const V*>(p.in);
+  V* __restrict__ out = static_cast<V*>(p.out);
+  const uint64_t n_tiles = p.n_rows * p.tiles_per_row;
+  for (uint64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const uint64_t t = fdiv(tile, p.div_tpr);
+    const uint64_t seg = tile - t * p.tiles_per_row;
     const uint64_t o = fdiv(t, p.div_dout);
-    const int j = (int)(t - o * p.div_dout.d);
-    const int src = p.idx[j];
-    out[e] = src < 0 ? (T)0 : in[((int64_t)o * p.d_in + src) * p.inner + (int64_t)i];
+    const int src = p.idx[(int)(t - o * p.div_dout.d)];
+    const uint64_t v0 = seg * kTakeTile + threadIdx.x;
+    V* dst = out + t * p.row_v;
+    if (src < 0) {
+#pragma unroll
+      for (int u = 0; u < kTakeUnroll; ++u) {
+        const uint64_t v = v0 + (uint64_t)u * kTakeBlock;
+        if (v < p.row_v) dst[v] = V{};
+      }
+      continue;
+    }
+    const V* s = in + (o * (uint64_t)p.d_in + (uint64_t)src) * p.row_v;
+    V r[kTakeUnroll];
+#pragma unroll
+    for (int u = 0; u < kTakeUnroll; ++u) {
+      const uint64_t v = v0 + (uint64_t)u * kTakeBlock;
+      if (v < p.row_v) r[u] = s[v];
+    }
+#pragma unroll
+    for (int u = 0; u < kTakeUnroll; ++u) {
+      const uint64_t v = v0 + (uint64_t)u * kTakeBlock;
+      if (v < p.row_v) dst[v] = r[u];
+    }
+  }
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kTakeBlock) take_units_kernel(const __grid_constant__ TakeParams p) {
+  const V* __restrict__ in = static_cast<const V*>(p.in);
+  V* __restrict__ out = static_cast<V*>(p.out);
+  const uint64_t stride = (uint64_t)gridDim.x * kTakeBlock;
+  for (uint64_t e0 = (uint64_t)blockIdx.x * kTakeBlock + threadIdx.x; e0 < p.n_units;
+       e0 += stride * kTakeUnroll) {
+    V r[kTakeUnroll];
+#pragma unroll
+    for (int u = 0; u < kTakeUnroll; ++u) {
+      const uint64_t e = e0 + (uint64_t)u * stride;
+      r[u] = V{};
+      if (e < p.n_units) {
+        const uint64_t t = fdiv(e, p.div_rowv);
+        const uint64_t i = e - t * p.row_v;
+        const uint64_t o = fdiv(t, p.div_dout);
+        const int src = p.idx[(int)(t - o * p.div_dout.d)];
+        if (src >= 0) r[u] = in[(o * (uint64_t)p.d_in + (uint64_t)src) * p.row_v + i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kTakeUnroll; ++u) {
+      const uint64_t e = e0 + (uint64_t)u * stride;
+      if (e < p.n_units) out[e] = r[u];
+    }
   }
 }
 
@@ -270,21 +332,41 @@ extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t oute
   TakeParams p{};
   p.in = in;
   p.out = out;
-  p.n_out = (uint64_t)outer * d_out * inner;
-  p.div_inner = make_fastdiv((uint64_t)inner);
-  p.div_dout = make_fastdiv((uint64_t)d_out);
-  p.d_in = d_in;
-  p.inner = inner;
   for (int64_t j = 0; j < d_out; ++j) {
     if (idx[j] >= d_in || idx[j] < -1) return QSGB_ERR_INVALID;
     p.idx[j] = idx[j];
   }
-  const int block = 256;
+  const size_t esz = dtype == QSGB_F64 ? 8 : 4;
+  // 16-byte units when a row is a whole number of them and both tensors
+  // start on a 16-byte boundary
+  const bool wide = ((uint64_t)inner * esz) % 16 == 0 && (uintptr_t)in % 16 == 0 && (uintptr_t)out % 16 == 0;
+  const size_t usz = wide ? 16 : esz;
+  p.row_v = (uint64_t)inner * esz / usz;
+  p.n_rows = (uint64_t)outer * (uint64_t)d_out;
+  p.d_in = d_in;
+  p.div_dout = make_fastdiv((uint64_t)d_out);
   cudaStream_t s = as_stream(stream);
-  if (dtype == QSGB_F64)
-    take_kernel<double><<<grid_for(p.n_out, block), block, 0, s>>>(p);
-  else
-    take_kernel<float><<<grid_for(p.n_out, block), block, 0, s>>>(p);
+  const bool rows = p.row_v >= 128;
+  unsigned grid;
+  if (rows) {
+    p.tiles_per_row = (p.row_v + kTakeTile - 1) / kTakeTile;
+    p.div_tpr = make_fastdiv(p.tiles_per_row);
+    grid = grid_for(p.n_rows * p.tiles_per_row * kTakeBlock, kTakeBlock);
+  } else {
+    p.n_units = p.n_rows * p.row_v;
+    p.div_rowv = make_fastdiv(p.row_v);
+    grid = grid_for((p.n_units + kTakeUnroll - 1) / kTakeUnroll, kTakeBlock);
+  }
+  if (usz == 16) {
+    if (rows) take_rows_kernel<uint4><<<grid, kTakeBlock, 0, s>>>(p);
+    else take_units_kernel<uint4><<<grid, kTakeBlock, 0, s>>>(p);
+  } else if (usz == 8) {
+    if (rows) take_rows_kernel<unsigned long long><<<grid, kTakeBlock, 0, s>>>(p);
+    else take_units_kernel<unsigned long long><<<grid, kTakeBlock, 0, s>>>(p);
+  } else {
+    if (rows) take_rows_kernel<unsigned><<<grid, kTakeBlock, 0, s>>>(p);
+    else take_units_kernel<unsigned><<<grid, kTakeBlock, 0, s>>>(p);
+  }
   return launch_status();
 }
 
@@ -457,25 +539,69 @@ namespace {
 constexpr int64_t kNoAllocScratchDoubles = 16384;
 __device__ __align__(256) double g_noalloc_marg_scratch[kNoAllocScratchDoubles];
 
-// Device address of the array, looked up once per device (the name is only a
-// host-side stand-in for the symbol in host code).
+// Device address of the array, looked up once per device and CUDA context
+// (the name is only a host-side stand-in for the symbol in host code).  The
+// address belongs to the context the module was loaded in: after
+// cudaDeviceReset, or under another context made current through the driver
+// API, the lookup is done again.  Contexts are told apart by their driver
+// id, which is never reused within a process.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+struct NoAllocSlot {
+  unsigned long long ctx_id;
+  double* ptr;
+};
 std::mutex g_noalloc_mu;
-double* g_noalloc_ptr[64] = {nullptr};
+NoAllocSlot g_noalloc_slot[64] = {};
+
+// Driver id of the current context (0 if none is current or the driver
+// entry points are unavailable, in which case the address is looked up on
+// every call).
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 int noalloc_scratch(double** ptr) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return QSGB_ERR_CUDA;
   if (dev < 0 || dev >= 64) return QSGB_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_marg_scratch) != cudaSuccess || !p) {
-      cudaGetLastError();
-      return QSGB_ERR_CUDA;
-    }
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  const unsigned long long id = current_context_id();
+  NoAllocSlot& slot = g_noalloc_slot[dev];
+  if (id != 0 && slot.ptr && slot.ctx_id == id) {
+    *ptr = slot.ptr;
+    return QSGB_OK;
   }
-  *ptr = g_noalloc_ptr[dev];
+  // first call on this device (or in this context): the lookup loads the
+  // library's device module if needed, which reserves the array
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_marg_scratch) != cudaSuccess || !p) {
+    cudaGetLastError();
+    return QSGB_ERR_CUDA;
+  }
+  slot.ptr = static_cast<double*>(p);
+  slot.ctx_id = id != 0 ? id : current_context_id();  // a context now exists
+  *ptr = slot.ptr;
   return QSGB_OK;
 }
 

@@ -78,6 +78,28 @@ def assert_close_dot(actual, expected, absref, rtol=RTOL_F64, atol=0.0):
     assert worst <= 1.0, 'max error / bound = {:.3g}'.format(worst)
 
 
+def chain_rtol(units):
+    """Relative forward-error bound, against the |P| chain applied to |x|,
+    of applying `units` ((ptm, qudits) pairs) one after another, as the GPU
+    does and as the oracle does.
+
+    One application's row is a dot product of K = (PTM input size) terms.
+    On the GPU each term is formed in float-float: the input truncated to 47
+    significant bits, the PTM entry rounded to 48, the product error kept to
+    48 bits, one two-sum per term, and the row rounded once to double, so
+    the row's error is at most (K + 4) 2^-47 of sum_k |P_rk| |x_k|.  The
+    oracle's FP64 dot product adds K 2^-53 of the same sum, and a fused PTM
+    formed on the host in FP64 adds K 2^-53 of its |P| product.  An error
+    made at one unit reaches the output through the later PTMs, where it is
+    bounded by the |P| chain.  Summing over the units: sum_u (K_u + 4)
+    2^-46 bounds the whole chain."""
+    total = 0.0
+    for ptm, qudits in units:
+        k = int(np.prod(np.shape(ptm)[len(qudits):]))
+        total += (k + 4) * 2.0 ** -46
+    return total
+
+
 def assert_close_f64(actual, expected, rtol=RTOL_F64, atol=ATOL_F64):
     np.testing.assert_allclose(np.asarray(actual), np.asarray(expected),
                                rtol=rtol, atol=atol)

@@ -10,8 +10,8 @@ quantumsim/operations/operation.py:529-551, 600-604), and stores, per case,
 the input, the reference output, the bases' dimensions before and after,
 and the (ptm, qudits) units that ``quantumsim_gb300.circuit.units_of``
 extracts.
-It needs the reference source tree (default ``/root/reference``, or
-``$QUANTUMSIM_REF``) and the stand-ins in ``tests/golden/_stubs``; the file
+It needs the reference source tree (``$QUANTUMSIM_REF``, or
+``../reference`` beside the checkout) and the stand-ins in ``tests/golden/_stubs``; the file
 it writes is self-contained.
 
 Usage:  python tests/golden/make_circuit_golden.py
@@ -24,7 +24,11 @@ import warnings
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get('QUANTUMSIM_REF', '/root/reference')
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.refsrc import reference_tree  # noqa: E402
+REF = reference_tree()
+if REF is None:
+    sys.exit('reference source tree not found: set $QUANTUMSIM_REF')
 sys.path[:0] = [os.path.join(HERE, '_stubs'), REF]
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 warnings.simplefilter('ignore')

@@ -7,7 +7,7 @@ full qubit basis, a state in reshuffled subbases, and states a
 ``FinalizedCircuit`` produced from ``State``'s one-element starting bases.
 Stores each state's Pauli vector, its bases (vectors and labels), the
 operator strings and the reference's values.  It needs the
-reference source tree (default ``/root/reference``, or ``$QUANTUMSIM_REF``)
+reference source tree (``$QUANTUMSIM_REF``, or ``../reference`` beside the checkout)
 and the stand-ins in ``tests/golden/_stubs``; the file it writes is
 self-contained.
 
@@ -24,7 +24,11 @@ import warnings
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get('QUANTUMSIM_REF', '/root/reference')
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.refsrc import reference_tree  # noqa: E402
+REF = reference_tree()
+if REF is None:
+    sys.exit('reference source tree not found: set $QUANTUMSIM_REF')
 sys.path[:0] = [os.path.join(HERE, '_stubs'), REF]
 warnings.simplefilter('ignore')
 

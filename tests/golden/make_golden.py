@@ -3,7 +3,7 @@
 Runs the REFERENCE implementation (quantumsim's ``PauliVectorNumpy`` and its
 gate library) on seeded inputs and stores inputs and outputs in
 ``tests/golden/pauli_vector_golden.npz``.  It needs the reference source tree
-(default ``/root/reference``, or ``$QUANTUMSIM_REF``) and the stand-in
+(``$QUANTUMSIM_REF``, or ``../reference`` beside the checkout) and the stand-in
 modules in ``tests/golden/_stubs`` for quantumsim's optional imports
 (pytools, more_itertools, yaml, matplotlib).  The fixtures it writes are
 self-contained: tests read them without the reference.
@@ -19,7 +19,11 @@ import warnings
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get('QUANTUMSIM_REF', '/root/reference')
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.refsrc import reference_tree  # noqa: E402
+REF = reference_tree()
+if REF is None:
+    sys.exit('reference source tree not found: set $QUANTUMSIM_REF')
 sys.path[:0] = [os.path.join(HERE, '_stubs'), REF]
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 warnings.simplefilter('ignore')

@@ -6,7 +6,7 @@ import math
 
 import numpy as np
 
-from conftest import assert_close_dot
+from conftest import assert_close_dot, chain_rtol
 from oracle import pauli_vector_np as O
 from quantumsim_gb300 import circuit as C
 from quantumsim_gb300 import workloads
@@ -38,7 +38,7 @@ def test_fused_noisy_circuit_equals_unit_by_unit():
     # the fused products are formed in FP64: equal up to the rounding of a
     # chain of dot products
     assert_close_dot(_apply_all(pv, fused), _apply_all(pv, units),
-                     _abs_all(np.abs(pv), units) * 8)
+                     _abs_all(np.abs(pv), units), rtol=chain_rtol(units))
 
 
 def test_merge_rules():
@@ -102,7 +102,7 @@ def test_qutrit_units_fuse():
     assert len(fused) < len(units)
     pv = _rand_pv(rng, (9, 9, 9))
     assert_close_dot(_apply_all(pv, fused), _apply_all(pv, units),
-                     _abs_all(np.abs(pv), units) * 8)
+                     _abs_all(np.abs(pv), units), rtol=chain_rtol(units))
 
 
 # ------------------------------------------------ reference operation runs
@@ -131,7 +131,8 @@ def test_reference_operation_runs_reproduced_by_units_and_fusion():
         fused = C.plan(units)
         assert len(fused) <= len(units)
         assert_close_dot(_apply_all(x_in, fused), x_out,
-                         _abs_all(np.abs(x_in), units) * 8)
+                         _abs_all(np.abs(x_in), units),
+                         rtol=chain_rtol(units))
 
 
 def test_units_of_matches_reference_when_available():
@@ -140,8 +141,9 @@ def test_units_of_matches_reference_when_available():
     import os
     import sys
     import warnings
-    ref = os.environ.get('QUANTUMSIM_REF', '/root/reference')
-    if not os.path.isdir(os.path.join(ref, 'quantumsim')):
+    from oracle.refsrc import reference_tree
+    ref = reference_tree()
+    if ref is None:
         import pytest
         pytest.skip('reference source tree not present')
     here = os.path.join(os.path.dirname(__file__), 'golden')

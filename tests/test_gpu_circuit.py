@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import ATOL_F64, assert_close_dot
+from conftest import ATOL_F64, assert_close_dot, chain_rtol
 from oracle import pauli_vector_np as O
 import quantumsim_gb300 as qg
 from quantumsim_gb300 import bases as B
@@ -34,7 +34,7 @@ def test_fused_qubit_circuit_matches_oracle():
     s = qg.PauliVectorGB300([B.general(2)] * 8, pv0)
     circ(s)
     assert_close_dot(s.to_pv(), _seq(pv0, units),
-                     _seq(np.abs(pv0), units, True) * 8)
+                     _seq(np.abs(pv0), units, True), rtol=chain_rtol(units))
 
 
 def test_fused_qutrit_circuit_matches_oracle():
@@ -46,7 +46,7 @@ def test_fused_qutrit_circuit_matches_oracle():
     s = qg.PauliVectorGB300([B.general(3)] * 4, pv0)
     circ(s)
     assert_close_dot(s.to_pv(), _seq(pv0, units),
-                     _seq(np.abs(pv0), units, True) * 8)
+                     _seq(np.abs(pv0), units, True), rtol=chain_rtol(units))
 
 
 @pytest.mark.parametrize('dtype', [np.float64, np.float32])
@@ -68,7 +68,8 @@ def test_graph_replay_equals_eager(dtype):
         assert torch.equal(replay._data, eager._data)
         if dtype == np.float64:
             assert_close_dot(replay.to_pv(), _seq(pv0, units),
-                             _seq(np.abs(pv0), units, True) * 8)
+                             _seq(np.abs(pv0), units, True),
+                             rtol=chain_rtol(units))
     with pytest.raises(ValueError):
         graph.run(qg.PauliVectorGB300([B.general(2)] * 5, dtype=dtype))
 
@@ -99,8 +100,8 @@ def test_reference_operations_fused_on_gpu():
             # complex arithmetic that built them), which leaves entries made
             # only of such residue at 0 instead of ~1e-17
             assert_close_dot(s.to_pv(), x_out,
-                             _seq(np.abs(x_in), units, True) * 8,
-                             atol=ATOL_F64)
+                             _seq(np.abs(x_in), units, True),
+                             rtol=chain_rtol(units), atol=ATOL_F64)
 
 
 def test_parallel_preparation_then_apply():
@@ -120,7 +121,8 @@ def test_parallel_preparation_then_apply():
         circ(s)
         ref = _seq(pv0, units)
         if dtype == torch.float64:
-            assert_close_dot(s.to_pv(), ref, _seq(np.abs(pv0), units, True) * 8)
+            assert_close_dot(s.to_pv(), ref, _seq(np.abs(pv0), units, True),
+                             rtol=chain_rtol(units))
         else:
             np.testing.assert_allclose(s.to_pv(), ref, rtol=0,
                                        atol=1e-5 * np.abs(ref).max())

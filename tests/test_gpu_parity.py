@@ -11,10 +11,11 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import (ATOL_PROB, assert_close_dot, assert_close_f64,
-                      golden_bases, golden_cases)
+from conftest import (ATOL_F64, ATOL_PROB, RTOL_F64, assert_close_dot,
+                      assert_close_f64, golden_bases, golden_cases)
 from oracle import pauli_vector_np as O
 import quantumsim_gb300 as qg
+from quantumsim_gb300 import _lib as L
 from quantumsim_gb300 import bases as B
 from quantumsim_gb300 import ptm as P
 from quantumsim_gb300 import workloads
@@ -422,13 +423,92 @@ def test_float32_storage_probabilities():
     assert s.trace() == pytest.approx(o.trace(), abs=1e-6)
 
 
-def test_device_status_reports_out_of_range_values():
-    s = GB([B.general(2)] * 2, np.full((4, 4), 1e300))
-    s.apply_ptm(np.full((4, 4), 0.5), 0)   # multi-term rows -> df64 path
-    with pytest.raises(RuntimeError, match='range'):
-        s.to_pv()
-    s2 = GB([B.general(2)] * 2)
-    s2.to_pv()                              # status was cleared
+def _range_cases(rng):
+    """(bases, ptm, qudits) covering every kernel form: group pairs, single
+    groups (dense), vector accesses on the last qubit, staged qutrit tiles
+    (9x9 and 81x81 on the last qutrits) and component order (81x81)."""
+    t1, t2 = workloads.coherence_times(rng, 6)
+    q2 = [B.general(2)] * 6
+    q3 = [B.general(3)] * 4
+    return [
+        (q2, workloads.noisy_1q(rng, t1[0], t2[0]), (0,)),
+        (q2, workloads.noisy_1q(rng, t1[5], t2[5]), (5,)),
+        (q2, workloads.noisy_cz(rng, (1, 4), t1, t2), (1, 4)),
+        (q2, workloads.noisy_cz(rng, (5, 4), t1, t2), (5, 4)),
+        (q2, P.compose(P.cphase(0.7),
+                       P.kron(P.rotate('x', 0.3), P.rotate('y', 1.1))).numpy(),
+         (2, 3)),
+        (q3, workloads.qutrit_1q(rng), (3,)),
+        (q3, workloads.qutrit_2q(rng), (2, 3)),
+        (q3, workloads.qutrit_2q(rng), (0, 2)),
+    ]
+
+
+@pytest.mark.parametrize("scale", [1e300, 1e-300, 1e-35, 1e-40])
+def test_full_double_range_matches_oracle(scale):
+    """States whose entries lie far outside the float-float range (near
+    1e300, 1e-300, and just below the float pair's 2^-102 floor) give the
+    oracle's result under arith='auto': the kernels recompute such items in
+    native FP64 instead of failing.  Checked per entry at 1e-12 relative,
+    with the absolute floor scaled with the state."""
+    rng = np.random.default_rng(91)
+    for bases, ptm, qs in _range_cases(rng):
+        shape = tuple(b.dim_pauli for b in bases)
+        pv = rand_pv(rng, shape) * scale
+        ref = O.apply_ptm(pv, ptm, *qs)
+        for jit in (True, False):
+            s = GB(bases, pv)
+            s._data = torch.ops.qsgb.apply_ptm(
+                s._data, torch.from_numpy(np.ascontiguousarray(ptm)),
+                list(qs), L.ARITH_AUTO, 0, False, jit)
+            np.testing.assert_allclose(s.to_pv(), ref, rtol=RTOL_F64,
+                                       atol=ATOL_F64 * scale)
+
+
+def test_mixed_magnitudes_in_one_group():
+    """One group holding entries of 1e300, 1, 1e-300 and 0: the items that
+    hold them run in FP64, every other item in float-float, and the whole
+    result matches the oracle per entry."""
+    rng = np.random.default_rng(92)
+    t1, t2 = workloads.coherence_times(rng, 5)
+    ptm = workloads.noisy_cz(rng, (1, 3), t1, t2)
+    pv = rand_pv(rng, (4,) * 5)
+    pv[0, 1, 0, 2, 0] = 1e300
+    pv[0, 2, 0, 3, 0] = -3e-300
+    pv[0, 3, 0, 1, 0] = 0.0
+    pv[1, 0, 1, 1, 1] = 7e-310            # a subnormal double
+    ref = O.apply_ptm(pv, ptm, 1, 3)
+    s = GB([B.general(2)] * 5, pv)
+    s.apply_ptm(ptm, 1, 3)
+    got = s.to_pv()
+    np.testing.assert_allclose(got, ref, rtol=RTOL_F64, atol=0)
+
+
+@pytest.mark.parametrize('dtype', [torch.float64, torch.float32])
+def test_take_axis_bit_exact_every_axis(dtype):
+    """reduce_basis / project as a copy of rows: every axis of a mixed
+    qutrit/qubit tensor (long rows in 16-byte units, short rows unit by
+    unit), aligned and 4/8-byte-offset tensors, and -1 entries (zeros);
+    bit-exact against numpy's take."""
+    rng = np.random.default_rng(71)
+    shape = (9, 3, 9, 4, 9, 9)
+    host = rng.standard_normal(shape)
+    for off in (0, 1):
+        buf = torch.empty(int(np.prod(shape)) + 1, dtype=dtype,
+                          device='cuda')
+        x = buf[off:off + int(np.prod(shape))].view(shape)
+        x.copy_(torch.from_numpy(host).to(dtype))
+        ref_host = x.cpu().numpy()
+        for axis, d in enumerate(shape):
+            for idx in ([0, d // 2, d - 1], [d - 1], [-1, 1] if d > 1
+                        else [0]):
+                got = torch.ops.qsgb.take_axis(x, axis, idx).cpu().numpy()
+                exp = np.take(ref_host, [max(i, 0) for i in idx], axis=axis)
+                if -1 in idx:
+                    sl = [slice(None)] * len(shape)
+                    sl[axis] = [j for j, i in enumerate(idx) if i < 0]
+                    exp[tuple(sl)] = 0
+                np.testing.assert_array_equal(got, exp)
 
 
 # ---------------------------------------------------------------- full size

@@ -49,41 +49,66 @@ def _marginals_noalloc(lib, diag, shape, axis, stream):
     return out
 
 
-def test_noalloc_marginals_match_scratch_version_twice():
+@pytest.fixture(scope='module')
+def lib_and_stream():
+    """The library, built if needed, with cuda:0 current (so each test also
+    runs on its own in a fresh process)."""
     qbuild.build()
     lib = L.load()
-    assert lib.qsgb_marginals_noalloc_max_scratch_bytes() == 16384 * 8
     dev = torch.device('cuda', 0)
     torch.cuda.set_device(dev)
     stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    return lib, dev, stream
+
+
+def _check_against_both(lib, dev, stream, probs, shape, ax):
+    diag = torch.from_numpy(probs).to(dev)
+    got = _marginals_noalloc(lib, diag, shape, ax, stream)
+    ref = _marginals_with_scratch(lib, diag, shape, ax, stream)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(got.cpu().numpy(), ref.cpu().numpy(),
+                               rtol=0, atol=ATOL_PROB)
+    expect = (probs.reshape(shape).sum(axis=tuple(
+        i for i in range(len(shape)) if i != ax))
+        if ax >= 0 else np.array([probs.sum()]))
+    np.testing.assert_allclose(got.cpu().numpy(), expect, rtol=0,
+                               atol=ATOL_PROB)
+
+
+def test_noalloc_marginals_match_scratch_version_twice(lib_and_stream):
+    lib, dev, stream = lib_and_stream
+    assert lib.qsgb_marginals_noalloc_max_scratch_bytes() == 16384 * 8
     rng = np.random.default_rng(2024)
     calls = [([2] * 14, 5), ([3, 2, 3, 3, 2, 3, 3], 2)]  # two calls in a row
     for shape, axis in calls:
         probs = rng.random(int(np.prod(shape)))
         probs /= probs.sum()
-        diag = torch.from_numpy(probs).to(dev)
         for ax in (axis, -1):
-            got = _marginals_noalloc(lib, diag, shape, ax, stream)
-            ref = _marginals_with_scratch(lib, diag, shape, ax, stream)
-            torch.cuda.synchronize()
-            np.testing.assert_allclose(got.cpu().numpy(), ref.cpu().numpy(),
-                                       rtol=0, atol=ATOL_PROB)
-            expect = (probs.reshape(shape).sum(axis=tuple(
-                i for i in range(len(shape)) if i != ax))
-                if ax >= 0 else np.array([probs.sum()]))
-            np.testing.assert_allclose(got.cpu().numpy(), expect, rtol=0,
-                                       atol=ATOL_PROB)
+            _check_against_both(lib, dev, stream, probs, shape, ax)
 
 
-def test_noalloc_rejects_requests_beyond_the_fixed_array():
-    lib = L.load()
-    dev = torch.device('cuda', 0)
-    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
-    # 20000 outcomes on one axis need 20000 partial sums > 16384
-    shape = [20000, 2]
-    diag = torch.zeros(40000, dtype=torch.float64, device=dev)
-    out = torch.empty(20000, dtype=torch.float64, device=dev)
-    st = lib.qsgb_marginals_noalloc(ctypes.c_void_p(diag.data_ptr()), 2,
-                                    L.i64_array(shape), 0,
-                                    ctypes.c_void_p(out.data_ptr()), stream)
-    assert st == L.ERR_SCRATCH
+def test_noalloc_accepts_exactly_the_fixed_array(lib_and_stream):
+    """Requests that need exactly 16384 partial sums still run: one chunk
+    of 16384 outcomes, and 32 outcomes of 2^21 entries each (512 chunks of
+    4096, the documented limit for qudits of up to 32 levels)."""
+    lib, dev, stream = lib_and_stream
+    rng = np.random.default_rng(7)
+    for shape, ax in (([16384], 0), ([1 << 21, 32], 1)):
+        probs = rng.random(int(np.prod(shape)))
+        probs /= probs.sum()
+        _check_against_both(lib, dev, stream, probs, shape, ax)
+
+
+def test_noalloc_rejects_requests_beyond_the_fixed_array(lib_and_stream):
+    lib, dev, stream = lib_and_stream
+    # 16385 outcomes on one axis need 16385 partial sums > 16384; so do
+    # 20000 outcomes of two entries each
+    for shape in ([16385], [20000, 2]):
+        n = int(np.prod(shape))
+        diag = torch.zeros(n, dtype=torch.float64, device=dev)
+        out = torch.empty(shape[0], dtype=torch.float64, device=dev)
+        st = lib.qsgb_marginals_noalloc(ctypes.c_void_p(diag.data_ptr()),
+                                        len(shape), L.i64_array(shape), 0,
+                                        ctypes.c_void_p(out.data_ptr()),
+                                        stream)
+        assert st == L.ERR_SCRATCH
