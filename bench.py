@@ -335,7 +335,10 @@ def run_gb300(args):
         # the same launches with each arithmetic forced
         cz = workloads.noisy_cz(rng, (3, 7), t1, t2)
         r1 = workloads.noisy_1q(rng, t1[5], t2[5])
-        for arith in ('f64', 'df64', 'auto'):
+        for pair in [(0, 1), (12, 13), (13, 0), (6, 11)]:
+            per_target['2q_dense_{}_{}'.format(*pair)] = _time_app(
+                s, dense, pair, bytes_per_app)
+        for arith in ('f64', 'df64', 'auto', 'tc'):
             s._arith_key, s._arith = arith, qops_arith(arith)
             per_target['arith_{}_2q_cz_3_7'.format(arith)] = _time_app(
                 s, cz, (3, 7), bytes_per_app)
@@ -496,9 +499,13 @@ def run_qutrit_config():
     res['fused_final_trace'] = tr_f
     res['fused_max_abs_diff'] = float(np.abs(s.to_pv() - x_unfused).max())
     s = qg.PauliVectorGB300([bases.general(3)] * 8, force=True)
+    s._data.copy_(torch.rand_like(s._data) * 2.0 ** -12)
+    dense81 = rng.standard_normal((9, 9, 9, 9)) / 9
     for name, ptm, qs in (('9x9_q4', workloads.qutrit_1q(rng), (4,)),
                           ('81x81_q2_q5', workloads.qutrit_2q(rng), (2, 5)),
-                          ('81x81_q7_q6', workloads.qutrit_2q(rng), (7, 6))):
+                          ('81x81_q7_q6', workloads.qutrit_2q(rng), (7, 6)),
+                          # a dense 81x81 (6561 terms): the generic kernel
+                          ('81x81_dense_q2_q5', dense81, (2, 5))):
         res[name + '_gbs'] = _time_app(s, ptm, qs, nbytes)
     return res
 

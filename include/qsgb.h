@@ -52,6 +52,12 @@ extern "C" {
                               pipes; single-term rows use one FP64 multiply */
 #define QSGB_ARITH_F64 2   /* native FP64 FMA (exact IEEE, slow on GB300) */
 #define QSGB_ARITH_F32 3   /* FP32 FMA (F32 storage only) */
+#define QSGB_ARITH_TC 4    /* F64 storage: every dense-shaped 16 x 16 host
+                              PTM (two full-basis qubits) on the tensor
+                              cores (FP64 values split into FP16 digit
+                              planes, exact FP32 sums); other PTMs as AUTO.
+                              AUTO itself sends 16 x 16 host PTMs with more
+                              than 5 non-zero terms per row there */
 
 /* ---- PTM layout flags ---- */
 #define QSGB_PTM_SWAPPED 1    /* 2-qudit PTM given in order (less significant,
@@ -230,6 +236,27 @@ int qsgb_marginals(const double* diag, int ndim, const int64_t* shape,
 int64_t qsgb_marginals_noalloc_max_scratch_bytes(void);
 int qsgb_marginals_noalloc(const double* diag, int ndim, const int64_t* shape,
                            int axis, double* out, void* stream);
+
+/*
+ * Marginals of the DM diagonal read straight from the Pauli vector: the
+ * diagonal is the multitake of qsgb_gather (same host index lists; -1
+ * selects a zero), and out[j] = sum of its entries whose index along `axis`
+ * is j (j < number of indices of `axis`), or out[0] = the trace for
+ * axis == -1.  One launch, deterministic, FP64 accumulation for FP64 and
+ * FP32 vectors.  out[n_out] receives the value of the device status word
+ * *dev_status (0 when dev_status is NULL) as it stands when the kernel runs,
+ * so a single device-to-host copy of n_out + 1 doubles returns the result
+ * and every earlier kernel's status bits.  Diagonals of at most 2^22 entries
+ * and axes of at most 64 indices; larger ones return QSGB_ERR_UNSUPPORTED
+ * (use qsgb_gather and qsgb_marginals).
+ * Replaces: cuda.py:347-384 (trace and meas_prob: multitake, then a host
+ * sum or one ReductionKernel launch and device sync per outcome) and
+ * numpy.py:82-84, 97-107.
+ */
+int qsgb_diag_marginals(const void* in, int in_dtype, int ndim,
+                        const int64_t* in_shape, const int32_t* idx_off,
+                        const int32_t* idx, int axis, double* out,
+                        const unsigned* dev_status, void* stream);
 
 /*
  * Partial trace: out[kept...] = sum over traced qudits t of

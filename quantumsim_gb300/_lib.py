@@ -26,6 +26,7 @@ ARITH_AUTO = 0
 ARITH_DF64 = 1
 ARITH_F64 = 2
 ARITH_F32 = 3
+ARITH_TC = 4
 
 PTM_SWAPPED = 1
 PTM_TRANSPOSED = 2
@@ -57,6 +58,9 @@ SIGNATURES = {
                                    _i64]),
     'qsgb_gather': (_int, [_c_void_p, _c_void_p, _int, _int, _int, _p_i64,
                            _p_i32, _p_i32, _c_void_p]),
+    'qsgb_diag_marginals': (_int, [_c_void_p, _int, _int, _p_i64, _p_i32,
+                                   _p_i32, _int, _c_void_p, _c_void_p,
+                                   _c_void_p]),
     'qsgb_take_axis': (_int, [_c_void_p, _c_void_p, _int, _i64, _i64, _i64,
                               _p_i32, _i64, _c_void_p]),
     'qsgb_marginals_scratch_bytes': (_i64, [_i64, _i64]),

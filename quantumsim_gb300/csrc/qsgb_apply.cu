@@ -38,7 +38,9 @@
 
 #include "qsgb_common.cuh"
 #include "qsgb_jit.h"
+#include "qsgb_tc.h"
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -589,6 +591,40 @@ int launch_apply(ApplyParams& p, cudaStream_t stream) {
 // ---------------------------------------------------------------------------
 // Returns QSGB_ERR_UNSUPPORTED when the specialised path does not apply.
 // prepare_only: compile (or fetch) the kernel, launch nothing.
+// Op matrix M[r][k] (rows (ra, rb), columns (ka, kb), qudit a first) of a
+// PTM stored in `layout` (QSGB_PTM_SWAPPED / QSGB_PTM_TRANSPOSED bits).
+void op_matrix(const double* ptm, int da_out, int db_out, int da_in, int db_in, int layout, double* m) {
+  const int kin = da_in * db_in, kout = da_out * db_out;
+  for (int r = 0; r < kout; ++r)
+    for (int k = 0; k < kin; ++k) {
+      const int ra = r / db_out, rb = r % db_out, ka = k / db_in, kb = k % db_in;
+      int idx;
+      switch (layout & 3) {
+        case 0: idx = r * kin + k; break;
+        case QSGB_PTM_SWAPPED: idx = ((rb * da_out + ra) * db_in + kb) * da_in + ka; break;
+        case QSGB_PTM_TRANSPOSED: idx = k * kout + r; break;
+        default: idx = ((kb * da_in + ka) * db_out + rb) * da_out + ra; break;
+      }
+      m[r * kin + k] = ptm[idx];
+    }
+}
+
+// Under QSGB_ARITH_AUTO, a 16 x 16 PTM goes to the tensor cores when its
+// rows average more non-zero terms (above 2^-52 of the largest entry) than
+// QSGB_TC_MIN_TERMS (default 5): below that the specialised float-float
+// kernels stream at close to the HBM rate.
+bool tc_wanted(const double* op) {
+  static const double min_terms = [] {
+    const char* v = std::getenv("QSGB_TC_MIN_TERMS");
+    return v ? std::atof(v) : 5.0;
+  }();
+  double amax = 0.0;
+  for (int i = 0; i < 256; ++i) amax = std::max(amax, std::fabs(op[i]));
+  int n = 0;
+  for (int i = 0; i < 256; ++i) n += std::fabs(op[i]) > amax * 0x1p-52 ? 1 : 0;
+  return n > min_terms * 16.0;
+}
+
 // mode: kLaunch, kPrepare (compile and load, launch nothing) or kCompileOnly
 // (generate and compile the source, no device needed; *src_out gets it).
 enum { kLaunch = 0, kPrepare = 1, kCompileOnly = 2 };
@@ -668,7 +704,11 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   if (kin > kMaxK || kout > kMaxK || kin * kout > kMaxEntries) return QSGB_ERR_UNSUPPORTED;
   if (max_terms < 1 || max_terms > kin * kout) max_terms = kin * kout;
   if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
-  if (arith < QSGB_ARITH_AUTO || arith > QSGB_ARITH_F32) return QSGB_ERR_INVALID;
+  if (arith < QSGB_ARITH_AUTO || arith > QSGB_ARITH_TC) return QSGB_ERR_INVALID;
+  if (arith == QSGB_ARITH_TC && dtype != QSGB_F64) return QSGB_ERR_INVALID;
+  // dense 16 x 16 host PTMs on FP64 vectors: the tensor-core kernel
+  const int tc_arith = arith;
+  if (arith == QSGB_ARITH_TC) arith = QSGB_ARITH_AUTO;
   if (dtype == QSGB_F32 && arith == QSGB_ARITH_AUTO) arith = QSGB_ARITH_F32;
   if (dtype == QSGB_F32 && arith != QSGB_ARITH_F32) return QSGB_ERR_INVALID;
   if (dtype == QSGB_F64 && arith == QSGB_ARITH_F32) return QSGB_ERR_INVALID;
@@ -702,6 +742,15 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.div_z = make_fastdiv((uint64_t)(pair ? Z / 2 : Z));
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
+  // 0. dense 16 x 16 PTMs (two full-basis qubits) on the tensor cores
+  if (dtype == QSGB_F64 && (flags & QSGB_PTM_HOST) && da_in == 4 && db_in == 4 && da_out == 4 && db_out == 4) {
+    double op[256];
+    op_matrix(ptm, 4, 4, 4, 4, flags & 3, op);
+    if (tc::eligible(op, 16, 16) && (tc_arith == QSGB_ARITH_TC || (tc_arith == QSGB_ARITH_AUTO && tc_wanted(op)))) {
+      if (mode != kLaunch) return QSGB_ERR_UNSUPPORTED;  // precompiled: nothing to prepare
+      return tc::launch(op, in, out, (uint64_t)X, (uint64_t)Y, (uint64_t)Z, status, s);
+    }
+  }
   // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)
   const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s, mode, src_out);
   if (js != QSGB_ERR_UNSUPPORTED || mode != kLaunch) return js;

@@ -26,8 +26,12 @@ __device__ __forceinline__ qsgb_u64 qsgb_fdiv(qsgb_u64 n, qsgb_u64 m, int l) {
 
 // Split an IEEE double into hi + lo floats with integer operations only (the
 // FP64<->FP32 converters run on the slow FP64 pipe on GB300).  hi keeps the
-// top 24 significant bits (truncated), lo the next 23 bits, so hi + lo agrees
-// with x to 2^-47 relative.  Inputs the float pair cannot carry to that
+// top 24 significant bits (truncated), lo the next 23 bits rounded to
+// nearest on the 24th, so hi + lo agrees with x to 2^-47 relative, with an
+// error of either sign: a truncated lo would shrink every input by 2^-48 on
+// average, and that bias accumulates linearly over a long circuit (1050
+// applications: ~1e-12 relative) where unbiased errors grow as a square
+// root.  Inputs the float pair cannot carry to that
 // precision set `bad`: a non-zero |x| < 2^-102 (|x| < 2^-126 flushes to 0,
 // [2^-126, 2^-102) keeps only hi) and |x| >= 2^128, inf and nan (which give
 // nan).  Callers recompute the affected results in native FP64.
@@ -41,7 +45,9 @@ __device__ __forceinline__ void qsgb_split_f64(double x, float& hi, float& lo, u
   const unsigned t = __funnelshift_l(l, h, 3);
   const unsigned hb = ((t & 0x7fffffffu) ^ 0x40000000u) | sgn;
   const unsigned base = (hb & 0xff800000u) - (23u << 23);  // weight of m[28] is 2^(E-24)
-  const unsigned lb = base | ((l >> 6) & 0x7fffffu);
+  // m[28:6] rounded on m[5]: 0 .. 2^23, added (not or-ed) to base so that a
+  // carry out of the 23 bits lands in base's exponent (still exact)
+  const unsigned lb = base + ((l >> 6) & 0x7fffffu) + ((l >> 5) & 1u);
   const float lo_full = __uint_as_float(lb) - __uint_as_float(base);
   const bool in_range = (e - 897u) <= 253u;  // 897 <= e <= 1150
   const bool has_lo = e >= 920u;

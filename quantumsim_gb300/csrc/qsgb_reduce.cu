@@ -191,6 +191,58 @@ __global__ void marg_stage2(const double* __restrict__ part, int nchunks, double
   if (threadIdx.x == 0) out[j] = r;
 }
 
+// ------------------------------------------------ diagonal marginals, fused
+// Marginals of the DM diagonal read straight from the Pauli vector through
+// the multitake plan (no diagonal tensor): one block, outcome by outcome,
+// fixed-order reduction.  out[j] for j < n_out, then out[n_out] = the device
+// status word (so one device-to-host copy returns both).
+struct DiagRedParams {
+  const void* in;
+  double* out;
+  const unsigned* status;
+  int in_dtype;
+  int ndim;
+  int axis;        // -1: trace
+  int n_out;       // 1 for the trace, else the Hilbert dim of `axis`
+  uint64_t per_j;  // diagonal entries per outcome
+  FastDiv div_s;   // entries of the diagonal index after `axis`
+  uint64_t s_axis;
+  FastDiv div[kMaxDim];  // Hilbert dims per axis (diagonal index space)
+  int64_t in_stride[kMaxDim];
+  int idx_off[kMaxDim + 1];
+  int idx[kMaxIdx];
+};
+
+constexpr int kDiagRedBlock = 1024;
+
+__global__ void __launch_bounds__(kDiagRedBlock) diag_marginals_kernel(const __grid_constant__ DiagRedParams p) {
+  __shared__ double sh[32];
+  const uint64_t d_axis = p.axis < 0 ? 1 : p.div[p.axis].d;
+  for (int j = 0; j < p.n_out; ++j) {
+    double acc = 0.0;
+    for (uint64_t m = threadIdx.x; m < p.per_j; m += kDiagRedBlock) {
+      // m-th diagonal entry whose index along `axis` is j
+      const uint64_t hi = fdiv(m, p.div_s);
+      const uint64_t lo = m - hi * p.s_axis;
+      uint64_t rem = (hi * d_axis + (uint64_t)j) * p.s_axis + lo;
+      int64_t addr = 0;
+      bool zero = false;
+      for (int a = p.ndim - 1; a >= 0; --a) {
+        const uint64_t q = fdiv(rem, p.div[a]);
+        const int i = (int)(rem - q * p.div[a].d);
+        rem = q;
+        const int k = p.idx[p.idx_off[a] + i];
+        zero |= k < 0;
+        addr += (int64_t)(k < 0 ? 0 : k) * p.in_stride[a];
+      }
+      if (!zero) acc += load_f64(p.in, addr, p.in_dtype);
+    }
+    const double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) p.out[j] = r;
+  }
+  if (threadIdx.x == 0) p.out[p.n_out] = p.status ? (double)*p.status : 0.0;
+}
+
 // ---------------------------------------------------------------- partial trace
 constexpr int kMaxPtEntries = 1024;
 
@@ -367,6 +419,47 @@ extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t oute
     if (rows) take_rows_kernel<unsigned><<<grid, kTakeBlock, 0, s>>>(p);
     else take_units_kernel<unsigned><<<grid, kTakeBlock, 0, s>>>(p);
   }
+  return launch_status();
+}
+
+extern "C" int qsgb_diag_marginals(const void* in, int in_dtype, int ndim, const int64_t* in_shape,
+                                   const int32_t* idx_off, const int32_t* idx, int axis, double* out,
+                                   const unsigned* dev_status, void* stream) {
+  if (!in || !out || !idx_off || (ndim > 0 && (!in_shape || !idx))) return QSGB_ERR_INVALID;
+  if (in_dtype != QSGB_F64 && in_dtype != QSGB_F32) return QSGB_ERR_INVALID;
+  if (ndim < 0 || ndim > kMaxDim || axis < -1 || axis >= ndim) return QSGB_ERR_INVALID;
+  if (idx_off[0] != 0 || idx_off[ndim] > kMaxIdx) return QSGB_ERR_UNSUPPORTED;
+  DiagRedParams p{};
+  p.in = in;
+  p.out = out;
+  p.status = dev_status;
+  p.in_dtype = in_dtype;
+  p.ndim = ndim;
+  p.axis = axis;
+  uint64_t n = 1, s_axis = 1;
+  int64_t stride = 1;
+  for (int a = ndim - 1; a >= 0; --a) {
+    const int len = idx_off[a + 1] - idx_off[a];
+    if (len < 1 || in_shape[a] < 1) return QSGB_ERR_INVALID;
+    for (int i = idx_off[a]; i < idx_off[a + 1]; ++i)
+      if (idx[i] >= in_shape[a] || idx[i] < -1) return QSGB_ERR_INVALID;
+    p.div[a] = make_fastdiv((uint64_t)len);
+    p.in_stride[a] = stride;
+    stride *= in_shape[a];
+    if (axis >= 0 && a > axis) s_axis *= (uint64_t)len;
+    n *= (uint64_t)len;
+  }
+  // one block: diagonals of up to 2^22 entries (prod of Hilbert dims)
+  if (n > (1ull << 22)) return QSGB_ERR_UNSUPPORTED;
+  const uint64_t d = axis < 0 ? 1 : (uint64_t)(idx_off[axis + 1] - idx_off[axis]);
+  if (d > 64) return QSGB_ERR_UNSUPPORTED;
+  p.n_out = (int)d;
+  p.per_j = n / d;
+  p.s_axis = axis < 0 ? 1 : s_axis;
+  p.div_s = make_fastdiv(p.s_axis);
+  for (int a = 0; a <= ndim; ++a) p.idx_off[a] = idx_off[a];
+  for (int i = 0; i < idx_off[ndim]; ++i) p.idx[i] = idx[i];
+  diag_marginals_kernel<<<1, kDiagRedBlock, 0, as_stream(stream)>>>(p);
   return launch_status();
 }
 

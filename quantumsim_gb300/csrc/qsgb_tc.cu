@@ -1,0 +1,329 @@
+// Dense two-qubit PTMs (16 x 16, FP64 storage) on the tensor cores.
+//
+// A dense PTM row has 16 terms: in float-float on the FP32 pipes that is
+// ~12 instructions per term, and the kernel is bound by instruction issue at
+// a quarter of the HBM rate; in native FP64 it is bound by the FP64 pipe
+// (~0.6 T FMA/s on GB300).  This kernel computes the contraction exactly
+// enough for FP64 parity on the FP16 tensor cores instead, with an
+// error-free splitting in the spirit of the Ozaki scheme (Ozaki, Ogita,
+// Oishi and Rump, "Error-free transformations of matrix multiplication by
+// using fast routines of matrix multiplication and its applications",
+// Numer. Algorithms 59, 2012):
+//
+//  * Each group of 16 inputs (one bystander index) is scaled by its largest
+//    binary exponent and written as a signed fixed-point integer F of 57
+//    bits plus sign (|F| < 2^57), with integer operations on the double's
+//    bit pattern.  F + B, for B = 512 * sum_j 2^(10 j), is a non-negative
+//    60-bit integer whose six base-1024 digits v_j give F = sum_j (v_j - 512)
+//    2^(10 (5 - j)): six balanced digits d_j in [-512, 512), each exactly an
+//    FP16 number (|d_0| <= 128).
+//  * Each PTM row is split the same way on the host (per-row scale).
+//  * For every pair of digit planes (i, j) with i + j <= 5 one
+//    mma.sync.m16n8k16 (FP16 operands, FP32 accumulation) adds
+//    sum_k e_ik d_jk to the accumulator of level L = i + j.  A product of two
+//    digits is at most 2^18, a pair's K = 16 sum at most 2^22, and a level
+//    holds at most four such sums below 2^24, where FP32 sums of integers
+//    are exact; levels 4 and 5 may round their last bit, 2^-40 below level 0.
+//  * The six level sums are combined in 64-bit integer arithmetic,
+//    V = sum_L A_L 2^(10 (4 - L)), converted to double once and scaled by
+//    2^(Ex + Ep_r - 54) on the exponent field.
+//
+// The dropped levels (i + j >= 6) and the 57-bit truncation of inputs and
+// PTM entries bound the error by about 2^-47.7 * max_k |P_rk| * max_k |x_k|
+// of the row and group (4.4e-15 of that product), against 16 * 2^-53 *
+// sum_k |P_rk| |x_k| for an FP64 dot product.  Groups whose inputs hold inf,
+// nan, or whose results leave the normal double range are recomputed in
+// native FP64 by the same warp.
+//
+// Work mapping: a warp takes tiles of 8 groups (the N of the MMA).  Lane
+// (g, c) = (lane / 4, lane % 4) loads inputs k in {2c, 2c+1, 2c+8, 2c+9} of
+// group g (the B fragment layout of m16n8k16), and ends with outputs rows
+// {g, g+8} of groups {2c, 2c+1} (the accumulator layout).  The PTM digit
+// planes (the A fragments) are loaded into registers once per warp.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "qsgb_common.cuh"
+#include "qsgb_tc.h"
+
+namespace qsgb {
+namespace tc {
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ void mma16816(float* d, const unsigned* a, const unsigned* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Biased exponent of x as used for scaling (subnormals and zero count as 1)
+// and its 53-bit significand (implicit bit included for normal numbers).
+__device__ __forceinline__ unsigned exp_eff(unsigned hi) {
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  return e == 0u ? 1u : e;
+}
+
+// F + B for input x = (hi, lo) against group exponent emax (biased, >= e):
+// F = sign(x) * (m << 4) >> (emax - e), |F| < 2^57.
+__device__ __forceinline__ unsigned long long fixed_biased(unsigned hi, unsigned lo, unsigned emax) {
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  const unsigned mh = (hi & 0xfffffu) | (e != 0u ? 0x100000u : 0u);
+  const unsigned long long m = ((unsigned long long)mh << 32 | lo) << 4;
+  const unsigned s = emax - (e == 0u ? 1u : e);
+  unsigned long long f = s < 64u ? (m >> s) : 0ull;
+  if (hi & 0x80000000u) f = 0ull - f;
+  return f + kDigitBias;
+}
+
+// FP16x2 register of digit plane j (bit position p = 10 (5 - j)) of two
+// inputs: (v_a - 512, v_b - 512) built from 0x6400 | v = 1024 + v.
+__device__ __forceinline__ unsigned digit_pair(unsigned long long ua, unsigned long long ub, int p) {
+  const unsigned a = (unsigned)(ua >> p) & 0x3ffu;
+  const unsigned b = (unsigned)(ub >> p) & 0x3ffu;
+  const unsigned r = a | (b << 16) | 0x64006400u;
+  unsigned out;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(out) : "r"(r), "r"(0x66006600u));  // - (1536, 1536)
+  return out;
+}
+
+// 2^sc * sum_L A_L 2^(10 (4 - L)); bad |= 1 when the result is not a normal
+// double (or zero).
+__device__ __forceinline__ double combine(const float (&acc)[kDigits][4], int s, int sc, unsigned& bad) {
+  long long v = (long long)__float2int_rn(acc[0][s]) << 40;
+  v += (long long)__float2int_rn(acc[1][s]) << 30;
+  v += (long long)__float2int_rn(acc[2][s]) << 20;
+  v += (long long)__float2int_rn(acc[3][s]) << 10;
+  v += (long long)__float2int_rn(acc[4][s]);
+  v += (long long)(__float2int_rn(acc[5][s]) >> 10);
+  if (v == 0) return 0.0;
+  const double d = __ll2double_rn(v);
+  const int hi = __double2hiint(d);
+  const int e = ((hi >> 20) & 0x7ff) + sc;
+  bad |= (e < 1 || e > 2046) ? 1u : 0u;
+  return __hiloint2double(hi + (sc << 20), __double2loint(d));
+}
+
+template <bool CONTIG>
+__global__ void __launch_bounds__(kBlock) apply16_tc_kernel(const __grid_constant__ TcParams p) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane >> 2, c = lane & 3;
+  const int warps = kBlock / 32;
+  // A fragments of every digit plane: rows {g, g+8}, columns {2c, 2c+1} and
+  // {2c+8, 2c+9}
+  unsigned A[kDigits][4];
+#pragma unroll
+  for (int i = 0; i < kDigits; ++i) {
+    const unsigned short* d = &p.digits[i][0][0];
+    A[i][0] = d[g * 16 + 2 * c] | ((unsigned)d[g * 16 + 2 * c + 1] << 16);
+    A[i][1] = d[(g + 8) * 16 + 2 * c] | ((unsigned)d[(g + 8) * 16 + 2 * c + 1] << 16);
+    A[i][2] = d[g * 16 + 2 * c + 8] | ((unsigned)d[g * 16 + 2 * c + 9] << 16);
+    A[i][3] = d[(g + 8) * 16 + 2 * c + 8] | ((unsigned)d[(g + 8) * 16 + 2 * c + 9] << 16);
+  }
+  const int rsc0 = p.row_exp[g], rsc1 = p.row_exp[g + 8];
+  // this lane's inputs k = (ka, kb): 2c -> (c/2, 2(c%2)), +1 -> kb + 1,
+  // +8 -> ka + 2
+  const int ka = c >> 1, kb = 2 * (c & 1);
+  const int64_t in_off0 = ka * p.sai + kb * p.sbi;
+  const int64_t in_off2 = in_off0 + 2 * p.sai;
+  // this lane's outputs: rows g = (g/4, g%4) and g + 8 = (g/4 + 2, g%4)
+  const int64_t out_off0 = (g >> 2) * p.sao + (g & 3) * p.sbo;
+  const int64_t out_off1 = out_off0 + 2 * p.sao;
+
+  auto base = [&](uint64_t grp, int64_t sx, int64_t sy) -> int64_t {
+    const uint64_t t1 = fdiv(grp, p.div_z);
+    const uint64_t z = grp - t1 * p.div_z.d;
+    const uint64_t x = fdiv(t1, p.div_y);
+    const uint64_t y = t1 - x * p.div_y.d;
+    return (int64_t)x * sx + (int64_t)y * sy + (int64_t)z;
+  };
+
+  const uint64_t wstride = (uint64_t)gridDim.x * warps;
+  for (uint64_t tile = (uint64_t)blockIdx.x * warps + (threadIdx.x >> 5); tile < p.n_tiles; tile += wstride) {
+    const uint64_t g0 = tile * 8;
+    const uint64_t gi = g0 + g;  // this lane's input group
+    const bool live = gi < p.n_groups;
+    int64_t bi;
+    if (CONTIG) {
+      // 8 consecutive groups are 8 consecutive z of one (x, y)
+      bi = base(g0, p.sxi, p.syi) + g;
+    } else {
+      bi = live ? base(gi, p.sxi, p.syi) : 0;
+    }
+    double x[4] = {0.0, 0.0, 0.0, 0.0};
+    if (live) {
+      x[0] = p.in[bi + in_off0];
+      x[1] = p.in[bi + in_off0 + p.sbi];
+      x[2] = p.in[bi + in_off2];
+      x[3] = p.in[bi + in_off2 + p.sbi];
+    }
+    unsigned hi[4], lo[4];
+    unsigned emax = 1u, bad = 0u;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      hi[i] = (unsigned)__double2hiint(x[i]);
+      lo[i] = (unsigned)__double2loint(x[i]);
+      emax = max(emax, exp_eff(hi[i]));
+      bad |= ((hi[i] >> 20) & 0x7ffu) == 0x7ffu ? 1u : 0u;  // inf, nan
+    }
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    unsigned long long u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) u[i] = fixed_biased(hi[i], lo[i], emax);
+    unsigned B[kDigits][2];
+#pragma unroll
+    for (int j = 0; j < kDigits; ++j) {
+      B[j][0] = digit_pair(u[0], u[1], 10 * (kDigits - 1 - j));
+      B[j][1] = digit_pair(u[2], u[3], 10 * (kDigits - 1 - j));
+    }
+    float acc[kDigits][4];
+#pragma unroll
+    for (int l = 0; l < kDigits; ++l) acc[l][0] = acc[l][1] = acc[l][2] = acc[l][3] = 0.f;
+#pragma unroll
+    for (int i = 0; i < kDigits; ++i)
+#pragma unroll
+      for (int j = 0; i + j < kDigits; ++j) mma16816(acc[i + j], A[i], B[j]);
+    // output groups 2c and 2c+1: their exponents live in lanes 8c and 8c+4
+    const int ex0 = (int)__shfl_sync(0xffffffffu, emax, 8 * c) - 1022;
+    const int ex1 = (int)__shfl_sync(0xffffffffu, emax, 8 * c + 4) - 1022;
+    double y[4];
+    y[0] = combine(acc, 0, ex0 + rsc0, bad);  // row g, group 2c
+    y[1] = combine(acc, 1, ex1 + rsc0, bad);  // row g, group 2c+1
+    y[2] = combine(acc, 2, ex0 + rsc1, bad);  // row g+8, group 2c
+    y[3] = combine(acc, 3, ex1 + rsc1, bad);  // row g+8, group 2c+1
+    const uint64_t go0 = g0 + 2 * c, go1 = go0 + 1;
+    int64_t bo0, bo1;
+    if (CONTIG) {
+      bo0 = base(g0, p.sxo, p.syo) + 2 * c;
+      bo1 = bo0 + 1;
+    } else {
+      bo0 = go0 < p.n_groups ? base(go0, p.sxo, p.syo) : 0;
+      bo1 = go1 < p.n_groups ? base(go1, p.sxo, p.syo) : 0;
+    }
+    if (__any_sync(0xffffffffu, bad)) {
+      // inf / nan inputs or results outside the normal range: the tile's
+      // outputs in native FP64 (lane: rows g, g+8 of groups 2c, 2c+1)
+      const uint64_t gg[2] = {go0, go1};
+      const int64_t bb[2] = {bo0, bo1};
+#pragma unroll 1
+      for (int q = 0; q < 2; ++q) {
+        if (gg[q] >= p.n_groups) continue;
+        const int64_t b_in = base(gg[q], p.sxi, p.syi);
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+          const int r = g + 8 * h;
+          double a = 0.0;
+#pragma unroll 1
+          for (int k = 0; k < 16; ++k) a = fma(p.ptm[r][k], p.in[b_in + (k >> 2) * p.sai + (k & 3) * p.sbi], a);
+          y[2 * h + q] = a;
+        }
+      }
+      (void)bb;
+    }
+    if (CONTIG && p.pair_store) {
+      // groups 2c, 2c+1 are adjacent: 16-byte stores
+      *reinterpret_cast<double2*>(p.out + bo0 + out_off0) = make_double2(y[0], y[1]);
+      *reinterpret_cast<double2*>(p.out + bo0 + out_off1) = make_double2(y[2], y[3]);
+    } else {
+      if (go0 < p.n_groups) {
+        p.out[bo0 + out_off0] = y[0];
+        p.out[bo0 + out_off1] = y[2];
+      }
+      if (go1 < p.n_groups) {
+        p.out[bo1 + out_off0] = y[1];
+        p.out[bo1 + out_off1] = y[3];
+      }
+    }
+  }
+}
+
+// FP16 bit pattern of an integer |v| <= 2048 (exact).
+unsigned short half_bits(int v) {
+  if (v == 0) return 0;
+  const unsigned sgn = v < 0 ? 0x8000u : 0u;
+  unsigned a = (unsigned)std::abs(v);
+  int e = 31 - __builtin_clz(a);  // a in [2^e, 2^(e+1))
+  const unsigned mant = (a << (10 - e)) & 0x3ffu;
+  return (unsigned short)(sgn | ((unsigned)(e + 15) << 10) | mant);
+}
+
+// Host split of one PTM row (same fixed point as the device inputs).
+void split_row(const double* row, unsigned short (*dig)[16][16], int r, int* row_exp) {
+  unsigned emax = 1;
+  for (int k = 0; k < 16; ++k) {
+    uint64_t b;
+    std::memcpy(&b, &row[k], 8);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    emax = std::max(emax, e == 0u ? 1u : e);
+  }
+  for (int k = 0; k < 16; ++k) {
+    uint64_t b;
+    std::memcpy(&b, &row[k], 8);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    const uint64_t m = ((b & 0xfffffffffffffull) | (e != 0u ? (1ull << 52) : 0ull)) << 4;
+    const unsigned s = emax - (e == 0u ? 1u : e);
+    uint64_t f = s < 64u ? (m >> s) : 0ull;
+    if (b >> 63) f = 0ull - f;
+    const uint64_t u = f + kDigitBias;
+    for (int j = 0; j < kDigits; ++j) {
+      const int v = (int)((u >> (10 * (kDigits - 1 - j))) & 0x3ffu) - 512;
+      dig[j][r][k] = half_bits(v);
+    }
+  }
+  row_exp[r] = (int)emax - 1022 - 54;
+}
+
+}  // namespace
+
+bool eligible(const double* ptm_host, int kin, int kout) {
+  if (kin != 16 || kout != 16) return false;
+  for (int i = 0; i < 256; ++i) {
+    uint64_t b;
+    std::memcpy(&b, &ptm_host[i], 8);
+    if (((b >> 52) & 0x7ffu) == 0x7ffu) return false;  // inf, nan
+  }
+  return true;
+}
+
+int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z, unsigned* status,
+           cudaStream_t stream) {
+  TcParams p;
+  std::memset(&p, 0, sizeof p);
+  for (int r = 0; r < 16; ++r) {
+    split_row(op + 16 * r, p.digits, r, p.row_exp);
+    for (int k = 0; k < 16; ++k) p.ptm[r][k] = op[16 * r + k];
+  }
+  p.in = static_cast<const double*>(in);
+  p.out = static_cast<double*>(out);
+  p.status = status;
+  p.n_groups = X * Y * Z;
+  p.n_tiles = (p.n_groups + 7) / 8;
+  p.div_z = make_fastdiv(Z);
+  p.div_y = make_fastdiv(Y);
+  p.sbi = (int64_t)Z;
+  p.sai = (int64_t)(Y * 4 * Z);
+  p.syi = 4 * (int64_t)Z;
+  p.sxi = 16 * (int64_t)(Y * Z);
+  p.sbo = p.sbi;
+  p.sao = p.sai;
+  p.syo = p.syi;
+  p.sxo = p.sxi;
+  const bool contig = Z % 8 == 0;
+  p.pair_store = contig && (uintptr_t)out % 16 == 0 ? 1 : 0;
+  const uint64_t warps_needed = p.n_tiles;
+  const uint64_t blocks = (warps_needed + kBlock / 32 - 1) / (kBlock / 32);
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count() * 8));
+  if (contig)
+    apply16_tc_kernel<true><<<grid, kBlock, 0, stream>>>(p);
+  else
+    apply16_tc_kernel<false><<<grid, kBlock, 0, stream>>>(p);
+  return launch_status();
+}
+
+}  // namespace tc
+}  // namespace qsgb

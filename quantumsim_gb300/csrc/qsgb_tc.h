@@ -1,0 +1,42 @@
+// Interface between the apply entry points and the tensor-core kernel for
+// dense 16 x 16 PTMs (qsgb_tc.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qsgb_common.cuh"
+
+namespace qsgb {
+namespace tc {
+
+// digit planes of the split (six balanced base-1024 digits of a 57-bit
+// fixed-point value plus sign)
+constexpr int kDigits = 6;
+constexpr unsigned long long kDigitBias =
+    512ull * (1ull + (1ull << 10) + (1ull << 20) + (1ull << 30) + (1ull << 40) + (1ull << 50));
+
+struct TcParams {
+  const double* in;
+  double* out;
+  unsigned* status;
+  uint64_t n_groups, n_tiles;
+  FastDiv div_z, div_y;
+  int64_t sxi, syi, sai, sbi;  // strides of (x, a, y, b) in elements; z stride 1
+  int64_t sxo, syo, sao, sbo;
+  int pair_store;  // groups 2c, 2c+1 are adjacent and 16-byte aligned
+  int row_exp[16];                                // Ep_r - 1022 - 54 per row
+  unsigned short digits[kDigits][16][16];         // FP16 digit planes e_i[r][k]
+  double ptm[16][16];                             // the op matrix (FP64 fallback)
+};
+
+// The op matrix is 16 x 16 without inf or nan.
+bool eligible(const double* op, int kin, int kout);
+// Apply the 16 x 16 op matrix `op` (row-major, rows = (ra, rb), columns =
+// (ka, kb), qudit a more significant) to an FP64 tensor viewed as
+// (X, 4, Y, 4, Z).
+int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z, unsigned* status,
+           cudaStream_t stream);
+
+}  // namespace tc
+}  // namespace qsgb

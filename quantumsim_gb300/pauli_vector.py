@@ -23,8 +23,11 @@ Numerical semantics follow ``PauliVectorNumpy`` (the reference oracle):
 FP64 storage: by default (``arith='auto'``) the kernel computes each PTM
 row either with native FP64 FMAs or in float-float arithmetic (48-bit
 significand) on the FP32 pipes, whichever keeps the launch closest to the
-HBM bound; ``arith='f64'`` forces native FP64 everywhere and
-``arith='df64'`` float-float for every row with more than one term.
+HBM bound, and sends dense 16 x 16 PTMs (more than 5 non-zero terms per
+row) to the tensor cores, where FP64 values split into FP16 digit planes
+are multiplied with exact FP32 sums; ``arith='f64'`` forces native FP64
+everywhere, ``arith='df64'`` float-float for every row with more than one
+term, and ``arith='tc'`` the tensor cores for every 16 x 16 PTM.
 ``dtype=np.float32`` stores the vector in FP32 while every trace, marginal
 and partial-trace sum still accumulates in FP64.
 """
@@ -59,7 +62,7 @@ except Exception:  # pragma: no cover - depends on the environment
     REFERENCE_BASE = False
 
 _ARITH = {'auto': L.ARITH_AUTO, 'df64': L.ARITH_DF64, 'f64': L.ARITH_F64,
-          'f32': L.ARITH_F32}
+          'f32': L.ARITH_F32, 'tc': L.ARITH_TC}
 
 
 class _PtmCache:
@@ -142,8 +145,11 @@ class PauliVectorGB300(_Base):
         Storage type of the Pauli vector on the device.
     device : torch device or None
         CUDA device (default: the current one).
-    arith : 'auto' | 'df64' | 'f64' | 'f32'
-        Arithmetic of apply_ptm ('auto': df64 for FP64, f32 for FP32).
+    arith : 'auto' | 'df64' | 'f64' | 'f32' | 'tc'
+        Arithmetic of apply_ptm ('auto': per PTM, the specialised
+        float-float / FP64 kernels, or the tensor cores for 16 x 16 PTMs
+        with more than 5 terms per row; 'tc': every 16 x 16 PTM on the
+        tensor cores; f32 for FP32 storage).
     """
 
     def __init__(self, bases, pv=None, *, force=False, dtype=None,
@@ -166,7 +172,7 @@ class PauliVectorGB300(_Base):
         if arith not in _ARITH:
             raise ValueError('arith must be one of {}'.format(list(_ARITH)))
         if arith == 'f32' and tdtype != torch.float32 or \
-                arith in ('df64', 'f64') and tdtype != torch.float64:
+                arith in ('df64', 'f64', 'tc') and tdtype != torch.float64:
             raise ValueError('arith {!r} does not match storage {}'.format(
                 arith, tdtype))
         if arith == 'auto' and tdtype == torch.float32:

@@ -54,8 +54,9 @@ def test_generated_variants_compile(lib):
         (cz, (4,) * 8, (2, 5), {}),                      # group pairs
         (cz, (4,) * 8, (5, 2), {}),                      # swapped
         (cz, (4,) * 8, (6, 7), {}),                      # last two qudits
-        (dense, (4,) * 8, (1, 6), {}),                   # dense: single groups
-        (dense, (4,) * 8, (1, 6), {'transpose': True}),
+        # dense (float-float: arith='auto' sends it to the tensor cores)
+        (dense, (4,) * 8, (1, 6), {'arith': L.ARITH_DF64}),
+        (dense, (4,) * 8, (1, 6), {'arith': L.ARITH_DF64, 'transpose': True}),
         (rot, (4,) * 8, (3,), {}),
         (rot, (4,) * 8, (7,), {}),                       # vector accesses
         (rot, (4,) * 8, (7,), {'dtype': L.F32, 'arith': L.ARITH_F32}),
@@ -75,15 +76,21 @@ def test_generated_variants_compile(lib):
 def test_float_float_rows_carry_the_fp64_fallback(lib):
     rng = np.random.default_rng(4)
     dense = rng.standard_normal((4, 4, 4, 4))
-    st, src = _check(lib, dense, (4,) * 6, (1, 4))
+    st, src = _check(lib, dense, (4,) * 6, (1, 4), arith=L.ARITH_DF64)
     assert st == L.OK
     assert 'qfb_k[]' in src and 'qsgb_df_suspect' in src
+    # under arith='auto' the dense PTM goes to the precompiled tensor-core
+    # kernel: nothing to generate
+    st, _ = _check(lib, dense, (4,) * 6, (1, 4))
+    assert st == L.ERR_UNSUPPORTED
     # native FP64 throughout: no float-float rows, no fallback
     st, src = _check(lib, dense, (4,) * 6, (1, 4), arith=L.ARITH_F64)
     assert st == L.OK and 'qfb_k[]' not in src
     # a PTM whose magnitude leaves the float pair's range runs in FP64
-    st, src = _check(lib, dense * 2.0 ** 120, (4,) * 6, (1, 4))
+    st, src = _check(lib, dense * 2.0 ** 120, (4,) * 6, (1, 4),
+                     arith=L.ARITH_DF64)
     assert st == L.OK and 'qfb_k[]' not in src
-    st, src = _check(lib, dense * 2.0 ** -120, (4,) * 6, (1, 4))
+    st, src = _check(lib, dense * 2.0 ** -120, (4,) * 6, (1, 4),
+                     arith=L.ARITH_DF64)
     assert st == L.OK and 'qfb_k[]' not in src
     assert math.isfinite(float(st))
