@@ -749,6 +749,33 @@ def run_profile_case(args):
     print(json.dumps({'profile_case': n, 'trace': s.trace()}))
 
 
+def run_profile_tc(args):
+    """Small workload for ncu captures of the tensor-core kernel for dense
+    16x16 PTMs: a 12-qubit FP64 state (134 MB, larger than L2), one circuit
+    layer (12 noisy rotations + 3 noisy CZs), then 3x [dense PTM on (3, 7),
+    on the last two qubits (10, 11), and on (0, 11)].
+    Launch order: 15 setup launches, then 3 per repetition."""
+    import numpy as np
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads
+    n = args.profile_qubits
+    s = qg.PauliVectorGB300([bases.general(2)] * n, force=True)
+    rng = np.random.default_rng(3)
+    t1, t2 = workloads.coherence_times(rng, n)
+    for op in workloads.config1_layer(rng, n, t1, t2, 3):
+        s.apply_ptm(op[1], *op[2])
+    dense = rng.standard_normal((4, 4, 4, 4)) * 0.25
+    for _ in range(3):
+        s.apply_ptm(dense, 3, 7)
+        s.apply_ptm(dense, n - 2, n - 1)
+        s.apply_ptm(dense, 0, n - 1)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_case': 'tc', 'trace': s.trace()}))
+
+
 def run_profile_qutrits(args):
     """Small workload for ncu captures of the qutrit kernels: 8 qutrits
     (9^8 float64 entries, 344 MB); one layer of 9x9 PTMs on every qutrit, then
@@ -881,7 +908,7 @@ def main():
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', nargs='?', const='apply',
-                    choices=['apply', 'qutrits', 'batched', 'circuit',
+                    choices=['apply', 'qutrits', 'tc', 'batched', 'circuit',
                              'adjoint2'],
                     help='run a small ncu profiling workload and exit')
     ap.add_argument('--profile-qubits', type=int, default=12)
@@ -890,6 +917,7 @@ def main():
     args = ap.parse_args()
     if args.profile_case:
         {'apply': run_profile_case, 'qutrits': run_profile_qutrits,
+         'tc': run_profile_tc,
          'batched': run_profile_batched, 'adjoint2': run_profile_adjoint2,
          'circuit': run_profile_circuit}[args.profile_case](args)
         return

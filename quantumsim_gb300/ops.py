@@ -427,6 +427,101 @@ def scale_by_inverse_(pv: torch.Tensor, denom: torch.Tensor,
     L.check(status, 'qsgb_scale_by_inverse')
 
 
+# ------------------------------------------------------- eager fast paths
+# PauliVectorGB300 calls the C ABI directly for eager work on host numpy
+# PTMs: the operators above go through the torch dispatcher and a Python
+# kernel (~10 us), and recompute the geometry on every call (~15 us of
+# Python); an eager application with a cached, validated plan costs the
+# output allocation and one ctypes call.
+_STATUS_PTR = {}
+_DIAG_BUF = {}
+
+
+def status_ptr(index):
+    """Address of the device status word of CUDA device `index`."""
+    p = _STATUS_PTR.get(index)
+    if p is None:
+        p = status_tensor(torch.device('cuda', index)).data_ptr()
+        _STATUS_PTR[index] = p
+    return p
+
+
+def eager_plan(shape, dtype, qudits, ptm_shape):
+    """Validated geometry of applying a host PTM of `ptm_shape` to `qudits`
+    of a contiguous vector of `shape` and torch `dtype`: (output shape, two
+    qudits?, size arguments, layout flags, dtype code).  Raises ValueError
+    like apply_geometry."""
+    new_shape, (X, Y, Z), (dao, dbo, dai, dbi), swapped = apply_geometry(
+        shape, list(qudits), ptm_shape)
+    flags = L.PTM_HOST | (L.PTM_SWAPPED if swapped else 0)
+    code = L.F64 if dtype == torch.float64 else L.F32
+    if len(qudits) == 1:
+        return tuple(new_shape), False, (dbo, dbi, Y, Z), flags, code
+    return (tuple(new_shape), True, (dao, dbo, dai, dbi, X, Y, Z), flags,
+            code)
+
+
+def eager_apply(pv, ptm, plan, arith):
+    """Apply the contiguous float64 numpy PTM `ptm` to the contiguous CUDA
+    tensor `pv` with a plan from eager_plan; returns the new tensor."""
+    new_shape, two, sizes, flags, code = plan
+    out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
+    if out.numel() == 0:
+        return out
+    lib = L.load()
+    idx = pv.device.index
+    stream = _RAW_STREAM(idx) if _RAW_STREAM is not None else \
+        torch.cuda.current_stream(pv.device).cuda_stream
+    addr = ptm.__array_interface__['data'][0]
+    if two:
+        st = lib.qsgb_apply_ptm2(pv.data_ptr(), out.data_ptr(), addr, *sizes,
+                                 flags, code, arith, 0, status_ptr(idx),
+                                 stream)
+    else:
+        st = lib.qsgb_apply_ptm1(pv.data_ptr(), out.data_ptr(), addr, *sizes,
+                                 flags, code, arith, 0, status_ptr(idx),
+                                 stream)
+    if st == L.OK:
+        return out
+    if st == L.ERR_UNSUPPORTED:
+        return None  # the caller takes the general operator path
+    L.check(st, 'qsgb_apply_ptm')
+    return out
+
+
+def diag_marginals(pv, plan_arrays, axis):
+    """Marginals (axis >= 0) or trace (axis == -1) of the DM diagonal of the
+    CUDA tensor `pv` through the gather plan, in one launch and one
+    device-to-host copy that also returns the device status word (raises
+    like check_device_status).  None when the fused kernel does not serve
+    the request (the caller takes the gather + reduction path)."""
+    idx_off_c, idx_c, shape_c, n_out = plan_arrays
+    index = pv.device.index
+    bufs = _DIAG_BUF.get(index)
+    if bufs is None:
+        bufs = (torch.empty(80, dtype=torch.float64, device=pv.device),
+                torch.empty(80, dtype=torch.float64, pin_memory=True))
+        _DIAG_BUF[index] = bufs
+    dev, host = bufs
+    n = (1 if axis < 0 else n_out[axis]) + 1
+    if n > 65:
+        return None
+    stream = _RAW_STREAM(index) if _RAW_STREAM is not None else \
+        torch.cuda.current_stream(pv.device).cuda_stream
+    st = L.load().qsgb_diag_marginals(
+        pv.data_ptr(), _dtype_code(pv), pv.dim(), shape_c, idx_off_c, idx_c,
+        axis, dev.data_ptr(), status_ptr(index), stream)
+    if st == L.ERR_UNSUPPORTED:
+        return None
+    L.check(st, 'qsgb_diag_marginals')
+    host[:n].copy_(dev[:n], non_blocking=True)
+    torch.cuda.current_stream(pv.device).synchronize()
+    vals = host[:n].numpy().copy()
+    if vals[-1]:
+        _raise_status(status_tensor(pv.device), int(vals[-1]))
+    return vals[:-1]
+
+
 def prepare_ptm(shape, dtype, ptm, qudits, arith, transpose=False):
     """Compile ahead of time the specialised kernel that
     ``torch.ops.qsgb.apply_ptm`` would use for this host PTM (numpy float64)

@@ -89,6 +89,9 @@ class _PtmCache:
 
 _PTM_CACHE = _PtmCache()
 
+# validated plans of eager host-PTM applications (see ops.eager_plan)
+_APPLY_PLANS = {}
+
 
 _PLAN_CACHE = {}
 
@@ -108,6 +111,29 @@ def _diag_plan(bases):
         _PLAN_CACHE.clear()
     _PLAN_CACHE[key] = (tuple(bases), plan)
     return plan
+
+
+_DIAG_ARRAYS = {}
+
+
+def _diag_arrays(bases, shape):
+    """The gather plan of _diag_plan as C arrays for ops.diag_marginals
+    (index offsets, indices, vector shape, outcomes per qudit), or None for
+    bases without a gather plan.  Cached like _diag_plan."""
+    key = (tuple(id(b) for b in bases), tuple(shape))
+    hit = _DIAG_ARRAYS.get(key)
+    if hit is not None:
+        return hit[1]
+    plan = _diag_plan(bases)
+    arrays = None
+    if plan is not None:
+        idx_off, idx = plan
+        arrays = (L.i32_array(idx_off), L.i32_array(idx), L.i64_array(shape),
+                  [idx_off[a + 1] - idx_off[a] for a in range(len(bases))])
+    if len(_DIAG_ARRAYS) > 256:
+        _DIAG_ARRAYS.clear()
+    _DIAG_ARRAYS[key] = (tuple(bases), arrays)
+    return arrays
 
 
 def _diag_plan_of(bases):
@@ -247,6 +273,52 @@ class PauliVectorGB300(_Base):
         """Apply a PTM of shape (d_out..., d_in...) to `qubits` (argument
         order, any position); ``bases`` are left to the caller
         (quantumsim/operations/operation.py:549-551)."""
+        if type(ptm) is np.ndarray:
+            # host PTM: a validated plan per geometry, then one C call
+            if ptm.dtype != np.float64 or not ptm.flags.c_contiguous:
+                ptm = np.ascontiguousarray(ptm, dtype=np.float64)
+            data = self._data
+            key = (data.shape, data.dtype, qubits, ptm.shape)
+            plan = _APPLY_PLANS.get(key)
+            if plan is None:
+                self._validate_apply(ptm.shape, qubits)
+                plan = ops.eager_plan(tuple(data.shape), data.dtype, qubits,
+                                      ptm.shape)
+                if len(_APPLY_PLANS) > 4096:
+                    _APPLY_PLANS.clear()
+                _APPLY_PLANS[key] = plan
+            out = ops.eager_apply(data, ptm, plan, self._arith)
+            if out is not None:
+                self._data = out
+                return
+        self._apply_general(ptm, *qubits)
+
+    def _validate_apply(self, shape, qubits):
+        """The reference's argument errors for a PTM of `shape` on
+        `qubits` (quantumsim/pauli_vectors/pauli_vector.py:102-116,
+        cuda.py:125-127, 164-168, 240-243)."""
+        n = len(qubits)
+        if len(shape) != 2 * n:
+            raise ValueError('{}-qubit PTM must have {} dimensions, got {}'
+                             .format(n, 2 * n, len(shape)))
+        if n == 0:
+            raise NotImplementedError('Applying a 0-qubit PTM is not '
+                                      'implemented in this backend.')
+        if n > 2:
+            raise NotImplementedError('Applying {}-qubit PTM is not '
+                                      'implemented in the active backend.'
+                                      .format(n))
+        for i, q in enumerate(qubits):
+            self._validate_qubit(q, 'qubit{}'.format(i))
+        if n == 2 and qubits[0] == qubits[1]:
+            raise ValueError('The two qubits of a 2-qubit PTM must differ')
+        for q, din in zip(qubits, shape[n:]):
+            if self._data.shape[q] != din:
+                raise ValueError(
+                    'PTM acts on a {}-dimensional Pauli space, qubit {} has '
+                    'dim_pauli {}'.format(din, q, self._data.shape[q]))
+
+    def _apply_general(self, ptm, *qubits):
         n = len(qubits)
         if isinstance(ptm, torch.Tensor):
             ptm_t = ptm.to(torch.float64)
@@ -330,11 +402,26 @@ class PauliVectorGB300(_Base):
         diag = self._diagonal_device()
         return torch.ops.qsgb.marginals(diag, [diag.numel()], -1)
 
+    def _diag_reduce(self, axis):
+        """Trace (axis -1) or marginals of one qudit in one launch and one
+        device-to-host copy (ops.diag_marginals); None when the bases have no
+        gather plan or the diagonal is too large for the fused kernel."""
+        arrays = _diag_arrays(self.bases, self._data.shape)
+        if arrays is None:
+            return None
+        return ops.diag_marginals(self._data, arrays, axis)
+
     def trace(self):
+        vals = self._diag_reduce(-1)
+        if vals is not None:
+            return float(vals[0])
         return float(ops.fetch_checked(self._trace_device())[0])
 
     def meas_prob(self, qubit):
         self._validate_qubit(qubit, 'qubit')
+        vals = self._diag_reduce(qubit)
+        if vals is not None:
+            return vals
         diag = self._diagonal_device()
         probs = torch.ops.qsgb.marginals(diag, list(self.dim_hilbert), qubit)
         return ops.fetch_checked(probs)

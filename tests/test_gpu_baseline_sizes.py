@@ -14,7 +14,9 @@ PauliVectorNumpy, quantumsim/pauli_vectors/numpy.py:50-117) at full size:
 
 Each runs unit by unit (PauliVectorGB300.apply_ptm) and through the fused
 executor.  Required agreement: 1e-12 relative per Pauli-vector entry with a
-1e-14 absolute floor, and 1e-12 absolute on diagonals, marginals and traces.
+1e-14 absolute floor, and 1e-12 absolute on diagonals, marginals and traces
+(for the qutrit circuit under arith='auto', the per-entry bar scaled by the
+conditioning of its projection, as its test explains).
 """
 import numpy as np
 import pytest
@@ -69,15 +71,24 @@ def qutrit_oracle():
     return ops, ref, traces
 
 
-@pytest.mark.parametrize('fused', [False, True])
-def test_qutrit_8q_30_layers_with_measurement(qutrit_oracle, fused):
+@pytest.mark.parametrize('arith,fused', [('f64', False), ('f64', True),
+                                         ('auto', False), ('auto', True)])
+def test_qutrit_8q_30_layers_with_measurement(qutrit_oracle, arith, fused):
+    """Native FP64 meets the flat bar.  The float-float rows of
+    arith='auto' carry 2^-48 per application where FP64 carries 2^-53, and
+    this circuit multiplies every error made before its mid-circuit
+    projection by 1/p on the surviving entries: the projected outcome has
+    probability p = 0.0092 (the renormalisation trace), so 'auto' is held to
+    the same bar scaled by 1/p."""
     ops, ref, ref_traces = qutrit_oracle
-    s = qg.PauliVectorGB300([B.general(3)] * 8, force=True)
+    s = qg.PauliVectorGB300([B.general(3)] * 8, force=True, arith=arith)
     traces = (_run_fused if fused else workloads.run)(s, ops)
     assert len(traces) == len(ref_traces) == 1
     assert abs(traces[0] - ref_traces[0]) <= ATOL_PROB
     assert [b.dim_pauli for b in s.bases] == [b.dim_pauli for b in ref.bases]
-    _close(s.to_pv(), ref.to_pv())
+    amp = 1.0 if arith == 'f64' else 1.0 / ref_traces[0]
+    np.testing.assert_allclose(s.to_pv(), ref.to_pv(), rtol=RTOL_F64 * amp,
+                               atol=ATOL_F64 * amp)
     _measurements_agree(s, ref, (0, 3, 7))
 
 
