@@ -246,7 +246,10 @@ int qsgb_marginals_noalloc(const double* diag, int ndim, const int64_t* shape,
  * FP32 vectors.  out[n_out] receives the value of the device status word
  * *dev_status (0 when dev_status is NULL) as it stands when the kernel runs,
  * so a single device-to-host copy of n_out + 1 doubles returns the result
- * and every earlier kernel's status bits.  Diagonals of at most 2^22 entries
+ * and every earlier kernel's status bits.  With host_out != NULL the call
+ * also makes that copy into host_out (pinned memory for an asynchronous
+ * copy) and waits for it on the stream before returning; with NULL it
+ * returns at once, the results on the device.  Diagonals of at most 2^22 entries
  * and axes of at most 64 indices; larger ones return QSGB_ERR_UNSUPPORTED
  * (use qsgb_gather and qsgb_marginals).
  * Replaces: cuda.py:347-384 (trace and meas_prob: multitake, then a host
@@ -256,7 +259,8 @@ int qsgb_marginals_noalloc(const double* diag, int ndim, const int64_t* shape,
 int qsgb_diag_marginals(const void* in, int in_dtype, int ndim,
                         const int64_t* in_shape, const int32_t* idx_off,
                         const int32_t* idx, int axis, double* out,
-                        const unsigned* dev_status, void* stream);
+                        const unsigned* dev_status, double* host_out,
+                        void* stream);
 
 /*
  * Partial trace: out[kept...] = sum over traced qudits t of

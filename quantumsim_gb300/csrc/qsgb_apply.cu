@@ -648,11 +648,56 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
   // Z == 1 and either Y == 1 (two adjacent last qudits) or Da == 1 (one qudit)
   const bool contiguous = Z == 1 && (p.div_y.d == 1 || (da_in == 1 && da_out == 1)) &&
                           (uintptr_t)p.in % 16 == 0 && (uintptr_t)p.out % 16 == 0;
+  const int vin = vwidth(db_in, p.in), vout = vwidth(db_out, p.out);
+  // the cached kernel and term list of this geometry class and term mask
+  // (the rule of jit::make_spec: entries above 2^-52 of the largest, 2^-30
+  // for FP32, non-zero for native FP64 or a PTM outside [2^-100, 2^100])
+  const int ne = (int)(da_in * db_in * da_out * db_out);
+  jit::FastKey key;
+  const bool keyed = ne <= 64 * 104;
+  if (keyed) {
+    double amax = 0.0;
+    for (int i = 0; i < ne; ++i) amax = std::max(amax, std::fabs(ptm_host[i]));
+    int eff = arith;
+    if (arith != QSGB_ARITH_F32 && !(amax >= 0x1p-100 && amax <= 0x1p100)) eff = QSGB_ARITH_F64;
+    const double thr = eff == QSGB_ARITH_F64 ? 0.0 : amax * (eff == QSGB_ARITH_F32 ? 0x1p-30 : 0x1p-52);
+    const unsigned char hdr[16] = {(unsigned char)da_out, (unsigned char)db_out, (unsigned char)da_in,
+                                   (unsigned char)db_in, (unsigned char)(flags & 3), (unsigned char)dtype,
+                                   (unsigned char)eff, (unsigned char)pair, (unsigned char)(Z == 1),
+                                   (unsigned char)contiguous, (unsigned char)vin, (unsigned char)vout,
+                                   (unsigned char)(mode == kLaunch), 0, 0, 0};
+    std::memcpy(key.hdr, hdr, sizeof hdr);
+    key.nwords = (ne + 63) / 64;
+    for (int w = 0; w < key.nwords; ++w) key.mask[w] = 0;
+    for (int i = 0; i < ne; ++i)
+      if (std::fabs(ptm_host[i]) > thr) key.mask[i >> 6] |= 1ull << (i & 63);
+  }
+  auto geometry = [&](bool pair_final) {
+    const int NL = pair_final ? 2 : 1;
+    jit::Geometry g;
+    g.in = p.in;
+    g.out = p.out;
+    g.status = p.status;
+    g.n_items = pair_final ? p.n_items : (pair ? p.n_items * 2 : p.n_items);
+    g.div_z = pair_final ? p.div_z : (pair ? make_fastdiv((uint64_t)Z) : p.div_z);
+    g.div_y = p.div_y;
+    g.sxi = p.sxi / NL;
+    g.syi = p.syi / NL;
+    g.sai = p.sai / NL;
+    g.sbi = p.sbi / NL;
+    g.sxo = p.sxo / NL;
+    g.syo = p.syo / NL;
+    g.sao = p.sao / NL;
+    g.sbo = p.sbo / NL;
+    return g;
+  };
+  if (keyed && mode == kLaunch) {
+    if (const jit::FastEntry* e = jit::fast_find(key))
+      return jit::launch_entry(*e, geometry(e->spec.pair), ptm_host, stream);
+  }
   if (!jit::make_spec(ptm_host, (int)da_out, (int)db_out, (int)da_in, (int)db_in, flags & 3, dtype, arith, pair,
-                      Z == 1, contiguous, vwidth(db_in, p.in), vwidth(db_out, p.out), spec, coef))
+                      Z == 1, contiguous, vin, vout, spec, coef))
     return QSGB_ERR_UNSUPPORTED;
-  uint64_t n_items = p.n_items;
-  FastDiv div_z = p.div_z;
   // Two groups per thread (16-byte accesses) pay off for one-qudit PTMs and
   // for two-qudit PTMs of up to 2.5 terms per row; denser two-qudit rows
   // run faster one group per thread.  Measured on GB300 (14 qubits, GB/s,
@@ -661,32 +706,18 @@ int try_jit(const double* ptm_host, int64_t da_out, int64_t db_out, int64_t da_i
   // 4.38 terms/row 4534 / 5245, 6.12 terms/row 2629 / 3984; two rotations
   // on one qubit 5968 / 5042.
   if (pair && spec.kin > 4 && spec.n_coef() > 2.5 * spec.kout) {
-    pair = false;
-    n_items *= 2;
-    div_z = make_fastdiv((uint64_t)Z);
     if (!jit::make_spec(ptm_host, (int)da_out, (int)db_out, (int)da_in, (int)db_in, flags & 3, dtype, arith, false,
-                        Z == 1, contiguous, vwidth(db_in, p.in), vwidth(db_out, p.out), spec, coef))
+                        Z == 1, contiguous, vin, vout, spec, coef))
       return QSGB_ERR_UNSUPPORTED;
   }
   if (mode == kPrepare) return jit::prepare(spec);
   if (mode == kCompileOnly) return jit::compile_only(spec, src_out);
-  const int NL = pair ? 2 : 1;
-  jit::Geometry g;
-  g.in = p.in;
-  g.out = p.out;
-  g.status = p.status;
-  g.n_items = n_items;
-  g.div_z = div_z;
-  g.div_y = p.div_y;
-  g.sxi = p.sxi / NL;
-  g.syi = p.syi / NL;
-  g.sai = p.sai / NL;
-  g.sbi = p.sbi / NL;
-  g.sxo = p.sxo / NL;
-  g.syo = p.syo / NL;
-  g.sao = p.sao / NL;
-  g.sbo = p.sbo / NL;
-  return jit::launch(spec, g, coef.data(), stream);
+  if (keyed) {
+    if (const jit::FastEntry* e =
+            jit::fast_insert(key, spec, flags & 3, (int)da_out, (int)db_out, (int)da_in, (int)db_in))
+      return jit::launch_entry(*e, geometry(e->spec.pair), ptm_host, stream);
+  }
+  return jit::launch(spec, geometry(spec.pair), coef.data(), stream);
 }
 
 // mode kPrepare / kCompileOnly: validate, then compile the specialised

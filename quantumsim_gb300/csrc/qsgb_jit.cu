@@ -942,13 +942,9 @@ int compile_only(const Spec& s, std::string* src_out) {
   return cr == NVRTC_SUCCESS ? QSGB_OK : QSGB_ERR_CUDA;
 }
 
-int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t stream) {
-  cudaKernel_t kern;
-  const int st = kernel_for(s, &kern, nullptr);
-  if (st != QSGB_OK) return st;
-  const int nc = std::max(1, s.n_coef());
-  std::vector<unsigned char> blob(sizeof(Hdr) + 8 * (size_t)nc, 0);
-  Hdr h;
+namespace {
+
+void fill_header(Hdr& h, const Geometry& g) {
   h.in = g.in;
   h.out = g.out;
   h.status = g.status;
@@ -967,15 +963,109 @@ int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t st
   h.syo = g.syo;
   h.sao = g.sao;
   h.sbo = g.sbo;
-  std::memcpy(blob.data(), &h, sizeof h);
-  std::memcpy(blob.data() + sizeof h, coef, 8 * (size_t)s.n_coef());
-  void* args[] = {blob.data()};
+}
+
+// The parameter block (header + coefficients) is assembled in `blob`.
+int launch_blob(cudaKernel_t kern, const Spec& s, const Geometry& g, unsigned char* blob, cudaStream_t stream) {
+  Hdr h;
+  fill_header(h, g);
+  std::memcpy(blob, &h, sizeof h);
+  void* args[] = {blob};
   const unsigned block = s.stage_warps ? 32u * (unsigned)s.stage_warps : 128u;
   const uint64_t need = (g.n_items + block - 1) / block;
   const uint64_t cap = (uint64_t)sm_count() * 16;
   const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min(need, cap));
   QSGB_CUDA_TRY(cudaLaunchKernel((const void*)kern, dim3(grid), dim3(block), args, 0, stream));
   return QSGB_OK;
+}
+
+struct FastKeyHash {
+  size_t operator()(const FastKey& k) const {
+    unsigned long long h = 1469598103934665603ull;
+    for (unsigned char c : k.hdr) h = (h ^ c) * 1099511628211ull;
+    for (int i = 0; i < k.nwords; ++i) h = (h ^ k.mask[i]) * 1099511628211ull;
+    return (size_t)h;
+  }
+};
+
+struct FastCache {
+  std::mutex mu;
+  std::unordered_map<FastKey, FastEntry, FastKeyHash> map;
+};
+FastCache& fast_cache() {
+  static FastCache c;
+  return c;
+}
+
+}  // namespace
+
+bool FastKey::operator==(const FastKey& o) const {
+  if (nwords != o.nwords || std::memcmp(hdr, o.hdr, sizeof hdr) != 0) return false;
+  return std::memcmp(mask, o.mask, sizeof(unsigned long long) * (size_t)nwords) == 0;
+}
+
+const FastEntry* fast_find(const FastKey& key) {
+  FastCache& c = fast_cache();
+  std::lock_guard<std::mutex> g(c.mu);
+  auto it = c.map.find(key);
+  return it == c.map.end() ? nullptr : &it->second;  // entries are never erased
+}
+
+const FastEntry* fast_insert(const FastKey& key, const Spec& spec, int layout, int da_out, int db_out, int da_in,
+                             int db_in) {
+  FastEntry e;
+  if (kernel_for(spec, &e.kern, nullptr) != QSGB_OK) return nullptr;
+  e.spec = spec;
+  const int kin = da_in * db_in, kout = da_out * db_out;
+  for (int r = 0; r < spec.kout; ++r)
+    for (int k : spec.cols[r]) {
+      const int ra = r / db_out, rb = r % db_out, ka = k / db_in, kb = k % db_in;
+      int idx;
+      switch (layout & 3) {
+        case 0: idx = r * kin + k; break;
+        case QSGB_PTM_SWAPPED: idx = ((rb * da_out + ra) * db_in + kb) * da_in + ka; break;
+        case QSGB_PTM_TRANSPOSED: idx = k * kout + r; break;
+        default: idx = ((kb * da_in + ka) * db_out + rb) * da_out + ra; break;
+      }
+      e.src.push_back(idx);
+      e.kind.push_back((unsigned char)spec.mode[r]);
+    }
+  FastCache& c = fast_cache();
+  std::lock_guard<std::mutex> g(c.mu);
+  auto it = c.map.emplace(key, std::move(e)).first;
+  return &it->second;
+}
+
+int launch_entry(const FastEntry& e, const Geometry& g, const double* ptm_host, cudaStream_t stream) {
+  // header + coefficients, at most 32764 bytes (kMaxCoef)
+  alignas(16) unsigned char blob[sizeof(Hdr) + 8 * (size_t)kMaxCoef];
+  double* coef = reinterpret_cast<double*>(blob + sizeof(Hdr));
+  const size_t n = e.src.size();
+  for (size_t t = 0; t < n; ++t) {
+    const double v = ptm_host[e.src[t]];
+    if (e.kind[t] == kModeDF) {
+      const float h = (float)v;
+      const float l = (float)(v - (double)h);
+      const uint64_t bits = ((uint64_t)__builtin_bit_cast(uint32_t, h) << 32) | __builtin_bit_cast(uint32_t, l);
+      coef[t] = __builtin_bit_cast(double, bits);
+    } else if (e.kind[t] == kModeF32) {
+      coef[t] = __builtin_bit_cast(double, (uint64_t)__builtin_bit_cast(uint32_t, (float)v));
+    } else {
+      coef[t] = v;
+    }
+  }
+  if (n == 0) coef[0] = 0.0;
+  return launch_blob(e.kern, e.spec, g, blob, stream);
+}
+
+int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t stream) {
+  cudaKernel_t kern;
+  const int st = kernel_for(s, &kern, nullptr);
+  if (st != QSGB_OK) return st;
+  const int nc = std::max(1, s.n_coef());
+  std::vector<unsigned char> blob(sizeof(Hdr) + 8 * (size_t)nc, 0);
+  std::memcpy(blob.data() + sizeof(Hdr), coef, 8 * (size_t)s.n_coef());
+  return launch_blob(kern, s, g, blob.data(), stream);
 }
 
 }  // namespace jit

@@ -60,6 +60,34 @@ int kernel_for(const Spec& s, cudaKernel_t* k, std::string* src_out);
 int launch(const Spec& s, const Geometry& g, const double* coef, cudaStream_t stream);
 // Compile (or fetch from the caches) the kernel of `s` without launching it.
 int prepare(const Spec& s);
+// ------------------------------------------------------------ fast path
+// A specialisation request up to the PTM values: the geometry class and
+// arithmetic (hdr) and the PTM's term mask in stored order.  Requests with
+// equal keys get the same kernel and the same term list, so a cached entry
+// serves them with a gather of the coefficients and a launch.
+struct FastKey {
+  unsigned char hdr[16];
+  int nwords;
+  unsigned long long mask[104];  // up to 81 x 81 entries
+  bool operator==(const FastKey& o) const;
+};
+struct FastEntry {
+  Spec spec;                      // final spec (group pairs or single groups)
+  cudaKernel_t kern;
+  std::vector<int> src;           // stored PTM index of each term, row order
+  std::vector<unsigned char> kind;  // per term: kModeDP / kModeDF / kModeF32
+};
+// Cached entry of `key`, or nullptr.
+const FastEntry* fast_find(const FastKey& key);
+// Build and cache the entry of a compiled spec; `layout` is the stored PTM
+// layout (QSGB_PTM_SWAPPED / QSGB_PTM_TRANSPOSED bits) and da/db the
+// target dims.  Returns the cached entry (or nullptr if the kernel cannot
+// be had).
+const FastEntry* fast_insert(const FastKey& key, const Spec& spec, int layout, int da_out, int db_out, int da_in,
+                             int db_in);
+// Launch a cached entry with coefficients gathered from the host PTM.
+int launch_entry(const FastEntry& e, const Geometry& g, const double* ptm_host, cudaStream_t stream);
+
 // Generate the source of `s` and compile it with NVRTC without loading it
 // (no device needed): QSGB_OK, QSGB_ERR_CUDA on a compile error,
 // QSGB_ERR_UNSUPPORTED without NVRTC.

@@ -218,24 +218,35 @@ constexpr int kDiagRedBlock = 1024;
 __global__ void __launch_bounds__(kDiagRedBlock) diag_marginals_kernel(const __grid_constant__ DiagRedParams p) {
   __shared__ double sh[32];
   const uint64_t d_axis = p.axis < 0 ? 1 : p.div[p.axis].d;
+  constexpr int U = 8;  // independent loads in flight per thread
   for (int j = 0; j < p.n_out; ++j) {
     double acc = 0.0;
-    for (uint64_t m = threadIdx.x; m < p.per_j; m += kDiagRedBlock) {
-      // m-th diagonal entry whose index along `axis` is j
-      const uint64_t hi = fdiv(m, p.div_s);
-      const uint64_t lo = m - hi * p.s_axis;
-      uint64_t rem = (hi * d_axis + (uint64_t)j) * p.s_axis + lo;
-      int64_t addr = 0;
-      bool zero = false;
-      for (int a = p.ndim - 1; a >= 0; --a) {
-        const uint64_t q = fdiv(rem, p.div[a]);
-        const int i = (int)(rem - q * p.div[a].d);
-        rem = q;
-        const int k = p.idx[p.idx_off[a] + i];
-        zero |= k < 0;
-        addr += (int64_t)(k < 0 ? 0 : k) * p.in_stride[a];
+    for (uint64_t m0 = threadIdx.x; m0 < p.per_j; m0 += (uint64_t)U * kDiagRedBlock) {
+      double v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        // m-th diagonal entry whose index along `axis` is j
+        const uint64_t m = m0 + (uint64_t)u * kDiagRedBlock;
+        v[u] = 0.0;
+        if (m < p.per_j) {
+          const uint64_t hi = fdiv(m, p.div_s);
+          const uint64_t lo = m - hi * p.s_axis;
+          uint64_t rem = (hi * d_axis + (uint64_t)j) * p.s_axis + lo;
+          int64_t addr = 0;
+          bool zero = false;
+          for (int a = p.ndim - 1; a >= 0; --a) {
+            const uint64_t q = fdiv(rem, p.div[a]);
+            const int i = (int)(rem - q * p.div[a].d);
+            rem = q;
+            const int k = p.idx[p.idx_off[a] + i];
+            zero |= k < 0;
+            addr += (int64_t)(k < 0 ? 0 : k) * p.in_stride[a];
+          }
+          if (!zero) v[u] = load_f64(p.in, addr, p.in_dtype);
+        }
       }
-      if (!zero) acc += load_f64(p.in, addr, p.in_dtype);
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc += v[u];  // fixed order
     }
     const double r = block_sum(acc, sh);
     if (threadIdx.x == 0) p.out[j] = r;
@@ -424,7 +435,7 @@ extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t oute
 
 extern "C" int qsgb_diag_marginals(const void* in, int in_dtype, int ndim, const int64_t* in_shape,
                                    const int32_t* idx_off, const int32_t* idx, int axis, double* out,
-                                   const unsigned* dev_status, void* stream) {
+                                   const unsigned* dev_status, double* host_out, void* stream) {
   if (!in || !out || !idx_off || (ndim > 0 && (!in_shape || !idx))) return QSGB_ERR_INVALID;
   if (in_dtype != QSGB_F64 && in_dtype != QSGB_F32) return QSGB_ERR_INVALID;
   if (ndim < 0 || ndim > kMaxDim || axis < -1 || axis >= ndim) return QSGB_ERR_INVALID;
@@ -459,8 +470,13 @@ extern "C" int qsgb_diag_marginals(const void* in, int in_dtype, int ndim, const
   p.div_s = make_fastdiv(p.s_axis);
   for (int a = 0; a <= ndim; ++a) p.idx_off[a] = idx_off[a];
   for (int i = 0; i < idx_off[ndim]; ++i) p.idx[i] = idx[i];
-  diag_marginals_kernel<<<1, kDiagRedBlock, 0, as_stream(stream)>>>(p);
-  return launch_status();
+  cudaStream_t st = as_stream(stream);
+  diag_marginals_kernel<<<1, kDiagRedBlock, 0, st>>>(p);
+  const int ls = launch_status();
+  if (ls != QSGB_OK || !host_out) return ls;
+  QSGB_CUDA_TRY(cudaMemcpyAsync(host_out, out, (d + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+  QSGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return QSGB_OK;
 }
 
 static void marg_geometry(int64_t n, int64_t n_out, int* nchunks, uint64_t* chunk) {

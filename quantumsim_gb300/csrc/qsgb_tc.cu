@@ -207,23 +207,24 @@ __global__ void __launch_bounds__(kBlock) apply16_tc_kernel(const __grid_constan
     }
     if (__any_sync(0xffffffffu, bad)) {
       // inf / nan inputs or results outside the normal range: the tile's
-      // outputs in native FP64 (lane: rows g, g+8 of groups 2c, 2c+1)
-      const uint64_t gg[2] = {go0, go1};
-      const int64_t bb[2] = {bo0, bo1};
-#pragma unroll 1
+      // outputs in native FP64 (lane: rows g, g+8 of groups 2c, 2c+1); the
+      // loops over q and h are unrolled so that y[] stays in registers
+#pragma unroll
       for (int q = 0; q < 2; ++q) {
-        if (gg[q] >= p.n_groups) continue;
-        const int64_t b_in = base(gg[q], p.sxi, p.syi);
+        const uint64_t gq = q ? go1 : go0;
+        if (gq < p.n_groups) {
+          const int64_t b_in = base(gq, p.sxi, p.syi);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int r = g + 8 * h;
+            double a = 0.0;
 #pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-          const int r = g + 8 * h;
-          double a = 0.0;
-#pragma unroll 1
-          for (int k = 0; k < 16; ++k) a = fma(p.ptm[r][k], p.in[b_in + (k >> 2) * p.sai + (k & 3) * p.sbi], a);
-          y[2 * h + q] = a;
+            for (int k = 0; k < 16; ++k)
+              a = fma(p.ptm[r][k], p.in[b_in + (k >> 2) * p.sai + (k & 3) * p.sbi], a);
+            y[2 * h + q] = a;
+          }
         }
       }
-      (void)bb;
     }
     if (CONTIG && p.pair_store) {
       // groups 2c, 2c+1 are adjacent: 16-byte stores

@@ -508,15 +508,14 @@ def diag_marginals(pv, plan_arrays, axis):
         return None
     stream = _RAW_STREAM(index) if _RAW_STREAM is not None else \
         torch.cuda.current_stream(pv.device).cuda_stream
+    # the library copies the n values into the pinned buffer and waits
     st = L.load().qsgb_diag_marginals(
         pv.data_ptr(), _dtype_code(pv), pv.dim(), shape_c, idx_off_c, idx_c,
-        axis, dev.data_ptr(), status_ptr(index), stream)
+        axis, dev.data_ptr(), status_ptr(index), host.data_ptr(), stream)
     if st == L.ERR_UNSUPPORTED:
         return None
     L.check(st, 'qsgb_diag_marginals')
-    host[:n].copy_(dev[:n], non_blocking=True)
-    torch.cuda.current_stream(pv.device).synchronize()
-    vals = host[:n].numpy().copy()
+    vals = host.numpy()[:n].copy()
     if vals[-1]:
         _raise_status(status_tensor(pv.device), int(vals[-1]))
     return vals[:-1]
