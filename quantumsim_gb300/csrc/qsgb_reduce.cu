@@ -72,6 +72,10 @@ constexpr int kTakeBlock = 256;
 constexpr int kTakeUnroll = 4;
 constexpr uint64_t kTakeTile = (uint64_t)kTakeBlock * kTakeUnroll;
 
+// NIDX: capacity of the index list carried in the launch parameters (a
+// small block for the usual reduce / project requests, which keeps the
+// per-launch parameter copy short)
+template <int NIDX>
 struct TakeParams {
   const void* in;
   void* out;
@@ -81,11 +85,11 @@ struct TakeParams {
   uint64_t n_units;        // unit mode: n_rows * row_v
   FastDiv div_tpr, div_dout, div_rowv;
   int64_t d_in;
-  int idx[kMaxIdx];
+  int idx[NIDX];
 };
 
-template <typename V>
-__global__ void __launch_bounds__(kTakeBlock) take_rows_kernel(const __grid_constant__ TakeParams p) {
+template <typename V, int NIDX>
+__global__ void __launch_bounds__(kTakeBlock) take_rows_kernel(const __grid_constant__ TakeParams<NIDX> p) {
   const V* __restrict__ in = static_cast<const V*>(p.in);
   V* __restrict__ out = static_cast<V*>(p.out);
   const uint64_t n_tiles = p.n_rows * p.tiles_per_row;
@@ -119,8 +123,8 @@ __global__ void __launch_bounds__(kTakeBlock) take_rows_kernel(const __grid_cons
   }
 }
 
-template <typename V>
-__global__ void __launch_bounds__(kTakeBlock) take_units_kernel(const __grid_constant__ TakeParams p) {
+template <typename V, int NIDX>
+__global__ void __launch_bounds__(kTakeBlock) take_units_kernel(const __grid_constant__ TakeParams<NIDX> p) {
   const V* __restrict__ in = static_cast<const V*>(p.in);
   V* __restrict__ out = static_cast<V*>(p.out);
   const uint64_t stride = (uint64_t)gridDim.x * kTakeBlock;
@@ -386,19 +390,13 @@ extern "C" int qsgb_gather(const void* in, void* out, int in_dtype, int out_dtyp
   return launch_status();
 }
 
-extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t outer, int64_t d_in, int64_t inner,
-                              const int32_t* idx, int64_t d_out, void* stream) {
-  if (!in || !out || !idx || in == out) return QSGB_ERR_INVALID;
-  if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
-  if (outer < 1 || d_in < 1 || inner < 1 || d_out < 1) return QSGB_ERR_INVALID;
-  if (d_out > kMaxIdx) return QSGB_ERR_UNSUPPORTED;
-  TakeParams p{};
+template <int NIDX>
+int take_launch(const void* in, void* out, int dtype, int64_t outer, int64_t d_in, int64_t inner,
+                const int32_t* idx, int64_t d_out, cudaStream_t s) {
+  TakeParams<NIDX> p{};
   p.in = in;
   p.out = out;
-  for (int64_t j = 0; j < d_out; ++j) {
-    if (idx[j] >= d_in || idx[j] < -1) return QSGB_ERR_INVALID;
-    p.idx[j] = idx[j];
-  }
+  for (int64_t j = 0; j < d_out; ++j) p.idx[j] = idx[j];
   const size_t esz = dtype == QSGB_F64 ? 8 : 4;
   // 16-byte units when a row is a whole number of them and both tensors
   // start on a 16-byte boundary
@@ -408,7 +406,6 @@ extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t oute
   p.n_rows = (uint64_t)outer * (uint64_t)d_out;
   p.d_in = d_in;
   p.div_dout = make_fastdiv((uint64_t)d_out);
-  cudaStream_t s = as_stream(stream);
   const bool rows = p.row_v >= 128;
   unsigned grid;
   if (rows) {
@@ -421,62 +418,29 @@ extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t oute
     grid = grid_for((p.n_units + kTakeUnroll - 1) / kTakeUnroll, kTakeBlock);
   }
   if (usz == 16) {
-    if (rows) take_rows_kernel<uint4><<<grid, kTakeBlock, 0, s>>>(p);
-    else take_units_kernel<uint4><<<grid, kTakeBlock, 0, s>>>(p);
+    if (rows) take_rows_kernel<uint4, NIDX><<<grid, kTakeBlock, 0, s>>>(p);
+    else take_units_kernel<uint4, NIDX><<<grid, kTakeBlock, 0, s>>>(p);
   } else if (usz == 8) {
-    if (rows) take_rows_kernel<unsigned long long><<<grid, kTakeBlock, 0, s>>>(p);
-    else take_units_kernel<unsigned long long><<<grid, kTakeBlock, 0, s>>>(p);
+    if (rows) take_rows_kernel<unsigned long long, NIDX><<<grid, kTakeBlock, 0, s>>>(p);
+    else take_units_kernel<unsigned long long, NIDX><<<grid, kTakeBlock, 0, s>>>(p);
   } else {
-    if (rows) take_rows_kernel<unsigned><<<grid, kTakeBlock, 0, s>>>(p);
-    else take_units_kernel<unsigned><<<grid, kTakeBlock, 0, s>>>(p);
+    if (rows) take_rows_kernel<unsigned, NIDX><<<grid, kTakeBlock, 0, s>>>(p);
+    else take_units_kernel<unsigned, NIDX><<<grid, kTakeBlock, 0, s>>>(p);
   }
   return launch_status();
 }
 
-extern "C" int qsgb_diag_marginals(const void* in, int in_dtype, int ndim, const int64_t* in_shape,
-                                   const int32_t* idx_off, const int32_t* idx, int axis, double* out,
-                                   const unsigned* dev_status, double* host_out, void* stream) {
-  if (!in || !out || !idx_off || (ndim > 0 && (!in_shape || !idx))) return QSGB_ERR_INVALID;
-  if (in_dtype != QSGB_F64 && in_dtype != QSGB_F32) return QSGB_ERR_INVALID;
-  if (ndim < 0 || ndim > kMaxDim || axis < -1 || axis >= ndim) return QSGB_ERR_INVALID;
-  if (idx_off[0] != 0 || idx_off[ndim] > kMaxIdx) return QSGB_ERR_UNSUPPORTED;
-  DiagRedParams p{};
-  p.in = in;
-  p.out = out;
-  p.status = dev_status;
-  p.in_dtype = in_dtype;
-  p.ndim = ndim;
-  p.axis = axis;
-  uint64_t n = 1, s_axis = 1;
-  int64_t stride = 1;
-  for (int a = ndim - 1; a >= 0; --a) {
-    const int len = idx_off[a + 1] - idx_off[a];
-    if (len < 1 || in_shape[a] < 1) return QSGB_ERR_INVALID;
-    for (int i = idx_off[a]; i < idx_off[a + 1]; ++i)
-      if (idx[i] >= in_shape[a] || idx[i] < -1) return QSGB_ERR_INVALID;
-    p.div[a] = make_fastdiv((uint64_t)len);
-    p.in_stride[a] = stride;
-    stride *= in_shape[a];
-    if (axis >= 0 && a > axis) s_axis *= (uint64_t)len;
-    n *= (uint64_t)len;
-  }
-  // one block: diagonals of up to 2^22 entries (prod of Hilbert dims)
-  if (n > (1ull << 22)) return QSGB_ERR_UNSUPPORTED;
-  const uint64_t d = axis < 0 ? 1 : (uint64_t)(idx_off[axis + 1] - idx_off[axis]);
-  if (d > 64) return QSGB_ERR_UNSUPPORTED;
-  p.n_out = (int)d;
-  p.per_j = n / d;
-  p.s_axis = axis < 0 ? 1 : s_axis;
-  p.div_s = make_fastdiv(p.s_axis);
-  for (int a = 0; a <= ndim; ++a) p.idx_off[a] = idx_off[a];
-  for (int i = 0; i < idx_off[ndim]; ++i) p.idx[i] = idx[i];
-  cudaStream_t st = as_stream(stream);
-  diag_marginals_kernel<<<1, kDiagRedBlock, 0, st>>>(p);
-  const int ls = launch_status();
-  if (ls != QSGB_OK || !host_out) return ls;
-  QSGB_CUDA_TRY(cudaMemcpyAsync(host_out, out, (d + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
-  QSGB_CUDA_TRY(cudaStreamSynchronize(st));
-  return QSGB_OK;
+extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t outer, int64_t d_in, int64_t inner,
+                              const int32_t* idx, int64_t d_out, void* stream) {
+  if (!in || !out || !idx || in == out) return QSGB_ERR_INVALID;
+  if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
+  if (outer < 1 || d_in < 1 || inner < 1 || d_out < 1) return QSGB_ERR_INVALID;
+  if (d_out > kMaxIdx) return QSGB_ERR_UNSUPPORTED;
+  for (int64_t j = 0; j < d_out; ++j)
+    if (idx[j] >= d_in || idx[j] < -1) return QSGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  if (d_out <= 32) return take_launch<32>(in, out, dtype, outer, d_in, inner, idx, d_out, s);
+  return take_launch<kMaxIdx>(in, out, dtype, outer, d_in, inner, idx, d_out, s);
 }
 
 static void marg_geometry(int64_t n, int64_t n_out, int* nchunks, uint64_t* chunk) {
