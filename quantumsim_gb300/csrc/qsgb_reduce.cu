@@ -443,6 +443,52 @@ extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t oute
   return take_launch<kMaxIdx>(in, out, dtype, outer, d_in, inner, idx, d_out, s);
 }
 
+extern "C" int qsgb_diag_marginals(const void* in, int in_dtype, int ndim, const int64_t* in_shape,
+                                   const int32_t* idx_off, const int32_t* idx, int axis, double* out,
+                                   const unsigned* dev_status, double* host_out, void* stream) {
+  if (!in || !out || !idx_off || (ndim > 0 && (!in_shape || !idx))) return QSGB_ERR_INVALID;
+  if (in_dtype != QSGB_F64 && in_dtype != QSGB_F32) return QSGB_ERR_INVALID;
+  if (ndim < 0 || ndim > kMaxDim || axis < -1 || axis >= ndim) return QSGB_ERR_INVALID;
+  if (idx_off[0] != 0 || idx_off[ndim] > kMaxIdx) return QSGB_ERR_UNSUPPORTED;
+  DiagRedParams p{};
+  p.in = in;
+  p.out = out;
+  p.status = dev_status;
+  p.in_dtype = in_dtype;
+  p.ndim = ndim;
+  p.axis = axis;
+  uint64_t n = 1, s_axis = 1;
+  int64_t stride = 1;
+  for (int a = ndim - 1; a >= 0; --a) {
+    const int len = idx_off[a + 1] - idx_off[a];
+    if (len < 1 || in_shape[a] < 1) return QSGB_ERR_INVALID;
+    for (int i = idx_off[a]; i < idx_off[a + 1]; ++i)
+      if (idx[i] >= in_shape[a] || idx[i] < -1) return QSGB_ERR_INVALID;
+    p.div[a] = make_fastdiv((uint64_t)len);
+    p.in_stride[a] = stride;
+    stride *= in_shape[a];
+    if (axis >= 0 && a > axis) s_axis *= (uint64_t)len;
+    n *= (uint64_t)len;
+  }
+  // one block: diagonals of up to 2^22 entries (prod of Hilbert dims)
+  if (n > (1ull << 22)) return QSGB_ERR_UNSUPPORTED;
+  const uint64_t d = axis < 0 ? 1 : (uint64_t)(idx_off[axis + 1] - idx_off[axis]);
+  if (d > 64) return QSGB_ERR_UNSUPPORTED;
+  p.n_out = (int)d;
+  p.per_j = n / d;
+  p.s_axis = axis < 0 ? 1 : s_axis;
+  p.div_s = make_fastdiv(p.s_axis);
+  for (int a = 0; a <= ndim; ++a) p.idx_off[a] = idx_off[a];
+  for (int i = 0; i < idx_off[ndim]; ++i) p.idx[i] = idx[i];
+  cudaStream_t st = as_stream(stream);
+  diag_marginals_kernel<<<1, kDiagRedBlock, 0, st>>>(p);
+  const int ls = launch_status();
+  if (ls != QSGB_OK || !host_out) return ls;
+  QSGB_CUDA_TRY(cudaMemcpyAsync(host_out, out, (d + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+  QSGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return QSGB_OK;
+}
+
 static void marg_geometry(int64_t n, int64_t n_out, int* nchunks, uint64_t* chunk) {
   const uint64_t per_j = (uint64_t)(n / std::max<int64_t>(n_out, 1));
   uint64_t c = std::max<uint64_t>(4096, (per_j + kMaxChunks - 1) / kMaxChunks);
