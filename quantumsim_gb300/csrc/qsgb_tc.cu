@@ -42,6 +42,7 @@
 // planes (the A fragments) are loaded into registers once per warp.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "qsgb_common.cuh"
@@ -243,6 +244,242 @@ __global__ void __launch_bounds__(kBlock) apply16_tc_kernel(const __grid_constan
   }
 }
 
+// ---------------------------------------------------------------------------
+// tcgen05 form: one thread per group, 128 groups per tile (the M of one
+// tcgen05.mma), the six level accumulators in tensor memory.
+//
+// Per tile, each thread loads its group's 16 inputs, splits them and writes
+// its row of the six input digit planes (the A operand, 128 x 16 FP16 each)
+// to shared memory; one thread issues the 21 tcgen05.mma.kind::f16 (A = input
+// plane j, B = PTM plane i, both K-major, D = level i + j: 16 FP32 columns of
+// tensor memory) and commits them to an mbarrier; after the barrier each warp
+// reads its 32 lanes (groups) of the accumulators with tcgen05.ld and
+// recombines its outputs.  Shared-memory operands use the canonical K-major
+// layout without swizzling: core matrices of 8 rows x 16 bytes (8 FP16 along
+// K) at (row / 8) * 256 + (k / 8) * 128, so the descriptors carry a leading
+// (K) byte offset of 128 and a stride (8-row) byte offset of 256.
+constexpr int kUBlock = 128;
+constexpr int kPlaneA = 128 * 16 * 2;  // one input digit plane: 128 rows x 16 FP16
+constexpr int kPlaneB = 16 * 16 * 2;   // one PTM digit plane: 16 rows x 16 FP16
+constexpr int kSmemB = kDigits * kPlaneA;             // 24576
+constexpr int kSmemBar = kSmemB + kDigits * kPlaneB;  // 27648
+constexpr int kSmemTmem = kSmemBar + 8;
+constexpr int kSmemFlag = kSmemTmem + 4;
+// the dynamic allocation is padded so that at most 4 blocks share an SM:
+// 4 x 128 tensor-memory columns fill its 512
+constexpr int kUmmaSmem = 56 * 1024;
+constexpr unsigned kTmemCols = 128;  // 6 levels x 16 columns, a power of two
+// kind::f16 instruction descriptor: D F32 (bits 4-5 = 1), A and B F16 (0),
+// both K-major, N / 8 at bits 17-22, M / 16 at bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr long long kSpinLimit = 1ll << 26;
+
+__host__ __device__ constexpr int core_off(int row, int k) {
+  return (row >> 3) * 256 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+// shared-memory matrix descriptor: start >> 4 (bits 0-13), leading byte
+// offset >> 4 (16-29), stride byte offset >> 4 (32-45), version 1 (46-47),
+// no swizzling (61-63 = 0)
+__device__ __forceinline__ unsigned long long smem_desc(uint32_t saddr) {
+  return (unsigned long long)((saddr >> 4) & 0x3fffu) | ((unsigned long long)(128 >> 4) << 16) |
+         ((unsigned long long)(256 >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint32_t tmem_ld4(uint32_t addr, uint32_t (&r)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr));
+  return 0;
+}
+
+// 2^sc * sum_L A_L 2^(10 (4 - L)) from the raw FP32 words of the six levels
+__device__ __forceinline__ double combine_words(const uint32_t (&w)[kDigits], int sc, unsigned& bad) {
+  long long v = (long long)__float2int_rn(__uint_as_float(w[0])) << 40;
+  v += (long long)__float2int_rn(__uint_as_float(w[1])) << 30;
+  v += (long long)__float2int_rn(__uint_as_float(w[2])) << 20;
+  v += (long long)__float2int_rn(__uint_as_float(w[3])) << 10;
+  v += (long long)__float2int_rn(__uint_as_float(w[4]));
+  v += (long long)(__float2int_rn(__uint_as_float(w[5])) >> 10);
+  if (v == 0) return 0.0;
+  const double d = __ll2double_rn(v);
+  const int hi = __double2hiint(d);
+  const int e = ((hi >> 20) & 0x7ff) + sc;
+  bad |= (e < 1 || e > 2046) ? 1u : 0u;
+  return __hiloint2double(hi + (sc << 20), __double2loint(d));
+}
+
+template <bool CONTIG>
+__global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_constant__ TcParams p) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int t = threadIdx.x, warp = t >> 5;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+  const uint32_t sA = sbase, sB = sbase + kSmemB, bar = sbase + kSmemBar;
+  volatile uint32_t* tslot = reinterpret_cast<volatile uint32_t*>(smem + kSmemTmem);
+  volatile uint32_t* flag = reinterpret_cast<volatile uint32_t*>(smem + kSmemFlag);
+  {  // PTM digit planes (the B operand)
+    const uint4* src = reinterpret_cast<const uint4*>(&p.bplanes[0][0]);
+    uint4* dst = reinterpret_cast<uint4*>(smem + kSmemB);
+    for (int i = t; i < kDigits * kPlaneB / 16; i += kUBlock) dst[i] = src[i];
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + kSmemTmem),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);
+  const int64_t sai = p.sai, sbi = p.sbi;
+
+  auto base = [&](uint64_t grp) -> int64_t {
+    const uint64_t t1 = fdiv(grp, p.div_z);
+    const uint64_t z = grp - t1 * p.div_z.d;
+    const uint64_t x = fdiv(t1, p.div_y);
+    const uint64_t y = t1 - x * p.div_y.d;
+    return (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
+  };
+
+  uint32_t phase = 0;
+  bool timed_out = false;
+  for (uint64_t tile = blockIdx.x; tile < p.n_tiles; tile += gridDim.x) {
+    const uint64_t gi = tile * kUBlock + t;
+    const bool live = gi < p.n_groups;
+    int64_t b = 0;
+    if (CONTIG) {
+      b = base(tile * kUBlock) + t;  // 128 consecutive z of one (x, y)
+    } else if (live) {
+      b = base(gi);
+    }
+    double x[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = live ? p.in[b + (k >> 2) * sai + (k & 3) * sbi] : 0.0;
+    unsigned emax = 1u, bad = 0u;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const unsigned h = (unsigned)__double2hiint(x[k]);
+      emax = max(emax, exp_eff(h));
+      bad |= ((h >> 20) & 0x7ffu) == 0x7ffu ? 1u : 0u;
+    }
+    unsigned long long u[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      u[k] = fixed_biased((unsigned)__double2hiint(x[k]), (unsigned)__double2loint(x[k]), emax);
+    // this thread's row of the six input digit planes
+#pragma unroll
+    for (int j = 0; j < kDigits; ++j) {
+      const int pos = 10 * (kDigits - 1 - j);
+      uint4 lo4, hi4;
+      lo4.x = digit_pair(u[0], u[1], pos);
+      lo4.y = digit_pair(u[2], u[3], pos);
+      lo4.z = digit_pair(u[4], u[5], pos);
+      lo4.w = digit_pair(u[6], u[7], pos);
+      hi4.x = digit_pair(u[8], u[9], pos);
+      hi4.y = digit_pair(u[10], u[11], pos);
+      hi4.z = digit_pair(u[12], u[13], pos);
+      hi4.w = digit_pair(u[14], u[15], pos);
+      *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 0)) = lo4;
+      *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 8)) = hi4;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int i = 0; i < kDigits; ++i) {
+        const unsigned long long bdesc = smem_desc(sB + i * kPlaneB);
+#pragma unroll
+        for (int j = 0; i + j < kDigits; ++j) {
+          const unsigned long long adesc = smem_desc(sA + j * kPlaneA);
+          const uint32_t d = tmem + 16u * (uint32_t)(i + j);
+          const uint32_t accumulate = i > 0 ? 1u : 0u;  // pair (0, L) starts level L
+          asm volatile(
+              "{ .reg .pred q; setp.ne.u32 q, %4, 0; "
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q; }" ::"r"(d),
+              "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+              : "memory");
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                   : "memory");
+      uint32_t done = 0;
+      for (long long spin = 0; spin < kSpinLimit && !done; ++spin)
+        asm volatile(
+            "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; selp.u32 %0, 1, 0, q; }"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+      *flag = done;
+    }
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (*flag == 0u) {  // the same value in every thread
+      timed_out = true;
+      break;
+    }
+    // outputs: rows r = 4c .. 4c + 3, six levels each
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      uint32_t w[kDigits][4];
+#pragma unroll
+      for (int l = 0; l < kDigits; ++l) tmem_ld4(tlane + 16u * l + 4u * c, w[l]);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      double y[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t lv[kDigits] = {w[0][q], w[1][q], w[2][q], w[3][q], w[4][q], w[5][q]};
+        y[q] = combine_words(lv, (int)emax - 1022 + p.row_exp[4 * c + q], bad);
+      }
+      if (live) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int r = 4 * c + q;
+          p.out[b + (r >> 2) * p.sao + (r & 3) * p.sbo] = y[q];
+        }
+      }
+    }
+    if (bad && live) {
+      // inf / nan inputs or results outside the normal range: this group's
+      // outputs again in native FP64
+#pragma unroll 1
+      for (int r = 0; r < 16; ++r) {
+        double a = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < 16; ++k) a = fma(p.ptm[r][k], p.in[b + (k >> 2) * sai + (k & 3) * sbi], a);
+        p.out[b + (r >> 2) * p.sao + (r & 3) * p.sbo] = a;
+      }
+    }
+  }
+  if (timed_out && t == 0) {
+    if (p.status) atomicOr(p.status, QSGB_DEV_TIMEOUT);
+    // bounded wait for the MMAs still in flight before the memory is freed
+    uint32_t done = 0;
+    for (long long spin = 0; spin < kSpinLimit && !done; ++spin)
+      asm volatile(
+          "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; selp.u32 %0, 1, 0, q; }"
+          : "=r"(done)
+          : "r"(bar), "r"(phase ^ 1u)
+          : "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
 // FP16 bit pattern of an integer |v| <= 2048 (exact).
 unsigned short half_bits(int v) {
   if (v == 0) return 0;
@@ -299,6 +536,11 @@ int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, 
     split_row(op + 16 * r, p.digits, r, p.row_exp);
     for (int k = 0; k < 16; ++k) p.ptm[r][k] = op[16 * r + k];
   }
+  // the same digits in the operand layout: element (row r, column k) of plane
+  // i at byte core_off(r, k)
+  for (int i = 0; i < kDigits; ++i)
+    for (int r = 0; r < 16; ++r)
+      for (int k = 0; k < 16; ++k) p.bplanes[i][core_off(r, k) / 2] = p.digits[i][r][k];
   p.in = static_cast<const double*>(in);
   p.out = static_cast<double*>(out);
   p.status = status;
@@ -314,15 +556,29 @@ int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, 
   p.sao = p.sai;
   p.syo = p.syi;
   p.sxo = p.sxi;
-  const bool contig = Z % 8 == 0;
-  p.pair_store = contig && (uintptr_t)out % 16 == 0 ? 1 : 0;
-  const uint64_t warps_needed = p.n_tiles;
-  const uint64_t blocks = (warps_needed + kBlock / 32 - 1) / (kBlock / 32);
-  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count() * 8));
-  if (contig)
-    apply16_tc_kernel<true><<<grid, kBlock, 0, stream>>>(p);
-  else
-    apply16_tc_kernel<false><<<grid, kBlock, 0, stream>>>(p);
+  static const bool mma_sync = [] {
+    const char* v = std::getenv("QSGB_TC_KERNEL");
+    return v && std::strcmp(v, "mma_sync") == 0;
+  }();
+  if (mma_sync) {
+    // warp-level form: tiles of 8 groups per warp
+    const bool contig = Z % 8 == 0;
+    p.pair_store = contig && (uintptr_t)out % 16 == 0 ? 1 : 0;
+    const uint64_t blocks = (p.n_tiles + kBlock / 32 - 1) / (kBlock / 32);
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count() * 8));
+    if (contig)
+      apply16_tc_kernel<true><<<grid, kBlock, 0, stream>>>(p);
+    else
+      apply16_tc_kernel<false><<<grid, kBlock, 0, stream>>>(p);
+    return launch_status();
+  }
+  // tcgen05 form: tiles of 128 groups per block, at most 4 blocks per SM
+  p.n_tiles = (p.n_groups + kUBlock - 1) / kUBlock;
+  const bool contig = Z % kUBlock == 0;
+  auto kern = contig ? apply16_umma_kernel<true> : apply16_umma_kernel<false>;
+  QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem));
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(p.n_tiles, (uint64_t)sm_count() * 4));
+  kern<<<grid, kUBlock, kUmmaSmem, stream>>>(p);
   return launch_status();
 }
 

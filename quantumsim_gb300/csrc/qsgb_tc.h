@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "qsgb_common.cuh"
@@ -27,8 +28,14 @@ struct TcParams {
   int pair_store;  // groups 2c, 2c+1 are adjacent and 16-byte aligned
   int row_exp[16];                                // Ep_r - 1022 - 54 per row
   unsigned short digits[kDigits][16][16];         // FP16 digit planes e_i[r][k]
+  alignas(16) unsigned short bplanes[kDigits][256];  // the same in the shared-memory
+                                                     // operand layout of tcgen05.mma
+                                                     // (copied with 16-byte loads)
   double ptm[16][16];                             // the op matrix (FP64 fallback)
 };
+
+static_assert(offsetof(TcParams, bplanes) % 16 == 0, "16-byte loads of the operand planes");
+static_assert(sizeof(TcParams) <= 32764, "kernel parameter limit");
 
 // The op matrix is 16 x 16 without inf or nan.
 bool eligible(const double* op, int kin, int kout);
