@@ -348,20 +348,44 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
     return (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
   };
 
-  uint32_t phase = 0;
-  bool timed_out = false;
-  for (uint64_t tile = blockIdx.x; tile < p.n_tiles; tile += gridDim.x) {
+  // a tile's inputs: this thread's group, 16 values; with unit stride along
+  // the last target (Z == 1, tensors 16-byte aligned) as 8 16-byte loads
+  auto load_tile = [&](uint64_t tile, double (&x)[16], int64_t& b, bool& live) {
     const uint64_t gi = tile * kUBlock + t;
-    const bool live = gi < p.n_groups;
-    int64_t b = 0;
+    live = tile < p.n_tiles && gi < p.n_groups;
+    b = 0;
     if (CONTIG) {
-      b = base(tile * kUBlock) + t;  // 128 consecutive z of one (x, y)
+      if (tile < p.n_tiles) b = base(tile * kUBlock) + t;  // 128 consecutive z of one (x, y)
     } else if (live) {
       b = base(gi);
     }
-    double x[16];
+    if (!live) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k) x[k] = live ? p.in[b + (k >> 2) * sai + (k & 3) * sbi] : 0.0;
+      for (int k = 0; k < 16; ++k) x[k] = 0.0;
+    } else if (p.vec_z1) {
+#pragma unroll
+      for (int ka = 0; ka < 4; ++ka) {
+        const double2 v0 = *reinterpret_cast<const double2*>(p.in + b + ka * sai);
+        const double2 v1 = *reinterpret_cast<const double2*>(p.in + b + ka * sai + 2);
+        x[4 * ka] = v0.x;
+        x[4 * ka + 1] = v0.y;
+        x[4 * ka + 2] = v1.x;
+        x[4 * ka + 3] = v1.y;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) x[k] = p.in[b + (k >> 2) * sai + (k & 3) * sbi];
+    }
+  };
+
+  uint32_t phase = 0;
+  bool timed_out = false;
+  double x[16];
+  int64_t b;
+  bool live;
+  uint64_t tile = blockIdx.x;
+  load_tile(tile, x, b, live);
+  for (; tile < p.n_tiles; tile += gridDim.x) {
     unsigned emax = 1u, bad = 0u;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
@@ -369,25 +393,27 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
       emax = max(emax, exp_eff(h));
       bad |= ((h >> 20) & 0x7ffu) == 0x7ffu ? 1u : 0u;
     }
-    unsigned long long u[16];
+    {
+      unsigned long long u[16];
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
-      u[k] = fixed_biased((unsigned)__double2hiint(x[k]), (unsigned)__double2loint(x[k]), emax);
-    // this thread's row of the six input digit planes
+      for (int k = 0; k < 16; ++k)
+        u[k] = fixed_biased((unsigned)__double2hiint(x[k]), (unsigned)__double2loint(x[k]), emax);
+      // this thread's row of the six input digit planes
 #pragma unroll
-    for (int j = 0; j < kDigits; ++j) {
-      const int pos = 10 * (kDigits - 1 - j);
-      uint4 lo4, hi4;
-      lo4.x = digit_pair(u[0], u[1], pos);
-      lo4.y = digit_pair(u[2], u[3], pos);
-      lo4.z = digit_pair(u[4], u[5], pos);
-      lo4.w = digit_pair(u[6], u[7], pos);
-      hi4.x = digit_pair(u[8], u[9], pos);
-      hi4.y = digit_pair(u[10], u[11], pos);
-      hi4.z = digit_pair(u[12], u[13], pos);
-      hi4.w = digit_pair(u[14], u[15], pos);
-      *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 0)) = lo4;
-      *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 8)) = hi4;
+      for (int j = 0; j < kDigits; ++j) {
+        const int pos = 10 * (kDigits - 1 - j);
+        uint4 lo4, hi4;
+        lo4.x = digit_pair(u[0], u[1], pos);
+        lo4.y = digit_pair(u[2], u[3], pos);
+        lo4.z = digit_pair(u[4], u[5], pos);
+        lo4.w = digit_pair(u[6], u[7], pos);
+        hi4.x = digit_pair(u[8], u[9], pos);
+        hi4.y = digit_pair(u[10], u[11], pos);
+        hi4.z = digit_pair(u[12], u[13], pos);
+        hi4.w = digit_pair(u[14], u[15], pos);
+        *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 0)) = lo4;
+        *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 8)) = hi4;
+      }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -411,6 +437,14 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                    : "memory");
+    }
+    // the next tile's inputs load while the tensor cores and the
+    // recombination work on this one
+    const int64_t bc = b;
+    const bool livec = live;
+    double xn[16];
+    load_tile(tile + gridDim.x, xn, b, live);
+    if (t == 0) {
       uint32_t done = 0;
       for (long long spin = 0; spin < kSpinLimit && !done; ++spin)
         asm volatile(
@@ -428,7 +462,7 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
       timed_out = true;
       break;
     }
-    // outputs: rows r = 4c .. 4c + 3, six levels each
+    // outputs: rows r = 4c .. 4c + 3 = (ra = c, rb = 0 .. 3), six levels each
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       uint32_t w[kDigits][4];
@@ -441,25 +475,29 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
         const uint32_t lv[kDigits] = {w[0][q], w[1][q], w[2][q], w[3][q], w[4][q], w[5][q]};
         y[q] = combine_words(lv, (int)emax - 1022 + p.row_exp[4 * c + q], bad);
       }
-      if (live) {
+      if (livec) {
+        if (p.vec_z1) {
+          *reinterpret_cast<double2*>(p.out + bc + c * p.sao) = make_double2(y[0], y[1]);
+          *reinterpret_cast<double2*>(p.out + bc + c * p.sao + 2) = make_double2(y[2], y[3]);
+        } else {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int r = 4 * c + q;
-          p.out[b + (r >> 2) * p.sao + (r & 3) * p.sbo] = y[q];
+          for (int q = 0; q < 4; ++q) p.out[bc + c * p.sao + q * p.sbo] = y[q];
         }
       }
     }
-    if (bad && live) {
+    if (bad && livec) {
       // inf / nan inputs or results outside the normal range: this group's
       // outputs again in native FP64
 #pragma unroll 1
       for (int r = 0; r < 16; ++r) {
         double a = 0.0;
 #pragma unroll 1
-        for (int k = 0; k < 16; ++k) a = fma(p.ptm[r][k], p.in[b + (k >> 2) * sai + (k & 3) * sbi], a);
-        p.out[b + (r >> 2) * p.sao + (r & 3) * p.sbo] = a;
+        for (int k = 0; k < 16; ++k) a = fma(p.ptm[r][k], p.in[bc + (k >> 2) * sai + (k & 3) * sbi], a);
+        p.out[bc + (r >> 2) * p.sao + (r & 3) * p.sbo] = a;
       }
     }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = xn[k];
   }
   if (timed_out && t == 0) {
     if (p.status) atomicOr(p.status, QSGB_DEV_TIMEOUT);
@@ -575,6 +613,7 @@ int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, 
   // tcgen05 form: tiles of 128 groups per block, at most 4 blocks per SM
   p.n_tiles = (p.n_groups + kUBlock - 1) / kUBlock;
   const bool contig = Z % kUBlock == 0;
+  p.vec_z1 = Z == 1 && (uintptr_t)in % 16 == 0 && (uintptr_t)out % 16 == 0 ? 1 : 0;
   auto kern = contig ? apply16_umma_kernel<true> : apply16_umma_kernel<false>;
   QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem));
   const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(p.n_tiles, (uint64_t)sm_count() * 4));

@@ -26,6 +26,8 @@ struct TcParams {
   int64_t sxi, syi, sai, sbi;  // strides of (x, a, y, b) in elements; z stride 1
   int64_t sxo, syo, sao, sbo;
   int pair_store;  // groups 2c, 2c+1 are adjacent and 16-byte aligned
+  int vec_z1;      // Z == 1 and both tensors 16-byte aligned: a group's
+                   // runs along the last target move as 16-byte vectors
   int row_exp[16];                                // Ep_r - 1022 - 54 per row
   unsigned short digits[kDigits][16][16];         // FP16 digit planes e_i[r][k]
   alignas(16) unsigned short bplanes[kDigits][256];  // the same in the shared-memory
