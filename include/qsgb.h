@@ -57,7 +57,7 @@ extern "C" {
                               cores (FP64 values split into FP16 digit
                               planes, exact FP32 sums); other PTMs as AUTO.
                               AUTO itself sends 16 x 16 host PTMs with more
-                              than 12 non-zero terms per row there */
+                              than 8 non-zero terms per row there */
 
 /* ---- PTM layout flags ---- */
 #define QSGB_PTM_SWAPPED 1    /* 2-qudit PTM given in order (less significant,

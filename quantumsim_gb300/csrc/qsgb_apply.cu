@@ -611,14 +611,15 @@ void op_matrix(const double* ptm, int da_out, int db_out, int da_in, int db_in, 
 
 // Under QSGB_ARITH_AUTO, a 16 x 16 PTM goes to the tensor cores when its
 // rows average more non-zero terms (above 2^-52 of the largest entry) than
-// QSGB_TC_MIN_TERMS (default 12).  Measured on GB300 (14 qubits): the
-// tensor-core kernel streams 1.6-1.8 TB/s whatever the density; the
-// specialised float-float kernels 2.46 TB/s at 11.25 terms per row and
-// 1.39-1.65 TB/s when dense.
+// QSGB_TC_MIN_TERMS (default 8).  Measured on GB300 (14 qubits): the
+// tensor-core kernel streams 3.35-3.46 TB/s whatever the density (2.77 when
+// the less significant target is the last qubit); the specialised
+// float-float kernels 4.0 TB/s at 6.12 terms per row, 2.46 at 11.25 and
+// 1.39-1.65 when dense, which crosses 3.3 TB/s near 8 terms per row.
 bool tc_wanted(const double* op) {
   static const double min_terms = [] {
     const char* v = std::getenv("QSGB_TC_MIN_TERMS");
-    return v ? std::atof(v) : 12.0;
+    return v ? std::atof(v) : 8.0;
   }();
   double amax = 0.0;
   for (int i = 0; i < 256; ++i) amax = std::max(amax, std::fabs(op[i]));

@@ -23,7 +23,7 @@ Numerical semantics follow ``PauliVectorNumpy`` (the reference oracle):
 FP64 storage: by default (``arith='auto'``) the kernel computes each PTM
 row either with native FP64 FMAs or in float-float arithmetic (48-bit
 significand) on the FP32 pipes, whichever keeps the launch closest to the
-HBM bound, and sends dense 16 x 16 PTMs (more than 12 non-zero terms per
+HBM bound, and sends dense 16 x 16 PTMs (more than 8 non-zero terms per
 row) to the tensor cores, where FP64 values split into FP16 digit planes
 are multiplied with exact FP32 sums; ``arith='f64'`` forces native FP64
 everywhere, ``arith='df64'`` float-float for every row with more than one
@@ -174,7 +174,7 @@ class PauliVectorGB300(_Base):
     arith : 'auto' | 'df64' | 'f64' | 'f32' | 'tc'
         Arithmetic of apply_ptm ('auto': per PTM, the specialised
         float-float / FP64 kernels, or the tensor cores for 16 x 16 PTMs
-        with more than 12 terms per row; 'tc': every 16 x 16 PTM on the
+        with more than 8 terms per row; 'tc': every 16 x 16 PTM on the
         tensor cores; f32 for FP32 storage).
     """
 
