@@ -245,38 +245,29 @@ __global__ void __launch_bounds__(kBlock) apply16_tc_kernel(const __grid_constan
 }
 
 // ---------------------------------------------------------------------------
-// tcgen05 form: 128 groups per tile (the M of one tcgen05.mma), two threads
-// per group, the six level accumulators in tensor memory.
+// tcgen05 form: one thread per group, 128 groups per tile (the M of one
+// tcgen05.mma), the six level accumulators in tensor memory.
 //
-// Per tile, thread (row, h) -- row = group of the tile, h = half -- loads
-// the group's 8 inputs k in [8h, 8h + 8), exchanges its partial exponent
-// maximum with the other half through shared memory, splits its inputs and
-// writes its 16 bytes of each of the six input digit planes (the A operand,
-// 128 x 16 FP16 each) to shared memory.  One thread issues the 21
-// tcgen05.mma.kind::f16 (A = input plane j, B = PTM plane i, both K-major,
-// D = level i + j: 16 FP32 columns of tensor memory) and commits them to an
-// mbarrier.  After the barrier each thread reads its group's lane of the
-// accumulators for its outputs r in [8h, 8h + 8) with tcgen05.ld (warp w
-// reaches lanes 32 (w % 4) .. + 31, which are its groups) and recombines
-// them.  The next tile's inputs are loaded while the tensor cores and the
-// recombination work on the current one.  Shared-memory operands use the
-// canonical K-major layout without swizzling: core matrices of 8 rows x 16
-// bytes (8 FP16 along K) at (row / 8) * 256 + (k / 8) * 128, so the
-// descriptors carry a leading (K) byte offset of 128 and a stride (8-row)
-// byte offset of 256.
-constexpr int kUTile = 128;   // groups per tile
-constexpr int kUBlock = 256;  // threads: two per group
+// Per tile, each thread loads its group's 16 inputs, splits them and writes
+// its row of the six input digit planes (the A operand, 128 x 16 FP16 each)
+// to shared memory; one thread issues the 21 tcgen05.mma.kind::f16 (A = input
+// plane j, B = PTM plane i, both K-major, D = level i + j: 16 FP32 columns of
+// tensor memory) and commits them to an mbarrier; after the barrier each warp
+// reads its 32 lanes (groups) of the accumulators with tcgen05.ld and
+// recombines its outputs.  Shared-memory operands use the canonical K-major
+// layout without swizzling: core matrices of 8 rows x 16 bytes (8 FP16 along
+// K) at (row / 8) * 256 + (k / 8) * 128, so the descriptors carry a leading
+// (K) byte offset of 128 and a stride (8-row) byte offset of 256.
+constexpr int kUBlock = 128;
 constexpr int kPlaneA = 128 * 16 * 2;  // one input digit plane: 128 rows x 16 FP16
 constexpr int kPlaneB = 16 * 16 * 2;   // one PTM digit plane: 16 rows x 16 FP16
 constexpr int kSmemB = kDigits * kPlaneA;             // 24576
 constexpr int kSmemBar = kSmemB + kDigits * kPlaneB;  // 27648
 constexpr int kSmemTmem = kSmemBar + 8;
 constexpr int kSmemFlag = kSmemTmem + 4;
-constexpr int kSmemEx = kSmemBar + 64;  // uint32 [2 buffers][2 halves][128 rows]
 // the dynamic allocation is padded so that at most 4 blocks share an SM:
 // 4 x 128 tensor-memory columns fill its 512
 constexpr int kUmmaSmem = 56 * 1024;
-static_assert(kSmemEx + 2 * 2 * kUTile * 4 <= kUmmaSmem, "shared memory layout");
 constexpr unsigned kTmemCols = 128;  // 6 levels x 16 columns, a power of two
 // kind::f16 instruction descriptor: D F32 (bits 4-5 = 1), A and B F16 (0),
 // both K-major, N / 8 at bits 17-22, M / 16 at bits 24-28
@@ -295,10 +286,11 @@ __device__ __forceinline__ unsigned long long smem_desc(uint32_t saddr) {
          ((unsigned long long)(256 >> 4) << 32) | (1ull << 46);
 }
 
-__device__ __forceinline__ void tmem_ld4(uint32_t addr, uint32_t (&r)[4]) {
+__device__ __forceinline__ uint32_t tmem_ld4(uint32_t addr, uint32_t (&r)[4]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(addr));
+  return 0;
 }
 
 // 2^sc * sum_L A_L 2^(10 (4 - L)) from the raw FP32 words of the six levels
@@ -317,29 +309,14 @@ __device__ __forceinline__ double combine_words(const uint32_t (&w)[kDigits], in
   return __hiloint2double(hi + (sc << 20), __double2loint(d));
 }
 
-// partial exponent maximum (low 16 bits) and inf / nan flag (bit 16) of
-// this thread's 8 inputs
-__device__ __forceinline__ uint32_t partial_scale(const double (&x)[8]) {
-  unsigned emax = 1u, bad = 0u;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const unsigned h = (unsigned)__double2hiint(x[i]);
-    emax = max(emax, exp_eff(h));
-    bad |= ((h >> 20) & 0x7ffu) == 0x7ffu ? 1u : 0u;
-  }
-  return emax | (bad << 16);
-}
-
 template <bool CONTIG>
-__global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_constant__ TcParams p) {
+__global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_constant__ TcParams p) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int t = threadIdx.x, warp = t >> 5;
-  const int row = t & (kUTile - 1), h = t >> 7;  // group of the tile, half
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
   const uint32_t sA = sbase, sB = sbase + kSmemB, bar = sbase + kSmemBar;
   volatile uint32_t* tslot = reinterpret_cast<volatile uint32_t*>(smem + kSmemTmem);
   volatile uint32_t* flag = reinterpret_cast<volatile uint32_t*>(smem + kSmemFlag);
-  uint32_t* ex = reinterpret_cast<uint32_t*>(smem + kSmemEx);  // [buffer][half][row]
   {  // PTM digit planes (the B operand)
     const uint4* src = reinterpret_cast<const uint4*>(&p.bplanes[0][0]);
     uint4* dst = reinterpret_cast<uint4*>(smem + kSmemB);
@@ -355,7 +332,14 @@ __global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_c
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);
   const int64_t sai = p.sai, sbi = p.sbi;
+
   auto base = [&](uint64_t grp) -> int64_t {
     const uint64_t t1 = fdiv(grp, p.div_z);
     const uint64_t z = grp - t1 * p.div_z.d;
@@ -363,75 +347,72 @@ __global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_c
     const uint64_t y = t1 - x * p.div_y.d;
     return (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
   };
-  // this thread's 8 inputs of a tile: (ka, kb) = (2h + i / 4, i % 4); with
-  // unit stride along the last target (Z == 1, tensors 16-byte aligned) as
-  // four 16-byte loads
-  auto load_tile = [&](uint64_t tile, double (&x)[8], int64_t& b, bool& live) {
-    const uint64_t gi = tile * kUTile + row;
+
+  // a tile's inputs: this thread's group, 16 values; with unit stride along
+  // the last target (Z == 1, tensors 16-byte aligned) as 8 16-byte loads
+  auto load_tile = [&](uint64_t tile, double (&x)[16], int64_t& b, bool& live) {
+    const uint64_t gi = tile * kUBlock + t;
     live = tile < p.n_tiles && gi < p.n_groups;
     b = 0;
     if (CONTIG) {
-      if (tile < p.n_tiles) b = base(tile * kUTile) + row;  // 128 consecutive z of one (x, y)
+      if (tile < p.n_tiles) b = base(tile * kUBlock) + t;  // 128 consecutive z of one (x, y)
     } else if (live) {
       b = base(gi);
     }
     if (!live) {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) x[i] = 0.0;
+      for (int k = 0; k < 16; ++k) x[k] = 0.0;
     } else if (p.vec_z1) {
 #pragma unroll
-      for (int a2 = 0; a2 < 2; ++a2) {
-        const double* q = p.in + b + (2 * h + a2) * sai;
-        const double2 v0 = *reinterpret_cast<const double2*>(q);
-        const double2 v1 = *reinterpret_cast<const double2*>(q + 2);
-        x[4 * a2] = v0.x;
-        x[4 * a2 + 1] = v0.y;
-        x[4 * a2 + 2] = v1.x;
-        x[4 * a2 + 3] = v1.y;
+      for (int ka = 0; ka < 4; ++ka) {
+        const double2 v0 = *reinterpret_cast<const double2*>(p.in + b + ka * sai);
+        const double2 v1 = *reinterpret_cast<const double2*>(p.in + b + ka * sai + 2);
+        x[4 * ka] = v0.x;
+        x[4 * ka + 1] = v0.y;
+        x[4 * ka + 2] = v1.x;
+        x[4 * ka + 3] = v1.y;
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) x[i] = p.in[b + (2 * h + (i >> 2)) * sai + (i & 3) * sbi];
+      for (int k = 0; k < 16; ++k) x[k] = p.in[b + (k >> 2) * sai + (k & 3) * sbi];
     }
   };
 
-  uint32_t phase = 0, buf = 0;
+  uint32_t phase = 0;
   bool timed_out = false;
-  double x[8];
+  double x[16];
   int64_t b;
   bool live;
   uint64_t tile = blockIdx.x;
   load_tile(tile, x, b, live);
-  ex[(0 * 2 + h) * kUTile + row] = partial_scale(x);
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tslot;
-  const uint32_t tlane = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-
   for (; tile < p.n_tiles; tile += gridDim.x) {
-    // the group's scale: both halves' partial maxima (written before the
-    // last barrier)
-    const uint32_t mine = ex[(buf * 2 + h) * kUTile + row];
-    const uint32_t other = ex[(buf * 2 + (h ^ 1)) * kUTile + row];
-    const unsigned emax = max(mine & 0xffffu, other & 0xffffu);
-    unsigned bad = ((mine | other) >> 16) & 1u;
-    {
-      unsigned long long u[8];
+    unsigned emax = 1u, bad = 0u;
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
-        u[i] = fixed_biased((unsigned)__double2hiint(x[i]), (unsigned)__double2loint(x[i]), emax);
-      // this thread's 16 bytes (k in [8h, 8h + 8)) of each input digit plane
+    for (int k = 0; k < 16; ++k) {
+      const unsigned h = (unsigned)__double2hiint(x[k]);
+      emax = max(emax, exp_eff(h));
+      bad |= ((h >> 20) & 0x7ffu) == 0x7ffu ? 1u : 0u;
+    }
+    {
+      unsigned long long u[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        u[k] = fixed_biased((unsigned)__double2hiint(x[k]), (unsigned)__double2loint(x[k]), emax);
+      // this thread's row of the six input digit planes
 #pragma unroll
       for (int j = 0; j < kDigits; ++j) {
         const int pos = 10 * (kDigits - 1 - j);
-        uint4 v;
-        v.x = digit_pair(u[0], u[1], pos);
-        v.y = digit_pair(u[2], u[3], pos);
-        v.z = digit_pair(u[4], u[5], pos);
-        v.w = digit_pair(u[6], u[7], pos);
-        *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(row, 8 * h)) = v;
+        uint4 lo4, hi4;
+        lo4.x = digit_pair(u[0], u[1], pos);
+        lo4.y = digit_pair(u[2], u[3], pos);
+        lo4.z = digit_pair(u[4], u[5], pos);
+        lo4.w = digit_pair(u[6], u[7], pos);
+        hi4.x = digit_pair(u[8], u[9], pos);
+        hi4.y = digit_pair(u[10], u[11], pos);
+        hi4.z = digit_pair(u[12], u[13], pos);
+        hi4.w = digit_pair(u[14], u[15], pos);
+        *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 0)) = lo4;
+        *reinterpret_cast<uint4*>(smem + j * kPlaneA + core_off(t, 8)) = hi4;
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -457,11 +438,11 @@ __global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_c
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                    : "memory");
     }
-    // the next tile's inputs load (and their partial scales go to the other
-    // buffer) while the tensor cores and the recombination work on this one
+    // the next tile's inputs load while the tensor cores and the
+    // recombination work on this one
     const int64_t bc = b;
     const bool livec = live;
-    double xn[8];
+    double xn[16];
     load_tile(tile + gridDim.x, xn, b, live);
     if (t == 0) {
       uint32_t done = 0;
@@ -474,8 +455,6 @@ __global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_c
       *flag = done;
     }
     phase ^= 1u;
-    buf ^= 1u;
-    ex[(buf * 2 + h) * kUTile + row] = partial_scale(xn);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -483,10 +462,9 @@ __global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_c
       timed_out = true;
       break;
     }
-    // outputs r = 4c .. 4c + 3 = (ra = c, rb = 0 .. 3) for c = 2h, 2h + 1
+    // outputs: rows r = 4c .. 4c + 3 = (ra = c, rb = 0 .. 3), six levels each
 #pragma unroll
-    for (int c2 = 0; c2 < 2; ++c2) {
-      const int c = 2 * h + c2;
+    for (int c = 0; c < 4; ++c) {
       uint32_t w[kDigits][4];
 #pragma unroll
       for (int l = 0; l < kDigits; ++l) tmem_ld4(tlane + 16u * l + 4u * c, w[l]);
@@ -508,10 +486,10 @@ __global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_c
       }
     }
     if (bad && livec) {
-      // inf / nan inputs or results outside the normal range: this thread's
-      // outputs of the group again in native FP64
+      // inf / nan inputs or results outside the normal range: this group's
+      // outputs again in native FP64
 #pragma unroll 1
-      for (int r = 8 * h; r < 8 * h + 8; ++r) {
+      for (int r = 0; r < 16; ++r) {
         double a = 0.0;
 #pragma unroll 1
         for (int k = 0; k < 16; ++k) a = fma(p.ptm[r][k], p.in[bc + (k >> 2) * sai + (k & 3) * sbi], a);
@@ -519,7 +497,7 @@ __global__ void __launch_bounds__(kUBlock, 4) apply16_umma_kernel(const __grid_c
       }
     }
 #pragma unroll
-    for (int i = 0; i < 8; ++i) x[i] = xn[i];
+    for (int k = 0; k < 16; ++k) x[k] = xn[k];
   }
   if (timed_out && t == 0) {
     if (p.status) atomicOr(p.status, QSGB_DEV_TIMEOUT);
@@ -633,8 +611,8 @@ int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, 
     return launch_status();
   }
   // tcgen05 form: tiles of 128 groups per block, at most 4 blocks per SM
-  p.n_tiles = (p.n_groups + kUTile - 1) / kUTile;
-  const bool contig = Z % kUTile == 0;
+  p.n_tiles = (p.n_groups + kUBlock - 1) / kUBlock;
+  const bool contig = Z % kUBlock == 0;
   p.vec_z1 = Z == 1 && (uintptr_t)in % 16 == 0 && (uintptr_t)out % 16 == 0 ? 1 : 0;
   auto kern = contig ? apply16_umma_kernel<true> : apply16_umma_kernel<false>;
   QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem));
