@@ -776,6 +776,29 @@ def run_profile_tc(args):
     print(json.dumps({'profile_case': 'tc', 'trace': s.trace()}))
 
 
+def run_profile_take(args):
+    """Small workload for ncu captures of the take-along-an-axis kernels
+    (reduce_basis / project): 8 qutrits (9^8 float64 entries, 344 MB); 3x
+    [reduce_basis 9 -> 3 of qutrit 3 (rows of 6561 entries, 16-byte units),
+    the same of qutrit 7 (rows of one entry), project 9 -> 1 of qutrit 5 of
+    the reduced vector].  Launch order: 3 per repetition."""
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases
+    g3 = bases.general(3)
+    comp = [g3.computational_basis_indices[i] for i in range(3)]
+    q = qg.PauliVectorGB300([g3] * 8, force=True)
+    q._data.copy_(torch.rand_like(q._data))
+    for _ in range(3):
+        red = torch.ops.qsgb.take_axis(q._data, 3, comp)
+        torch.ops.qsgb.take_axis(q._data, 7, comp)
+        torch.ops.qsgb.take_axis(red, 5, [comp[1]])
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_case': 'take', 'sum': float(red.sum())}))
+
+
 def run_profile_qutrits(args):
     """Small workload for ncu captures of the qutrit kernels: 8 qutrits
     (9^8 float64 entries, 344 MB); one layer of 9x9 PTMs on every qutrit, then
@@ -908,8 +931,8 @@ def main():
     ap.add_argument('--traffic', type=float, default=0.0,
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', nargs='?', const='apply',
-                    choices=['apply', 'qutrits', 'tc', 'batched', 'circuit',
-                             'adjoint2'],
+                    choices=['apply', 'qutrits', 'tc', 'take', 'batched',
+                             'circuit', 'adjoint2'],
                     help='run a small ncu profiling workload and exit')
     ap.add_argument('--profile-qubits', type=int, default=12)
     ap.add_argument('--profile-pair', default='5,6',
@@ -917,7 +940,7 @@ def main():
     args = ap.parse_args()
     if args.profile_case:
         {'apply': run_profile_case, 'qutrits': run_profile_qutrits,
-         'tc': run_profile_tc,
+         'tc': run_profile_tc, 'take': run_profile_take,
          'batched': run_profile_batched, 'adjoint2': run_profile_adjoint2,
          'circuit': run_profile_circuit}[args.profile_case](args)
         return
