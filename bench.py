@@ -643,9 +643,10 @@ def run_ops_config():
     out['reduce_basis_9to3_ms'] = tr * 1e3
     out['reduce_basis_gbs'] = 2 * n_red * 8 / tr / 1e9
     out['project_ms'] = tp * 1e3
-    # the take kernel alone (CUDA events on the launching stream, 20
-    # launches on resident tensors larger than L2): bytes = entries kept,
-    # read and written
+    # the take kernel alone: 20 launches on resident tensors larger than L2,
+    # replayed from a CUDA graph (a project kernel runs for a few us, less
+    # than one host call) and timed with CUDA events on the replaying
+    # stream; bytes = entries kept, read and written
     q = qg.PauliVectorGB300([g3] * 8, force=True)
     q._data.copy_(torch.rand_like(q._data))
     red = torch.ops.qsgb.take_axis(q._data, 3, comp)
@@ -653,17 +654,27 @@ def run_ops_config():
             ('reduce_basis_9to3', q._data, 3, comp, n_red),
             ('project_9to1', red, 5, [comp[1]], 9 ** 6 * 3)):
         torch.ops.qsgb.take_axis(x, axis, idx)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(graph, stream=side):
+                for _ in range(20):
+                    torch.ops.qsgb.take_axis(x, axis, idx)
+        torch.cuda.current_stream().wait_stream(side)
+        graph.replay()
         stream = torch.cuda.current_stream()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for _ in range(20):
-            torch.ops.qsgb.take_axis(x, axis, idx)
+        graph.replay()
         b.record(stream)
         torch.cuda.synchronize()
         dt = a.elapsed_time(b) / 1e3 / 20
         out[name + '_kernel_us'] = dt * 1e6
         out[name + '_kernel_gbs'] = 2 * n_keep * 8 / dt / 1e9
+        del graph
     del q, red
     out['workload'] = ('14 qubits FP64 (diagonal, trace, meas_prob, '
                        'partial_trace keeping 4, renormalize); 8 qutrits '
