@@ -707,6 +707,22 @@ def run_grad_config():
                 torch.cuda.synchronize()
                 ts.append(time.perf_counter() - t0)
             out[name + ('_fused' if fuse else '') + '_step_s'] = min(ts[1:])
+        # the circuit part of the step replayed from a CUDA graph (PTMs
+        # built on the GPU; fused layers)
+        step = fitting.GraphedGradient(m, target, dtype=dtype,
+                                       checkpoint_every=8, fuse=True)
+        ts = []
+        for rep in range(5):
+            p = {k: v.clone().to(step.dev).requires_grad_(True)
+                 for k, v in m.init.items()}
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            loss = step.step(p)
+            float(loss)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        out[name + '_graph_step_s'] = min(ts[1:])
+        del step
     return out
 
 

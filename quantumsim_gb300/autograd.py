@@ -37,12 +37,19 @@ class ApplyPTM(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, x, ptm, qudits, arith):
-        ptm_host = ptm.detach().to('cpu', torch.float64).contiguous()
-        max_terms = 0  # host PTM: counted by the library
-        out = torch.ops.qsgb.apply_ptm(x.contiguous(), ptm_host, list(qudits),
+        if ptm.is_cuda:
+            # a PTM built on the device stays there: the generic kernel reads
+            # it, nothing synchronises, and the call can be captured in a
+            # CUDA graph
+            ptm_k = ptm.detach().to(torch.float64).contiguous()
+        else:
+            # a host PTM: its sparsity pattern selects a specialised kernel
+            ptm_k = ptm.detach().to('cpu', torch.float64).contiguous()
+        max_terms = 0  # all entries (device) / counted by the library (host)
+        out = torch.ops.qsgb.apply_ptm(x.contiguous(), ptm_k, list(qudits),
                                        arith, max_terms, False)
         ctx.save_for_backward(x)
-        ctx.ptm_host = ptm_host
+        ctx.ptm_host = ptm_k
         ctx.ptm_device = ptm.device
         ctx.qudits = tuple(qudits)
         ctx.arith = arith
@@ -123,7 +130,9 @@ def diagonal_diff(x, bases):
 def checkpointed(layers, x, every=8):
     """Apply `layers` (callables state -> state) in order, keeping only the
     states at every `every`-th layer for the backward pass; the forward of
-    each segment is recomputed when its gradient is needed."""
+    each segment is recomputed when its gradient is needed (the layers draw
+    no random numbers, so no RNG state is saved, which also keeps the
+    checkpoints capturable in a CUDA graph)."""
     if every <= 0 or not torch.is_grad_enabled():
         for f in layers:
             x = f(x)
@@ -136,5 +145,6 @@ def checkpointed(layers, x, every=8):
                 state = f(state)
             return state
 
-        x = torch.utils.checkpoint.checkpoint(run, x, use_reentrant=False)
+        x = torch.utils.checkpoint.checkpoint(run, x, use_reentrant=False,
+                                              preserve_rng_state=False)
     return x

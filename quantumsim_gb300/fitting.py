@@ -74,10 +74,13 @@ class NoisyCircuitModel:
         return [(i, i + 1) for i in range(off, self.n - 1, 2)]
 
     def build_ptms(self, p):
-        """All PTMs of the circuit (float64 CPU tensors, differentiable)."""
+        """All PTMs of the circuit (float64 tensors on the parameters'
+        device, differentiable): one-qubit PTMs (n_layers, n, 4, 4) and CZs
+        (n - 1, 4, 4, 4, 4)."""
         n, nl = self.n, self.n_layers
-        groups = torch.arange(nl) % self.n_groups
-        angles = self.base_angles + p['angle_offset'][groups]
+        dev = p['angle_offset'].device
+        groups = torch.arange(nl, device=dev) % self.n_groups
+        angles = self.base_angles.to(dev) + p['angle_offset'][groups]
         axes = [ax for row in self.axes for ax in row]
         rot = P.rotations_batched(axes, angles.reshape(-1), self.basis)
         gamma, lam = P.damping_rates(p['t1'] * 1e-6, p['t2'] * 1e-6, T_GATE)
@@ -93,7 +96,10 @@ class NoisyCircuitModel:
         CZ (R_i (x) R_i+1) per pair, built in torch, and the rotations of
         unpaired qubits alone -- 6 applications per layer instead of 15 for
         10 qubits."""
-        one_q, cz = self.build_ptms(p)
+        return self.layers_of(*self.build_ptms(p), apply_fn, fuse=fuse)
+
+    def layers_of(self, one_q, cz, apply_fn, fuse=False):
+        """layers() for given one-qubit and CZ PTM tensors."""
         fns = []
         for l in range(self.n_layers):
             if fuse:
@@ -154,6 +160,82 @@ class NoisyCircuitModel:
         prob = self.probabilities(p, **kw)
         t = target.to(prob.device)
         return torch.sum(t * (torch.log(t) - torch.log(prob)))
+
+
+class GraphedGradient:
+    """Gradient steps of ``model.loss`` with the circuit replayed from a CUDA
+    graph.
+
+    A step builds the PTMs from the parameters on the GPU (eagerly: a few
+    dozen small torch operations), copies them into the graph's static PTM
+    tensors, replays the graph -- the circuit forward with checkpoints every
+    `checkpoint_every` layers, the diagonal, the KL loss and the whole
+    backward pass down to the PTMs: about a thousand kernel launches that
+    would otherwise each cost a host call -- and finishes the backward
+    through the PTM builder into the parameters.  The PTMs stay on the
+    device, so the apply kernels read them from device memory and nothing
+    synchronises inside the graph.
+
+    ``step(p)`` returns the loss as a device scalar and leaves the gradients
+    in ``p[name].grad`` (accumulated, as in ``loss.backward()``)."""
+
+    def __init__(self, model, target, dtype=torch.float64, checkpoint_every=8,
+                 fuse=True, device=None):
+        from .autograd import Diagonal, diagonal_indices
+        self.model = model
+        self.dev = torch.device(device) if device is not None else \
+            torch.device('cuda', torch.cuda.current_device())
+        self.dtype = dtype
+        self.every = checkpoint_every
+        self.fuse = fuse
+        n = model.n
+        self.target = target.to(self.dev, torch.float64)
+        self.x0 = model.initial_state(self.dev, dtype)
+        self.flat = torch.from_numpy(
+            diagonal_indices([model.basis] * n)).to(self.dev)
+        self.idx_off, self.idx_list = [0], []
+        for _ in range(n):
+            self.idx_list += [int(model.basis.computational_basis_indices[i])
+                              for i in range(2)]
+            self.idx_off.append(len(self.idx_list))
+        self._diag = Diagonal
+        with torch.no_grad():
+            p0 = {k: v.to(self.dev) for k, v in model.init.items()}
+            one_q, cz = model.build_ptms(p0)
+        self.one_q = one_q.detach().clone().requires_grad_(True)
+        self.cz = cz.detach().clone().requires_grad_(True)
+        # warm up on a side stream (compiles nothing: device PTMs use the
+        # precompiled kernels), then capture
+        side = torch.cuda.Stream(self.dev)
+        side.wait_stream(torch.cuda.current_stream(self.dev))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                self.one_q.grad = self.cz.grad = None
+                self._loss().backward()
+            self.one_q.grad = self.cz.grad = None
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=side):
+                self.loss = self._loss()
+                self.loss.backward()
+        torch.cuda.current_stream(self.dev).wait_stream(side)
+
+    def _loss(self):
+        fns = self.model.layers_of(
+            self.one_q, self.cz,
+            lambda s, pt, qs: apply_ptm_diff(s, pt, *qs), fuse=self.fuse)
+        x = checkpointed(fns, self.x0.clone(), self.every)
+        prob = self._diag.apply(x, self.flat, self.idx_off, self.idx_list)
+        t = self.target
+        return torch.sum(t * (torch.log(t) - torch.log(prob)))
+
+    def step(self, p):
+        one_q, cz = self.model.build_ptms(p)
+        with torch.no_grad():
+            self.one_q.copy_(one_q)
+            self.cz.copy_(cz)
+        self.graph.replay()
+        torch.autograd.backward([one_q, cz], [self.one_q.grad, self.cz.grad])
+        return self.loss
 
 
 def _einsum_apply(x, ptm, qs):
