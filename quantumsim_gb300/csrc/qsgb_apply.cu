@@ -111,7 +111,9 @@ struct SmemLayout {
   size_t offin_off;         // int64[kin]
   size_t offout_off;        // int64[kout]
   size_t cnt_off;           // int[kout] term counts
-  size_t red_off;           // double[34] reduction scratch + flag
+  size_t srt_off;           // int[kout] term counts in ascending order
+  size_t ord_off;           // int[kout] rows in descending weight order
+  size_t red_off;           // double[36] reduction scratch, flag, plan values
   size_t total;
 };
 
@@ -140,8 +142,12 @@ SmemLayout make_layout(int kin, int kout, int max_terms, int tile, size_t item_b
   o = align_up(o + (size_t)kout * sizeof(int64_t), 16);
   L.cnt_off = o;
   o = align_up(o + (size_t)kout * sizeof(int), 16);
+  L.srt_off = o;
+  o = align_up(o + (size_t)kout * sizeof(int), 16);
+  L.ord_off = o;
+  o = align_up(o + (size_t)kout * sizeof(int), 16);
   L.red_off = o;
-  o = align_up(o + 34 * sizeof(double), 16);
+  o = align_up(o + 36 * sizeof(double), 16);
   L.total = o;
   return L;
 }
@@ -277,33 +283,45 @@ __device__ bool build_terms(const ApplyParams& p, const SmemLayout& L, unsigned 
     cnt[r] = c;
   }
   __syncthreads();
+  // The row plan, computed by all threads (every block repeats it for a
+  // device PTM, so it must cost little): term counts in ascending order, the
+  // dp / df split (AUTO), each row's mode and term offset, then rows in
+  // descending weight order and their longest-first assignment to the row
+  // groups.  Ties are broken by row index throughout, as a sequential pass
+  // would.
+  int* srt = reinterpret_cast<int*>(smem + L.srt_off);  // counts, ascending
+  int* ord = reinterpret_cast<int*>(smem + L.ord_off);  // rows, weight descending
+  int* ctl = reinterpret_cast<int*>(red + 34);          // cut, ties
+  for (int r = tid; r < p.kout; r += nthr) {
+    const int c = cnt[r];
+    int rank = 0;
+    for (int q = 0; q < p.kout; ++q) {
+      const int cq = cnt[q];
+      rank += (cq < c || (cq == c && q < r)) ? 1 : 0;
+    }
+    srt[rank] = c;
+  }
+  __syncthreads();
   if (tid == 0) {
     int cut = 1 << 30, ties = 0;
     if (p.arith == QSGB_ARITH_AUTO) {
-      int sorted[kMaxK];
-      for (int r = 0; r < p.kout; ++r) {
-        int v = cnt[r], j = r;
-        while (j > 0 && sorted[j - 1] > v) {
-          sorted[j] = sorted[j - 1];
-          --j;
-        }
-        sorted[j] = v;
-      }
       // n_dp = number of rows (ascending count) computed in FP64; rows with
       // one term are always dp.  Evaluate every n_dp incrementally.
       SplitCost sc{0.f, 0.f, 0.f, 5.f * (p.kin + p.kout), (float)(p.kin + p.kout) * (float)sizeof(T) / 23.f};
       for (int i = 0; i < p.kout; ++i) {
-        if (sorted[i] == 1)
+        const int v = srt[i];
+        if (v == 1)
           sc.add_dp(1, 1.f);
-        else if (sorted[i] > 1)
-          sc.add_df(sorted[i], 1.f);
+        else if (v > 1)
+          sc.add_df(v, 1.f);
       }
       float best = sc.time();
       int n_dp_best = 0;
       for (int i = 0; i < p.kout; ++i) {
-        if (sorted[i] > 1) {
-          sc.add_df(sorted[i], -1.f);
-          sc.add_dp(sorted[i], 1.f);
+        const int v = srt[i];
+        if (v > 1) {
+          sc.add_df(v, -1.f);
+          sc.add_dp(v, 1.f);
         }
         const float c = sc.time();
         if (c < best * 0.999f) {
@@ -311,12 +329,23 @@ __device__ bool build_terms(const ApplyParams& p, const SmemLayout& L, unsigned 
           n_dp_best = i + 1;
         }
       }
-      cut = n_dp_best > 0 ? sorted[n_dp_best - 1] : -1;
-      for (int i = 0; i < n_dp_best; ++i) ties += sorted[i] == cut;
+      cut = n_dp_best > 0 ? srt[n_dp_best - 1] : -1;
+      for (int i = 0; i < n_dp_best; ++i) ties += srt[i] == cut;
     }
-    int t = 0;
-    for (int r = 0; r < p.kout; ++r) {
+    ctl[0] = cut;
+    ctl[1] = ties;
+  }
+  __syncthreads();
+  {
+    const int cut = ctl[0], ties = ctl[1];
+    for (int r = tid; r < p.kout; r += nthr) {
       const int c = cnt[r];
+      int beg = 0, tie_rank = 0;
+      for (int q = 0; q < r; ++q) {
+        const int cq = cnt[q];
+        beg += cq;
+        tie_rank += cq == cut ? 1 : 0;
+      }
       int mode;
       if (c == 0)
         mode = kZero;
@@ -328,44 +357,58 @@ __device__ bool build_terms(const ApplyParams& p, const SmemLayout& L, unsigned 
         mode = kDF;
       else if (c < cut)
         mode = kDP;
-      else if (c == cut && ties > 0) {
+      else if (c == cut && tie_rank < ties)  // the first `ties` rows of count `cut`
         mode = kDP;
-        --ties;
-      } else
+      else
         mode = kDF;
-      rows[r].beg = t;
-      rows[r].end = t + c;
+      rows[r].beg = beg;
+      rows[r].end = beg + c;
       rows[r].mode = mode;
       rows[r].pad = 0;
-      t += c;
+      if (r == p.kout - 1) *flag = (beg + c > p.max_terms) ? 1 : 0;
     }
-    *flag = (t > p.max_terms) ? 1 : 0;
+  }
+  __syncthreads();
+  for (int r = tid; r < p.kout; r += nthr) {
+    const int w = row_weight(rows[r].mode, cnt[r]);
+    int rank = 0;
+    for (int q = 0; q < p.kout; ++q) {
+      const int wq = row_weight(rows[q].mode, cnt[q]);
+      rank += (wq > w || (wq == w && q < r)) ? 1 : 0;
+    }
+    ord[rank] = r;
+  }
+  __syncthreads();
+  if (tid == 0) {
     // balance rows over the row groups (longest processing time first)
     const int rg_count = kWarps / p.iw;
-    int load[kWarps];
-    for (int g = 0; g < rg_count; ++g) {
+    int load[kWarps], n[kWarps];
+#pragma unroll
+    for (int g = 0; g < kWarps; ++g) {
       load[g] = 0;
-      rg_n[g] = 0;
+      n[g] = 0;
     }
-    bool used[kMaxK];
-    for (int r = 0; r < p.kout; ++r) used[r] = false;
     for (int step = 0; step < p.kout; ++step) {
-      int rbest = -1, wbest = -1;
-      for (int r = 0; r < p.kout; ++r) {
-        if (used[r]) continue;
-        const int w = row_weight(rows[r].mode, cnt[r]);
-        if (w > wbest) {
-          wbest = w;
-          rbest = r;
+      const int r = ord[step];
+      const int w = row_weight(rows[r].mode, cnt[r]);
+      int g = 0, lg = load[0];
+#pragma unroll
+      for (int h = 1; h < kWarps; ++h)
+        if (h < rg_count && load[h] < lg) {
+          g = h;
+          lg = load[h];
         }
-      }
-      used[rbest] = true;
-      int g = 0;
-      for (int h = 1; h < rg_count; ++h)
-        if (load[h] < load[g]) g = h;
-      load[g] += wbest;
-      rg_rows[g * p.kout + rg_n[g]++] = rbest;
+#pragma unroll
+      for (int h = 0; h < kWarps; ++h)
+        if (h == g) {
+          rg_rows[h * p.kout + n[h]] = r;
+          load[h] += w;
+          ++n[h];
+        }
     }
+#pragma unroll
+    for (int g = 0; g < kWarps; ++g)
+      if (g < rg_count) rg_n[g] = n[g];
   }
   __syncthreads();
   if (*flag) {
@@ -573,8 +616,10 @@ int launch_apply(ApplyParams& p, cudaStream_t stream) {
   }
   if (L.total > 227 * 1024) return QSGB_ERR_UNSUPPORTED;
   p.iw = iw;
-  if (L.total > 48 * 1024)
-    QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
+  {
+    const int st = allow_dynamic_smem((const void*)kern, (int)L.total);
+    if (st != QSGB_OK) return st;
+  }
   int occ = 0;
   QSGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlock, L.total));
   if (occ < 1) return QSGB_ERR_UNSUPPORTED;
@@ -626,6 +671,16 @@ bool tc_wanted(const double* op) {
   int n = 0;
   for (int i = 0; i < 256; ++i) n += std::fabs(op[i]) > amax * 0x1p-52 ? 1 : 0;
   return n > min_terms * 16.0;
+}
+
+// Under QSGB_ARITH_AUTO every 16 x 16 device PTM goes to the tensor cores
+// (QSGB_TC_DEVICE=0: to the generic kernel instead).
+bool tc_device_auto() {
+  static const bool on = [] {
+    const char* v = std::getenv("QSGB_TC_DEVICE");
+    return !(v && std::strcmp(v, "0") == 0);
+  }();
+  return on;
 }
 
 // mode: kLaunch, kPrepare (compile and load, launch nothing) or kCompileOnly
@@ -776,13 +831,22 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   p.div_z = make_fastdiv((uint64_t)(pair ? Z / 2 : Z));
   p.n_items = (uint64_t)X * Y * (pair ? Z / 2 : Z);
   cudaStream_t s = as_stream(stream);
-  // 0. dense 16 x 16 PTMs (two full-basis qubits) on the tensor cores
-  if (dtype == QSGB_F64 && (flags & QSGB_PTM_HOST) && da_in == 4 && db_in == 4 && da_out == 4 && db_out == 4) {
-    double op[256];
-    op_matrix(ptm, 4, 4, 4, 4, flags & 3, op);
-    if (tc::eligible(op, 16, 16) && (tc_arith == QSGB_ARITH_TC || (tc_arith == QSGB_ARITH_AUTO && tc_wanted(op)))) {
-      if (mode != kLaunch) return QSGB_ERR_UNSUPPORTED;  // precompiled: nothing to prepare
-      return tc::launch(op, in, out, (uint64_t)X, (uint64_t)Y, (uint64_t)Z, status, s);
+  // 0. dense 16 x 16 PTMs (two full-basis qubits) on the tensor cores; a
+  // device PTM's values are not read on the host, so every 16 x 16 device
+  // PTM goes there under 'auto' (the generic kernel would run its 256 terms
+  // per group in float-float or FP64)
+  if (dtype == QSGB_F64 && da_in == 4 && db_in == 4 && da_out == 4 && db_out == 4) {
+    if (flags & QSGB_PTM_HOST) {
+      double op[256];
+      op_matrix(ptm, 4, 4, 4, 4, flags & 3, op);
+      if (tc::eligible(op, 16, 16) &&
+          (tc_arith == QSGB_ARITH_TC || (tc_arith == QSGB_ARITH_AUTO && tc_wanted(op)))) {
+        if (mode != kLaunch) return QSGB_ERR_UNSUPPORTED;  // precompiled: nothing to prepare
+        return tc::launch(op, in, out, (uint64_t)X, (uint64_t)Y, (uint64_t)Z, status, s);
+      }
+    } else if (tc_arith == QSGB_ARITH_TC || (tc_arith == QSGB_ARITH_AUTO && tc_device_auto())) {
+      if (mode != kLaunch) return QSGB_ERR_UNSUPPORTED;
+      return tc::launch_device(ptm, flags & 3, in, out, (uint64_t)X, (uint64_t)Y, (uint64_t)Z, status, s);
     }
   }
   // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)

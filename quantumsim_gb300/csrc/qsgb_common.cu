@@ -1,6 +1,9 @@
 // Library-wide helpers: status strings, ABI version, device SM count.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <vector>
+
 #include "qsgb_common.cuh"
 
 namespace qsgb {
@@ -15,6 +18,30 @@ int sm_count() {
     cache[dev] = n;
   }
   return cache[dev];
+}
+
+int allow_dynamic_smem(const void* func, int bytes) {
+  if (bytes <= 48 * 1024) return QSGB_OK;
+  struct Entry {
+    const void* func;
+    int dev, bytes;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> table;
+  int dev = 0;
+  QSGB_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  for (Entry& e : table) {
+    if (e.func == func && e.dev == dev) {
+      if (bytes <= e.bytes) return QSGB_OK;
+      QSGB_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+      e.bytes = bytes;
+      return QSGB_OK;
+    }
+  }
+  QSGB_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  table.push_back({func, dev, bytes});
+  return QSGB_OK;
 }
 
 int launch_status() {

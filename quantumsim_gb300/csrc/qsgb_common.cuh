@@ -23,6 +23,11 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 int sm_count();         // cached per device
 int launch_status();    // cudaGetLastError mapped to a status code
+// Let kernel `func` take `bytes` of dynamic shared memory on the current
+// device.  The attribute only ever grows: a launch captured in a CUDA graph
+// with a larger size stays launchable after later launches of the same
+// kernel ask for less.
+int allow_dynamic_smem(const void* func, int bytes);
 
 // ---------------------------------------------------------------------------
 // Unsigned 64-bit division by an invariant divisor (Granlund & Montgomery,

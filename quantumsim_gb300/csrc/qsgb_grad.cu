@@ -5,11 +5,30 @@
 // qsgb_apply.cu.)  The reference has no differentiation; the operation is
 // the adjoint of quantumsim/pauli_vectors/numpy.py:50-64.
 //
-// Stage 1: each block walks tiles of 32 groups, stages the tile's inputs and
-// output-gradients in shared memory and accumulates its share of the Kout*Kin
-// entries (FP64 accumulation; FP32 storage multiplies in FP32 inside a tile
-// and carries the tile sums in FP64).  Stage 2 adds the per-block partials in
-// a fixed order (deterministic).
+// The reduction has Kout * Kin multiply-adds per group: 256 for a two-qubit
+// PTM, ~16 per streamed element.  On GB300 the FP64 pipe issues ~0.6 T FMA/s,
+// so native FP64 products cap the kernel near 0.3 TB/s; the products here run
+// on the FP32 pipes in float-float ("df64") arithmetic instead:
+//
+// Stage 1: each block walks tiles of `tg` groups.  The tile's inputs and
+// output-gradients are loaded (the next tile's into registers while the
+// current one is computed), split into float pairs hi + lo (48 significant
+// bits, qsgb_split_f64) and staged in shared memory group-major.  Each thread
+// owns a 4 x 4 micro-tile of (r, k) entries and a slice of the tile's groups
+// and accumulates exact products hi*hi + the cross terms in float-float
+// (qsgb_df_fma: error ~2^-47 per product, relative).  At the end of the block
+// the slices' float-float sums are added in a fixed order and rounded to
+// one double per entry (integer operations, qsgb_df_to_double).
+//
+// A tile holding a non-zero value outside [2^-100, 2^40] (where products or
+// their sums could leave the float range) is computed in native FP64 instead,
+// from global memory, into FP64 accumulators in shared memory that join the
+// block's sums at the end.  Products of in-range values below the float
+// range (< 2^-126) lose their low bits: the absolute error per product stays
+// below 2^-149.
+//
+// Stage 2 adds the per-block partials of each entry in a fixed order
+// (deterministic).
 #include <algorithm>
 
 #include "qsgb_common.cuh"
@@ -17,107 +36,342 @@
 namespace qsgb {
 namespace {
 
-constexpr int kTile = 32;
 constexpr int kGradBlock = 256;
-constexpr int kMaxPerThread = 26;  // ceil(6561 / 256)
+constexpr int kLoads = 8;  // (Kin + Kout) * tg <= kLoads * kGradBlock
+constexpr int kStage2Entries = 32;
+constexpr int kStage2Slices = 32;
 
 struct GradParams {
   const void* x;
   const void* g;
   int kin, kout, db_in, db_out;
-  uint64_t n_groups;
+  int kpi, kpo;    // float2 row lengths of the staged inputs / gradients
+  int tg;          // groups per tile (a power of two dividing kGradBlock)
+  int nmt_c, nmt;  // 4 x 4 micro-tiles along k, in total
+  int slices;      // group slices of a tile (micro-tiles <= kGradBlock)
+  uint64_t n_groups, n_tiles;
   FastDiv div_z, div_y;
   int64_t sxi, syi, sai, sbi;
   int64_t sxo, syo, sao, sbo;
+  // shared-memory byte offsets
+  int off_gb, off_offs, off_fb, off_red2, off_flag, smem;
 };
 
-unsigned grad_blocks(uint64_t n_groups) {
-  const uint64_t tiles = (n_groups + kTile - 1) / kTile;
+unsigned grad_blocks(uint64_t n_groups, int tg) {
+  const uint64_t tiles = (n_groups + tg - 1) / tg;
   return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)sm_count() * 2));
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kGradBlock) grad_stage1(GradParams p, double* __restrict__ part) {
+// groups per tile: the largest power of two <= kGradBlock with
+// rows * tg <= kLoads * kGradBlock
+int grad_tile(int rows) {
+  int tg = kGradBlock;
+  while (tg > 1 && rows * tg > kLoads * kGradBlock) tg >>= 1;
+  return tg;
+}
+
+__device__ __forceinline__ unsigned out_of_band(double v) {
+  const unsigned h = (unsigned)__double2hiint(v);
+  const unsigned e = (h >> 20) & 0x7ffu;
+  const bool nz = ((h << 1) | (unsigned)__double2loint(v)) != 0u;
+  return (nz && (e < 923u || e > 1063u)) ? 1u : 0u;  // 2^-100 <= |v| <= 2^40
+}
+
+__device__ __forceinline__ unsigned out_of_band(float v) {
+  const unsigned b = __float_as_uint(v) & 0x7fffffffu;
+  const unsigned e = b >> 23;
+  return (b != 0u && (e < 27u || e > 167u)) ? 1u : 0u;
+}
+
+__device__ __forceinline__ float2 split_pair(double v) {
+  float h, l;
+  unsigned ignored = 0;
+  qsgb_split_f64(v, h, l, ignored);
+  return make_float2(h, l);
+}
+
+__device__ __forceinline__ float2 split_pair(float v) { return make_float2(v, 0.0f); }
+
+// (s, c) += (s2, c2), float-float
+__device__ __forceinline__ void df_add(float& s, float& c, float s2, float c2) {
+  const float r = s + s2;
+  const float bp = r - s;
+  const float err = (s - (r - bp)) + (s2 - bp);
+  s = r;
+  c += err + c2;
+}
+
+template <typename T, int MPT>
+__global__ void __launch_bounds__(kGradBlock) grad_stage1(const __grid_constant__ GradParams p,
+                                                          double* __restrict__ part) {
   extern __shared__ __align__(16) unsigned char smem[];
-  T* xs = reinterpret_cast<T*>(smem);            // [kin][kTile]
-  T* gs = xs + (size_t)p.kin * kTile;            // [kout][kTile]
+  float2* sx = reinterpret_cast<float2*>(smem);  // [tg][kpi]
+  float2* sg = sx + p.tg * p.kpi;                // [tg][kpo]
+  int64_t* gb = reinterpret_cast<int64_t*>(smem + p.off_gb);      // [2][tg]: group bases (in, out), -1 idle
+  int64_t* offs = reinterpret_cast<int64_t*>(smem + p.off_offs);  // [kin + kout] row offsets
+  double* fb = reinterpret_cast<double*>(smem + p.off_fb);        // [kGradBlock][MPT][16] FP64 tiles
+  int* fb_any = reinterpret_cast<int*>(smem + p.off_flag);
   const T* __restrict__ X = static_cast<const T*>(p.x);
   const T* __restrict__ G = static_cast<const T*>(p.g);
-  const int E = p.kin * p.kout;
-  double acc[kMaxPerThread];
+  const int t = threadIdx.x;
+  const int R = p.kin + p.kout;
+
+  // zero the staging area (padding rows stay zero) and the FP64 sums
+  {
+    float4* z = reinterpret_cast<float4*>(smem);
+    for (int i = t; i < p.off_gb / 16; i += kGradBlock) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    double* f = fb;
+    for (int i = t; i < kGradBlock * MPT * 16; i += kGradBlock) f[i] = 0.0;
+  }
+  for (int r = t; r < R; r += kGradBlock) {
+    if (r < p.kin) {
+      const int ka = r / p.db_in, kb = r - ka * p.db_in;
+      offs[r] = ka * p.sai + kb * p.sbi;
+    } else {
+      const int rr = r - p.kin, ra = rr / p.db_out, rb = rr - ra * p.db_out;
+      offs[r] = ra * p.sao + rb * p.sbo;
+    }
+  }
+  if (t == 0) *fb_any = 0;
+  __syncthreads();
+
+  // loader role: group gg_ld of the tile, rows r0_ld + j * rstep
+  const int gg_ld = t & (p.tg - 1);
+  const int r0_ld = t / p.tg, rstep = kGradBlock / p.tg;
+  T v[kLoads];
+  int64_t bin = -1, bout = -1;
+  auto fetch = [&](uint64_t tile) {
+    const uint64_t g = tile * p.tg + gg_ld;
+    const bool live = tile < p.n_tiles && g < p.n_groups;
+    bin = bout = -1;
+    if (live) {
+      const uint64_t t1 = fdiv(g, p.div_z);
+      const uint64_t z = g - t1 * p.div_z.d;
+      const uint64_t x = fdiv(t1, p.div_y);
+      const uint64_t y = t1 - x * p.div_y.d;
+      bin = (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
+      bout = (int64_t)x * p.sxo + (int64_t)y * p.syo + (int64_t)z;
+    }
 #pragma unroll
-  for (int j = 0; j < kMaxPerThread; ++j) acc[j] = 0.0;
-  const uint64_t n_tiles = (p.n_groups + kTile - 1) / kTile;
-  const int rows = p.kin + p.kout;
-  for (uint64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const uint64_t g0 = tile * kTile;
-    __syncthreads();
-    for (int i = threadIdx.x; i < rows * kTile; i += blockDim.x) {
-      const int row = i / kTile, gg = i - row * kTile;
-      const uint64_t g = g0 + gg;
-      T v = (T)0;
-      if (g < p.n_groups) {
-        const uint64_t t1 = fdiv(g, p.div_z);
-        const uint64_t z = g - t1 * p.div_z.d;
-        const uint64_t x = fdiv(t1, p.div_y);
-        const uint64_t y = t1 - x * p.div_y.d;
-        if (row < p.kin) {
-          const int ka = row / p.db_in, kb = row - ka * p.db_in;
-          v = X[(int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z + ka * p.sai + kb * p.sbi];
-        } else {
-          const int r = row - p.kin;
-          const int ra = r / p.db_out, rb = r - ra * p.db_out;
-          v = G[(int64_t)x * p.sxo + (int64_t)y * p.syo + (int64_t)z + ra * p.sao + rb * p.sbo];
+    for (int j = 0; j < kLoads; ++j) {
+      const int r = r0_ld + j * rstep;
+      v[j] = (T)0;
+      if (live && r < R) v[j] = r < p.kin ? X[bin + offs[r]] : G[bout + offs[r]];
+    }
+  };
+  auto stage = [&]() -> unsigned {
+    unsigned bad = 0;
+#pragma unroll
+    for (int j = 0; j < kLoads; ++j) {
+      const int r = r0_ld + j * rstep;
+      if (r < R) {
+        bad |= out_of_band(v[j]);
+        const float2 s = split_pair(v[j]);
+        if (r < p.kin)
+          sx[gg_ld * p.kpi + r] = s;
+        else
+          sg[gg_ld * p.kpo + (r - p.kin)] = s;
+      }
+    }
+    if (r0_ld == 0) {
+      gb[gg_ld] = bin;
+      gb[p.tg + gg_ld] = bout;
+    }
+    return bad;
+  };
+
+  // compute role: micro-tiles and group slice
+  int mt[MPT], r0[MPT], k0[MPT];
+  bool act[MPT];
+  int slice;
+  if (MPT == 1) {
+    mt[0] = t % p.nmt;
+    slice = t / p.nmt;
+    act[0] = slice < p.slices;
+  } else {
+    slice = 0;
+#pragma unroll
+    for (int m = 0; m < MPT; ++m) {
+      mt[m] = t + m * kGradBlock;
+      act[m] = mt[m] < p.nmt;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < MPT; ++m) {
+    r0[m] = (mt[m] / p.nmt_c) * 4;
+    k0[m] = (mt[m] % p.nmt_c) * 4;
+  }
+  float s[MPT][16], c[MPT][16];
+#pragma unroll
+  for (int m = 0; m < MPT; ++m)
+#pragma unroll
+    for (int q = 0; q < 16; ++q) s[m][q] = c[m][q] = 0.0f;
+
+  fetch(blockIdx.x);
+  for (uint64_t tile = blockIdx.x; tile < p.n_tiles; tile += gridDim.x) {
+    __syncthreads();  // the previous tile is consumed
+    const int bad = __syncthreads_or((int)stage());
+    fetch(tile + gridDim.x);  // in flight while this tile is computed
+    if (!bad) {
+#pragma unroll
+      for (int m = 0; m < MPT; ++m) {
+        if (!act[m]) continue;
+        for (int gg = slice; gg < p.tg; gg += p.slices) {
+          const float4 a01 = *reinterpret_cast<const float4*>(sg + gg * p.kpo + r0[m]);
+          const float4 a23 = *reinterpret_cast<const float4*>(sg + gg * p.kpo + r0[m] + 2);
+          const float4 b01 = *reinterpret_cast<const float4*>(sx + gg * p.kpi + k0[m]);
+          const float4 b23 = *reinterpret_cast<const float4*>(sx + gg * p.kpi + k0[m] + 2);
+          const float ah[4] = {a01.x, a01.z, a23.x, a23.z}, al[4] = {a01.y, a01.w, a23.y, a23.w};
+          const float bh[4] = {b01.x, b01.z, b23.x, b23.z}, bl[4] = {b01.y, b01.w, b23.y, b23.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) qsgb_df_fma(s[m][4 * i + j], c[m][4 * i + j], ah[i], al[i], bh[j], bl[j]);
         }
       }
-      xs[i] = v;  // xs and gs are contiguous: row < kin -> xs, else gs
-    }
-    __syncthreads();
+    } else {
+      // a value outside the float-float band: this tile in native FP64
+      if (t == 0) *fb_any = 1;
+#pragma unroll 1
+      for (int m = 0; m < MPT; ++m) {
+        if (!act[m]) continue;
+        double* acc = fb + ((int64_t)t * MPT + m) * 16;
+#pragma unroll 1
+        for (int gg = slice; gg < p.tg; gg += p.slices) {
+          const int64_t bi = gb[gg], bo = gb[p.tg + gg];
+          if (bi < 0) continue;
+          double a[4], b[4];
 #pragma unroll
-    for (int j = 0; j < kMaxPerThread; ++j) {
-      const int e = threadIdx.x + j * kGradBlock;
-      if (e < E) {
-        const int r = e / p.kin, k = e - r * p.kin;
-        const T* gr = gs + r * kTile;
-        const T* xk = xs + k * kTile;
-        T s = (T)0;
-#pragma unroll 8
-        for (int gg = 0; gg < kTile; ++gg) s = fma(gr[gg], xk[gg], s);
-        acc[j] += (double)s;
+          for (int i = 0; i < 4; ++i) {
+            a[i] = r0[m] + i < p.kout ? (double)G[bo + offs[p.kin + r0[m] + i]] : 0.0;
+            b[i] = k0[m] + i < p.kin ? (double)X[bi + offs[k0[m] + i]] : 0.0;
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[4 * i + j] = fma(a[i], b[j], acc[4 * i + j]);
+        }
       }
     }
   }
+
+  // block sums: slices in a fixed order, one double per entry
+  __syncthreads();
+  float2* red = reinterpret_cast<float2*>(smem);  // [kGradBlock][MPT][16], over the staging area
 #pragma unroll
-  for (int j = 0; j < kMaxPerThread; ++j) {
-    const int e = threadIdx.x + j * kGradBlock;
-    if (e < E) part[(int64_t)blockIdx.x * E + e] = acc[j];
+  for (int m = 0; m < MPT; ++m)
+#pragma unroll
+    for (int q = 0; q < 16; ++q) red[((int64_t)t * MPT + m) * 16 + q] = make_float2(s[m][q], c[m][q]);
+  __syncthreads();
+  const bool any_fb = *fb_any != 0;
+  const int E = p.kin * p.kout;
+  const int EP = p.nmt * 16;  // padded entries
+  float2* red2 = reinterpret_cast<float2*>(smem + p.off_red2);  // [chunks][EP] (MPT == 1)
+  double* fb2 = reinterpret_cast<double*>(smem + p.off_red2 + kGradBlock * sizeof(float2));
+  if (MPT == 1) {
+    // level 1: entry qp, slice chunk ch (slices ch, ch + nch, ...); with
+    // many slices (small PTMs) the chunks spread the sums over the block
+    const int nch = EP < kGradBlock ? kGradBlock / EP : 1;
+    for (int tq = t; tq < nch * EP; tq += kGradBlock) {
+      const int qp = tq % EP, ch = tq / EP;
+      const int mtq = qp >> 4, q = qp & 15;
+      float S = 0.0f, C = 0.0f;
+      double F = 0.0;
+      for (int sl = ch; sl < p.slices; sl += nch) {
+        const int64_t idx = ((int64_t)(sl * p.nmt + mtq)) * 16 + q;
+        const float2 v2 = red[idx];
+        df_add(S, C, v2.x, v2.y);
+        if (any_fb) F += fb[idx];
+      }
+      if (nch > 1) {
+        red2[ch * EP + qp] = make_float2(S, C);
+        fb2[ch * EP + qp] = F;
+      } else {
+        const int r = (mtq / p.nmt_c) * 4 + (q >> 2), k = (mtq % p.nmt_c) * 4 + (q & 3);
+        double d = qsgb_df_to_double(S, C);
+        if (any_fb) d += F;
+        if (r < p.kout && k < p.kin) part[(int64_t)blockIdx.x * E + r * p.kin + k] = d;
+      }
+    }
+    if (nch > 1) {
+      __syncthreads();
+      // level 2: the chunks of entry qp in order
+      for (int qp = t; qp < EP; qp += kGradBlock) {
+        const int mtq = qp >> 4, q = qp & 15;
+        float S = 0.0f, C = 0.0f;
+        double F = 0.0;
+        for (int ch = 0; ch < nch; ++ch) {
+          const float2 v2 = red2[ch * EP + qp];
+          df_add(S, C, v2.x, v2.y);
+          if (any_fb) F += fb2[ch * EP + qp];
+        }
+        const int r = (mtq / p.nmt_c) * 4 + (q >> 2), k = (mtq % p.nmt_c) * 4 + (q & 3);
+        double d = qsgb_df_to_double(S, C);
+        if (any_fb) d += F;
+        if (r < p.kout && k < p.kin) part[(int64_t)blockIdx.x * E + r * p.kin + k] = d;
+      }
+    }
+    return;
+  }
+  for (int qp = t; qp < EP; qp += kGradBlock) {
+    const int mtq = qp >> 4, q = qp & 15;
+    const int r = (mtq / p.nmt_c) * 4 + (q >> 2), k = (mtq % p.nmt_c) * 4 + (q & 3);
+    float S = 0.0f, C = 0.0f;
+    double F = 0.0;
+    {
+      const int tt = mtq % kGradBlock, m = mtq / kGradBlock;
+      const int64_t idx = ((int64_t)tt * MPT + m) * 16 + q;
+      const float2 v2 = red[idx];
+      S = v2.x;
+      C = v2.y;
+      if (any_fb) F = fb[idx];
+    }
+    double d = qsgb_df_to_double(S, C);
+    if (any_fb) d += F;
+    if (r < p.kout && k < p.kin) part[(int64_t)blockIdx.x * E + r * p.kin + k] = d;
   }
 }
 
-__global__ void grad_stage2(const double* __restrict__ part, int nblocks, int E, double* __restrict__ out) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= E) return;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += part[(int64_t)b * E + e];
-  out[e] = s;
+// out[e] = sum over blocks b of part[b][e]: kStage2Entries entries x
+// kStage2Slices block slices per thread block, slices added in order
+__global__ void __launch_bounds__(kStage2Entries* kStage2Slices)
+    grad_stage2(const double* __restrict__ part, int nblocks, int E, double* __restrict__ out) {
+  __shared__ double red[kStage2Slices][kStage2Entries + 1];
+  const int el = threadIdx.x % kStage2Entries, sl = threadIdx.x / kStage2Entries;
+  const int e = blockIdx.x * kStage2Entries + el;
+  double acc = 0.0;
+  if (e < E) {
+#pragma unroll 8
+    for (int b = sl; b < nblocks; b += kStage2Slices) acc += part[(int64_t)b * E + e];
+  }
+  red[sl][el] = acc;
+  __syncthreads();
+  if (sl == 0 && e < E) {
+    double s = 0.0;
+    for (int i = 0; i < kStage2Slices; ++i) s += red[i][el];
+    out[e] = s;
+  }
 }
 
-int grad_common(const void* x_in, const void* g_out, double* dptm, int64_t da_out, int64_t db_out, int64_t da_in,
-                int64_t db_in, int64_t X, int64_t Y, int64_t Z, int dtype, void* scratch, int64_t scratch_bytes,
-                void* stream) {
-  if (!x_in || !g_out || !dptm) return QSGB_ERR_INVALID;
-  if (da_out < 1 || db_out < 1 || da_in < 1 || db_in < 1 || X < 1 || Y < 1 || Z < 1) return QSGB_ERR_INVALID;
-  if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
-  const int64_t kin = da_in * db_in, kout = da_out * db_out;
-  if (kin * kout > (int64_t)kMaxPerThread * kGradBlock) return QSGB_ERR_UNSUPPORTED;
-  GradParams p;
+GradParams make_params(const void* x_in, const void* g_out, int64_t da_out, int64_t db_out, int64_t da_in,
+                       int64_t db_in, int64_t X, int64_t Y, int64_t Z) {
+  GradParams p{};
   p.x = x_in;
   p.g = g_out;
-  p.kin = (int)kin;
-  p.kout = (int)kout;
+  const int kin = (int)(da_in * db_in), kout = (int)(da_out * db_out);
+  p.kin = kin;
+  p.kout = kout;
   p.db_in = (int)db_in;
   p.db_out = (int)db_out;
+  const int pi = (kin + 3) / 4 * 4, po = (kout + 3) / 4 * 4;
+  p.kpi = pi + 2;  // + 16 bytes: consecutive groups start 4 banks apart
+  p.kpo = po + 2;
+  p.tg = grad_tile(kin + kout);
+  p.nmt_c = pi / 4;
+  p.nmt = (pi / 4) * (po / 4);
+  p.slices = p.nmt <= kGradBlock ? kGradBlock / p.nmt : 1;
   p.n_groups = (uint64_t)X * Y * Z;
+  p.n_tiles = (p.n_groups + p.tg - 1) / p.tg;
   p.div_z = make_fastdiv((uint64_t)Z);
   p.div_y = make_fastdiv((uint64_t)Y);
   p.sbi = Z;
@@ -128,23 +382,58 @@ int grad_common(const void* x_in, const void* g_out, double* dptm, int64_t da_ou
   p.syo = db_out * Z;
   p.sao = Y * db_out * Z;
   p.sxo = da_out * Y * db_out * Z;
-  const unsigned nb = grad_blocks(p.n_groups);
+  const int mpt = p.nmt <= kGradBlock ? 1 : 2;
+  const size_t stagebytes = (size_t)p.tg * (p.kpi + p.kpo) * sizeof(float2);
+  const size_t redbytes = (size_t)kGradBlock * mpt * 16 * sizeof(float2);
+  size_t o = (std::max(stagebytes, redbytes) + 15) / 16 * 16;
+  p.off_gb = (int)o;
+  o += 2 * (size_t)p.tg * sizeof(int64_t);
+  p.off_offs = (int)o;
+  o += ((size_t)(kin + kout) * sizeof(int64_t) + 15) / 16 * 16;
+  p.off_fb = (int)o;
+  o += (size_t)kGradBlock * mpt * 16 * sizeof(double);
+  p.off_red2 = (int)o;  // level-1 sums: kGradBlock float2 + kGradBlock double
+  o += (size_t)kGradBlock * (sizeof(float2) + sizeof(double));
+  p.off_flag = (int)o;
+  o += 16;
+  p.smem = (int)o;
+  return p;
+}
+
+template <typename T, int MPT>
+int launch_stage1(const GradParams& p, unsigned nb, double* part, cudaStream_t s) {
+  auto kern = grad_stage1<T, MPT>;
+  const int st = allow_dynamic_smem((const void*)kern, p.smem);
+  if (st != QSGB_OK) return st;
+  kern<<<nb, kGradBlock, p.smem, s>>>(p, part);
+  return QSGB_OK;
+}
+
+int grad_common(const void* x_in, const void* g_out, double* dptm, int64_t da_out, int64_t db_out, int64_t da_in,
+                int64_t db_in, int64_t X, int64_t Y, int64_t Z, int dtype, void* scratch, int64_t scratch_bytes,
+                void* stream) {
+  if (!x_in || !g_out || !dptm) return QSGB_ERR_INVALID;
+  if (da_out < 1 || db_out < 1 || da_in < 1 || db_in < 1 || X < 1 || Y < 1 || Z < 1) return QSGB_ERR_INVALID;
+  if (dtype != QSGB_F64 && dtype != QSGB_F32) return QSGB_ERR_INVALID;
+  const int64_t kin = da_in * db_in, kout = da_out * db_out;
+  // 4 x 4 micro-tiles: at most 2 per thread
+  if (kin > 256 || kout > 256 || ((kin + 3) / 4) * ((kout + 3) / 4) > 2 * kGradBlock)
+    return QSGB_ERR_UNSUPPORTED;
+  const GradParams p = make_params(x_in, g_out, da_out, db_out, da_in, db_in, X, Y, Z);
+  const unsigned nb = grad_blocks(p.n_groups, p.tg);
   const int E = (int)(kin * kout);
   if (!scratch || scratch_bytes < (int64_t)nb * E * (int64_t)sizeof(double)) return QSGB_ERR_SCRATCH;
   cudaStream_t s = as_stream(stream);
   double* part = static_cast<double*>(scratch);
-  if (dtype == QSGB_F64) {
-    const size_t sm = (size_t)(kin + kout) * kTile * sizeof(double);
-    if (sm > 48 * 1024)
-      QSGB_CUDA_TRY(cudaFuncSetAttribute(grad_stage1<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    grad_stage1<double><<<nb, kGradBlock, sm, s>>>(p, part);
-  } else {
-    const size_t sm = (size_t)(kin + kout) * kTile * sizeof(float);
-    if (sm > 48 * 1024)
-      QSGB_CUDA_TRY(cudaFuncSetAttribute(grad_stage1<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    grad_stage1<float><<<nb, kGradBlock, sm, s>>>(p, part);
-  }
-  grad_stage2<<<(E + 255) / 256, 256, 0, s>>>(part, (int)nb, E, dptm);
+  const bool two = p.nmt > kGradBlock;
+  int st;
+  if (dtype == QSGB_F64)
+    st = two ? launch_stage1<double, 2>(p, nb, part, s) : launch_stage1<double, 1>(p, nb, part, s);
+  else
+    st = two ? launch_stage1<float, 2>(p, nb, part, s) : launch_stage1<float, 1>(p, nb, part, s);
+  if (st != QSGB_OK) return st;
+  grad_stage2<<<(E + kStage2Entries - 1) / kStage2Entries, kStage2Entries * kStage2Slices, 0, s>>>(part, (int)nb, E,
+                                                                                                   dptm);
   return launch_status();
 }
 
@@ -153,7 +442,8 @@ int grad_common(const void* x_in, const void* g_out, double* dptm, int64_t da_ou
 
 extern "C" int64_t qsgb_ptm_grad_scratch_bytes(int64_t n_groups, int64_t k_out, int64_t k_in) {
   if (n_groups < 1 || k_out < 1 || k_in < 1) return 0;
-  return (int64_t)qsgb::grad_blocks((uint64_t)n_groups) * k_out * k_in * (int64_t)sizeof(double);
+  const int tg = qsgb::grad_tile((int)std::min<int64_t>(k_out + k_in, 1 << 20));
+  return (int64_t)qsgb::grad_blocks((uint64_t)n_groups, tg) * k_out * k_in * (int64_t)sizeof(double);
 }
 
 extern "C" int qsgb_ptm_grad1(const void* x_in, const void* g_out, double* dptm, int64_t d_out, int64_t d_in,

@@ -265,6 +265,8 @@ constexpr int kSmemB = kDigits * kPlaneA;             // 24576
 constexpr int kSmemBar = kSmemB + kDigits * kPlaneB;  // 27648
 constexpr int kSmemTmem = kSmemBar + 8;
 constexpr int kSmemFlag = kSmemTmem + 4;
+constexpr int kSmemRowExp = kSmemBar + 32;  // int[16] (device PTMs)
+static_assert(kSmemRowExp % 16 == 0 && kSmemRowExp + 64 <= 56 * 1024, "shared-memory layout");
 // the dynamic allocation is padded so that at most 4 blocks share an SM:
 // 4 x 128 tensor-memory columns fill its 512
 constexpr int kUmmaSmem = 56 * 1024;
@@ -309,7 +311,25 @@ __device__ __forceinline__ double combine_words(const uint32_t (&w)[kDigits], in
   return __hiloint2double(hi + (sc << 20), __double2loint(d));
 }
 
-template <bool CONTIG>
+// Offset of op element (r, k) in a 16 x 16 two-qubit PTM stored in `layout`.
+__device__ __forceinline__ int dev_index(int layout, int r, int k) {
+  const int ra = r >> 2, rb = r & 3, ka = k >> 2, kb = k & 3;
+  switch (layout & 3) {
+    case 0:
+      return r * 16 + k;
+    case QSGB_PTM_SWAPPED:  // (rb, ra, kb, ka)
+      return ((rb * 4 + ra) * 4 + kb) * 4 + ka;
+    case QSGB_PTM_TRANSPOSED:  // forward (ka, kb, ra, rb)
+      return k * 16 + r;
+    default:  // forward swapped (kb, ka, rb, ra)
+      return ((kb * 4 + ka) * 4 + rb) * 4 + ra;
+  }
+}
+
+// DEVP: the PTM is in device memory (p.dptm); threads 0..15 split one row
+// each into the B operand planes (the fixed point and digits of the host
+// split) and the row scales, in shared memory.
+template <bool CONTIG, bool DEVP>
 __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_constant__ TcParams p) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int t = threadIdx.x, warp = t >> 5;
@@ -317,27 +337,6 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
   const uint32_t sA = sbase, sB = sbase + kSmemB, bar = sbase + kSmemBar;
   volatile uint32_t* tslot = reinterpret_cast<volatile uint32_t*>(smem + kSmemTmem);
   volatile uint32_t* flag = reinterpret_cast<volatile uint32_t*>(smem + kSmemFlag);
-  {  // PTM digit planes (the B operand)
-    const uint4* src = reinterpret_cast<const uint4*>(&p.bplanes[0][0]);
-    uint4* dst = reinterpret_cast<uint4*>(smem + kSmemB);
-    for (int i = t; i < kDigits * kPlaneB / 16; i += kUBlock) dst[i] = src[i];
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + kSmemTmem),
-                 "r"(kTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tslot;
-  const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);
   const int64_t sai = p.sai, sbi = p.sbi;
 
   auto base = [&](uint64_t grp) -> int64_t {
@@ -384,9 +383,50 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
   int64_t b;
   bool live;
   uint64_t tile = blockIdx.x;
-  load_tile(tile, x, b, live);
+  load_tile(tile, x, b, live);  // in flight during the set-up below
+  int* srow = reinterpret_cast<int*>(smem + kSmemRowExp);
+  int ptm_bad = 0;  // device PTM with inf or nan entries (this thread's pair)
+  if (DEVP) {
+    // 8 threads per row (lanes 8r' .. 8r'+7 of a warp), two entries each
+    const int r = t >> 3, k = 2 * (t & 7);
+    const double v0 = p.dptm[dev_index(p.dlayout, r, k)];
+    const double v1 = p.dptm[dev_index(p.dlayout, r, k + 1)];
+    const unsigned h0 = (unsigned)__double2hiint(v0), h1 = (unsigned)__double2hiint(v1);
+    unsigned emax = max(exp_eff(h0), exp_eff(h1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 4));
+    ptm_bad = (((h0 >> 20) & 0x7ffu) == 0x7ffu || ((h1 >> 20) & 0x7ffu) == 0x7ffu) ? 1 : 0;
+    const unsigned long long u0 = fixed_biased(h0, (unsigned)__double2loint(v0), emax);
+    const unsigned long long u1 = fixed_biased(h1, (unsigned)__double2loint(v1), emax);
+#pragma unroll
+    for (int j = 0; j < kDigits; ++j)
+      *reinterpret_cast<unsigned*>(smem + kSmemB + j * kPlaneB + core_off(r, k)) =
+          digit_pair(u0, u1, 10 * (kDigits - 1 - j));
+    if ((t & 7) == 0) srow[r] = (int)emax - 1022 - 54;
+  } else {  // PTM digit planes (the B operand), split on the host
+    const uint4* src = reinterpret_cast<const uint4*>(&p.bplanes[0][0]);
+    uint4* dst = reinterpret_cast<uint4*>(smem + kSmemB);
+    for (int i = t; i < kDigits * kPlaneB / 16; i += kUBlock) dst[i] = src[i];
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + kSmemTmem),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  ptm_bad = __syncthreads_or(ptm_bad);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);
   for (; tile < p.n_tiles; tile += gridDim.x) {
-    unsigned emax = 1u, bad = 0u;
+    unsigned emax = 1u, bad = ptm_bad ? 1u : 0u;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
       const unsigned h = (unsigned)__double2hiint(x[k]);
@@ -473,7 +513,7 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const uint32_t lv[kDigits] = {w[0][q], w[1][q], w[2][q], w[3][q], w[4][q], w[5][q]};
-        y[q] = combine_words(lv, (int)emax - 1022 + p.row_exp[4 * c + q], bad);
+        y[q] = combine_words(lv, (int)emax - 1022 + (DEVP ? srow[4 * c + q] : p.row_exp[4 * c + q]), bad);
       }
       if (livec) {
         if (p.vec_z1) {
@@ -492,7 +532,10 @@ __global__ void __launch_bounds__(kUBlock) apply16_umma_kernel(const __grid_cons
       for (int r = 0; r < 16; ++r) {
         double a = 0.0;
 #pragma unroll 1
-        for (int k = 0; k < 16; ++k) a = fma(p.ptm[r][k], p.in[bc + (k >> 2) * sai + (k & 3) * sbi], a);
+        for (int k = 0; k < 16; ++k) {
+          const double pk = DEVP ? p.dptm[dev_index(p.dlayout, r, k)] : p.ptm[r][k];
+          a = fma(pk, p.in[bc + (k >> 2) * sai + (k & 3) * sbi], a);
+        }
         p.out[bc + (r >> 2) * p.sao + (r & 3) * p.sbo] = a;
       }
     }
@@ -566,19 +609,9 @@ bool eligible(const double* ptm_host, int kin, int kout) {
   return true;
 }
 
-int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z, unsigned* status,
-           cudaStream_t stream) {
-  TcParams p;
-  std::memset(&p, 0, sizeof p);
-  for (int r = 0; r < 16; ++r) {
-    split_row(op + 16 * r, p.digits, r, p.row_exp);
-    for (int k = 0; k < 16; ++k) p.ptm[r][k] = op[16 * r + k];
-  }
-  // the same digits in the operand layout: element (row r, column k) of plane
-  // i at byte core_off(r, k)
-  for (int i = 0; i < kDigits; ++i)
-    for (int r = 0; r < 16; ++r)
-      for (int k = 0; k < 16; ++k) p.bplanes[i][core_off(r, k) / 2] = p.digits[i][r][k];
+namespace {
+
+void set_geometry(TcParams& p, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z, unsigned* status) {
   p.in = static_cast<const double*>(in);
   p.out = static_cast<double*>(out);
   p.status = status;
@@ -594,6 +627,37 @@ int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, 
   p.sao = p.sai;
   p.syo = p.syi;
   p.sxo = p.sxi;
+}
+
+template <bool DEVP>
+int launch_umma(TcParams& p, const void* in, void* out, uint64_t Z, cudaStream_t stream) {
+  // tcgen05 form: tiles of 128 groups per block, at most 4 blocks per SM
+  p.n_tiles = (p.n_groups + kUBlock - 1) / kUBlock;
+  const bool contig = Z % kUBlock == 0;
+  p.vec_z1 = Z == 1 && (uintptr_t)in % 16 == 0 && (uintptr_t)out % 16 == 0 ? 1 : 0;
+  auto kern = contig ? apply16_umma_kernel<true, DEVP> : apply16_umma_kernel<false, DEVP>;
+  QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem));
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(p.n_tiles, (uint64_t)sm_count() * 4));
+  kern<<<grid, kUBlock, kUmmaSmem, stream>>>(p);
+  return launch_status();
+}
+
+}  // namespace
+
+int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z, unsigned* status,
+           cudaStream_t stream) {
+  TcParams p;
+  std::memset(&p, 0, sizeof p);
+  for (int r = 0; r < 16; ++r) {
+    split_row(op + 16 * r, p.digits, r, p.row_exp);
+    for (int k = 0; k < 16; ++k) p.ptm[r][k] = op[16 * r + k];
+  }
+  // the same digits in the operand layout: element (row r, column k) of plane
+  // i at byte core_off(r, k)
+  for (int i = 0; i < kDigits; ++i)
+    for (int r = 0; r < 16; ++r)
+      for (int k = 0; k < 16; ++k) p.bplanes[i][core_off(r, k) / 2] = p.digits[i][r][k];
+  set_geometry(p, in, out, X, Y, Z, status);
   static const bool mma_sync = [] {
     const char* v = std::getenv("QSGB_TC_KERNEL");
     return v && std::strcmp(v, "mma_sync") == 0;
@@ -610,15 +674,17 @@ int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, 
       apply16_tc_kernel<false><<<grid, kBlock, 0, stream>>>(p);
     return launch_status();
   }
-  // tcgen05 form: tiles of 128 groups per block, at most 4 blocks per SM
-  p.n_tiles = (p.n_groups + kUBlock - 1) / kUBlock;
-  const bool contig = Z % kUBlock == 0;
-  p.vec_z1 = Z == 1 && (uintptr_t)in % 16 == 0 && (uintptr_t)out % 16 == 0 ? 1 : 0;
-  auto kern = contig ? apply16_umma_kernel<true> : apply16_umma_kernel<false>;
-  QSGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kUmmaSmem));
-  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(p.n_tiles, (uint64_t)sm_count() * 4));
-  kern<<<grid, kUBlock, kUmmaSmem, stream>>>(p);
-  return launch_status();
+  return launch_umma<false>(p, in, out, Z, stream);
+}
+
+int launch_device(const double* dptm, int layout, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z,
+                  unsigned* status, cudaStream_t stream) {
+  TcParams p;
+  std::memset(&p, 0, sizeof p);
+  p.dptm = dptm;
+  p.dlayout = layout & 3;
+  set_geometry(p, in, out, X, Y, Z, status);
+  return launch_umma<true>(p, in, out, Z, stream);
 }
 
 }  // namespace tc

@@ -28,6 +28,8 @@ struct TcParams {
   int pair_store;  // groups 2c, 2c+1 are adjacent and 16-byte aligned
   int vec_z1;      // Z == 1 and both tensors 16-byte aligned: a group's
                    // runs along the last target move as 16-byte vectors
+  const double* dptm;  // device PTM (launch_device): split by each block
+  int dlayout;         // its storage (QSGB_PTM_SWAPPED / QSGB_PTM_TRANSPOSED bits)
   int row_exp[16];                                // Ep_r - 1022 - 54 per row
   unsigned short digits[kDigits][16][16];         // FP16 digit planes e_i[r][k]
   alignas(16) unsigned short bplanes[kDigits][256];  // the same in the shared-memory
@@ -46,6 +48,12 @@ bool eligible(const double* op, int kin, int kout);
 // (X, 4, Y, 4, Z).
 int launch(const double* op, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z, unsigned* status,
            cudaStream_t stream);
+// The same for a 16 x 16 PTM in device memory, stored in `layout`
+// (QSGB_PTM_SWAPPED / QSGB_PTM_TRANSPOSED bits): every block reads and
+// splits it (nothing is read on the host); inf or nan entries send every
+// group to the native FP64 path.
+int launch_device(const double* dptm, int layout, const void* in, void* out, uint64_t X, uint64_t Y, uint64_t Z,
+                  unsigned* status, cudaStream_t stream);
 
 }  // namespace tc
 }  // namespace qsgb

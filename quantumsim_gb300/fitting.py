@@ -125,6 +125,46 @@ class NoisyCircuitModel:
             fns.append(layer)
         return fns
 
+    def schedule(self, fuse=True):
+        """The applications of the circuit in order: per layer a list of
+        (kind, index, qudits), kind 1 for the one-qubit PTM singles[index]
+        and kind 2 for the two-qubit PTM pairs[index] of ``build_units``
+        (the order of ``layers``: unpaired rotations, then the pairs)."""
+        sched, singles, pairs = [], [], []
+        for l in range(self.n_layers):
+            ops_l = []
+            edges = [i for i, _ in self.pairs(l)]
+            paired = {q for i in edges for q in (i, i + 1)} if fuse else set()
+            for q in range(self.n):
+                if q not in paired:
+                    ops_l.append((1, len(singles), (q,)))
+                    singles.append((l, q))
+            for i in edges:
+                ops_l.append((2, len(pairs), (i, i + 1)))
+                pairs.append((l, i))
+            sched.append(ops_l)
+        return sched, singles, pairs
+
+    def build_units(self, p, fuse=True):
+        """All PTMs the circuit applies, in batch (a few dozen torch
+        operations whatever the depth): one-qubit PTMs (Ns, 4, 4) and
+        two-qubit PTMs (Np, 4, 4, 4, 4) indexed by ``schedule(fuse)``; with
+        `fuse` each pair PTM is CZ (R_i (x) R_i+1) of its layer."""
+        one_q, cz = self.build_ptms(p)
+        _, singles, pairs = self.schedule(fuse)
+        dev = one_q.device
+        ls = torch.tensor([l for l, _ in singles], device=dev)
+        qs = torch.tensor([q for _, q in singles], device=dev)
+        s = one_q[ls, qs]
+        lp = torch.tensor([l for l, _ in pairs], device=dev)
+        ip = torch.tensor([i for _, i in pairs], device=dev)
+        c = cz[ip]
+        if fuse:
+            k = torch.einsum('nac,nbd->nabcd', one_q[lp, ip], one_q[lp, ip + 1])
+            c = (c.reshape(-1, 16, 16) @ k.reshape(-1, 16, 16)).reshape(
+                -1, 4, 4, 4, 4)
+        return s, c
+
     def initial_state(self, device, dtype):
         x = torch.zeros((4,) * self.n, dtype=dtype, device=device)
         x[(0,) * self.n] = 1
@@ -166,15 +206,18 @@ class GraphedGradient:
     """Gradient steps of ``model.loss`` with the circuit replayed from a CUDA
     graph.
 
-    A step builds the PTMs from the parameters on the GPU (eagerly: a few
-    dozen small torch operations), copies them into the graph's static PTM
-    tensors, replays the graph -- the circuit forward with checkpoints every
-    `checkpoint_every` layers, the diagonal, the KL loss and the whole
-    backward pass down to the PTMs: about a thousand kernel launches that
-    would otherwise each cost a host call -- and finishes the backward
-    through the PTM builder into the parameters.  The PTMs stay on the
-    device, so the apply kernels read them from device memory and nothing
-    synchronises inside the graph.
+    A step builds every PTM of the circuit from the parameters on the GPU
+    in batch (``build_units``: a few dozen small torch operations), copies
+    them into the graph's two static PTM buffers, replays the graph -- the
+    circuit forward with checkpoints every `checkpoint_every` layers, the
+    diagonal, the KL loss and the whole backward pass down to the PTM
+    gradients, gathered into two static gradient buffers: about 1,500 kernel
+    launches that would otherwise each cost a host call -- and finishes the
+    backward through the batched builder into the parameters.  The PTMs stay
+    on the device, so the apply kernels read them from device memory and
+    nothing synchronises inside the graph.  Each application's PTM is a leaf
+    of its own (a view of the static buffer), so the backward pass writes
+    each PTM gradient once, with no scatter into a stacked tensor.
 
     ``step(p)`` returns the loss as a device scalar and leaves the gradients
     in ``p[name].grad`` (accumulated, as in ``loss.backward()``)."""
@@ -199,42 +242,58 @@ class GraphedGradient:
                               for i in range(2)]
             self.idx_off.append(len(self.idx_list))
         self._diag = Diagonal
+        self.sched = model.schedule(fuse)[0]
         with torch.no_grad():
             p0 = {k: v.to(self.dev) for k, v in model.init.items()}
-            one_q, cz = model.build_ptms(p0)
-        self.one_q = one_q.detach().clone().requires_grad_(True)
-        self.cz = cz.detach().clone().requires_grad_(True)
+            s0, c0 = model.build_units(p0, fuse)
+        self.s_buf = s0.detach().clone()
+        self.c_buf = c0.detach().clone()
+        self.s_leaves = [self.s_buf[i].detach().requires_grad_(True)
+                         for i in range(self.s_buf.shape[0])]
+        self.c_leaves = [self.c_buf[i].detach().requires_grad_(True)
+                         for i in range(self.c_buf.shape[0])]
         # warm up on a side stream (compiles nothing: device PTMs use the
         # precompiled kernels), then capture
         side = torch.cuda.Stream(self.dev)
         side.wait_stream(torch.cuda.current_stream(self.dev))
         with torch.cuda.stream(side):
             for _ in range(2):
-                self.one_q.grad = self.cz.grad = None
+                self._clear()
                 self._loss().backward()
-            self.one_q.grad = self.cz.grad = None
+            self._clear()
             self.graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self.graph, stream=side):
                 self.loss = self._loss()
                 self.loss.backward()
+                self.s_grad = torch.stack([t.grad for t in self.s_leaves])
+                self.c_grad = torch.stack([t.grad for t in self.c_leaves])
         torch.cuda.current_stream(self.dev).wait_stream(side)
 
+    def _clear(self):
+        for t in self.s_leaves + self.c_leaves:
+            t.grad = None
+
     def _loss(self):
-        fns = self.model.layers_of(
-            self.one_q, self.cz,
-            lambda s, pt, qs: apply_ptm_diff(s, pt, *qs), fuse=self.fuse)
+        leaves = {1: self.s_leaves, 2: self.c_leaves}
+        fns = []
+        for ops_l in self.sched:
+            def layer(x, ops_l=ops_l):
+                for kind, i, qs in ops_l:
+                    x = apply_ptm_diff(x, leaves[kind][i], *qs)
+                return x
+            fns.append(layer)
         x = checkpointed(fns, self.x0.clone(), self.every)
         prob = self._diag.apply(x, self.flat, self.idx_off, self.idx_list)
         t = self.target
         return torch.sum(t * (torch.log(t) - torch.log(prob)))
 
     def step(self, p):
-        one_q, cz = self.model.build_ptms(p)
+        s, c = self.model.build_units(p, self.fuse)
         with torch.no_grad():
-            self.one_q.copy_(one_q)
-            self.cz.copy_(cz)
+            self.s_buf.copy_(s)
+            self.c_buf.copy_(c)
         self.graph.replay()
-        torch.autograd.backward([one_q, cz], [self.one_q.grad, self.cz.grad])
+        torch.autograd.backward([s, c], [self.s_grad, self.c_grad])
         return self.loss
 
 

@@ -1,0 +1,100 @@
+"""The PTM gradient kernel (csrc/qsgb_grad.cu: float-float products, FP64
+tiles for values outside [2^-100, 2^40]) against the oracle's
+dP = sum_g g_out (x) x_in: per entry within 2^-44 of sum_g |g_out| |x_in|
+(the float-float bound, 2^-47 per product, with margin), for one- and
+two-qudit PTMs of every size the apply kernels take (4 x 4, 16 x 16 at ten
+qubits, qutrit 9 x 9 and 81 x 81, rectangular), every stride class, FP32
+storage, and tiles that hold out-of-band values."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import pauli_vector_np as O
+
+pytestmark = pytest.mark.gpu
+
+BOUND = 2.0 ** -44
+
+
+def _check(x, g, qs, rel=BOUND, floor=0.0):
+    xt = torch.from_numpy(x).cuda()
+    gt = torch.from_numpy(g).cuda()
+    got = torch.ops.qsgb.ptm_grad(xt, gt, list(qs)).cpu().numpy()
+    ref = O.ptm_grad(x, g, *qs)
+    absref = O.ptm_grad(np.abs(x), np.abs(g), *qs)
+    assert got.shape == ref.shape
+    err = np.abs(got - ref)
+    lim = rel * absref + floor
+    assert np.all(err <= lim), (qs, float((err / np.maximum(absref, 1e-300)).max()))
+    return got
+
+
+def _out_shape(shape, qs, dims_out):
+    s = list(shape)
+    for q, d in zip(qs, dims_out):
+        s[q] = d
+    return tuple(s)
+
+
+@pytest.mark.parametrize('qs', [(0,), (4,), (9,), (0, 1), (3, 7), (8, 9),
+                                (9, 8), (6, 2)])
+def test_qubit_ptms_at_ten_qubits(qs):
+    rng = np.random.default_rng(hash(qs) % 1000)
+    shape = (4,) * 10
+    x = rng.standard_normal(shape)
+    g = rng.standard_normal(shape)
+    _check(x, g, qs)
+
+
+def test_qutrit_and_rectangular_ptms():
+    rng = np.random.default_rng(31)
+    shape = (9, 4, 9, 9, 3)
+    x = rng.standard_normal(shape)
+    for qs, dout in [((0,), (9,)), ((2, 3), (9, 9)), ((3, 0), (9, 9)),
+                     ((1,), (2,)), ((4, 1), (9, 4)), ((0, 4), (3, 1))]:
+        g = rng.standard_normal(_out_shape(shape, qs, dout))
+        _check(x, g, qs)
+
+
+def test_fp32_storage():
+    rng = np.random.default_rng(32)
+    shape = (4,) * 8
+    x = rng.standard_normal(shape).astype(np.float32)
+    g = rng.standard_normal(shape).astype(np.float32)
+    for qs in [(2,), (1, 5), (7, 6)]:
+        xt = torch.from_numpy(x).cuda()
+        gt = torch.from_numpy(g).cuda()
+        got = torch.ops.qsgb.ptm_grad(xt, gt, list(qs)).cpu().numpy()
+        # the float inputs are exact in the float-float products
+        ref = O.ptm_grad(x.astype(np.float64), g.astype(np.float64), *qs)
+        absref = O.ptm_grad(np.abs(x).astype(np.float64),
+                            np.abs(g).astype(np.float64), *qs)
+        assert np.all(np.abs(got - ref) <= BOUND * absref)
+
+
+def test_out_of_band_values_take_the_fp64_tiles():
+    """Values above 2^40 or below 2^-100 (and the neighbours in their tiles)
+    are computed in native FP64; the rest of the vector in float-float."""
+    rng = np.random.default_rng(33)
+    shape = (4,) * 9
+    x = rng.standard_normal(shape)
+    g = rng.standard_normal(shape)
+    x[1, 2, 3, 0, 0, 1, 2, 3, 0] = 3e15
+    x[0, 0, 0, 0, 1, 1, 1, 1, 2] = 1e-40
+    g[3, 3, 3, 3, 3, 3, 3, 3, 3] = -1e-290
+    g[2, 0, 1, 0, 1, 0, 1, 0, 1] = 7e200
+    for qs in [(8,), (0, 3), (8, 7)]:
+        _check(x, g, qs)
+    # magnitudes that no float pair holds throughout
+    _check(x * 1e-200, g, (2, 5), floor=0.0)
+    _check(x, g * 1e50, (2, 5))
+
+
+def test_deterministic():
+    rng = np.random.default_rng(34)
+    shape = (4,) * 9
+    x = torch.from_numpy(rng.standard_normal(shape)).cuda()
+    g = torch.from_numpy(rng.standard_normal(shape)).cuda()
+    a = torch.ops.qsgb.ptm_grad(x, g, [3, 6])
+    b = torch.ops.qsgb.ptm_grad(x, g, [3, 6])
+    assert torch.equal(a, b)

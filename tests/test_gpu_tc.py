@@ -131,3 +131,45 @@ def test_inf_and_nan_inputs_follow_fp64():
     fin = np.isfinite(ref)
     np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
     np.testing.assert_allclose(got[fin], ref[fin], rtol=1e-12, atol=1e-14)
+
+
+def test_device_ptms_match_the_host_split_bitwise():
+    """A 16 x 16 PTM in device memory is split by the kernel itself: the
+    digits are the host split's, so every layout (plain, swapped,
+    transposed, both) gives the host path's bits; 'auto' sends device PTMs
+    there too."""
+    rng = np.random.default_rng(107)
+    n = 7
+    pv = torch.from_numpy(_rand_pv(rng, (4,) * n)).cuda()
+    for qs in [(0, 1), (1, 0), (2, 6), (6, 5), (5, 3)]:
+        ptm = rng.standard_normal((4, 4, 4, 4))
+        for tr in (False, True):
+            host = torch.ops.qsgb.apply_ptm(pv, torch.from_numpy(ptm), list(qs),
+                                            L.ARITH_TC, 0, tr)
+            for arith in (L.ARITH_TC, L.ARITH_AUTO):
+                dev = torch.ops.qsgb.apply_ptm(pv, torch.from_numpy(ptm).cuda(),
+                                               list(qs), arith, 0, tr)
+                assert torch.equal(dev, host), (qs, tr, arith)
+            ref = (O.apply_ptm_transposed(pv.cpu().numpy(), ptm, *qs) if tr
+                   else O.apply_ptm(pv.cpu().numpy(), ptm, *qs))
+            absref = (O.apply_ptm_transposed(np.abs(pv.cpu().numpy()),
+                                             np.abs(ptm), *qs) if tr
+                      else O.apply_ptm(np.abs(pv.cpu().numpy()), np.abs(ptm),
+                                       *qs))
+            assert_close_dot(host.cpu().numpy(), ref, absref)
+
+
+def test_device_ptm_with_inf_follows_fp64():
+    rng = np.random.default_rng(108)
+    pv = _rand_pv(rng, (4,) * 4)
+    ptm = rng.standard_normal((4, 4, 4, 4))
+    ptm[1, 2, 0, 3] = np.inf
+    got = torch.ops.qsgb.apply_ptm(torch.from_numpy(pv).cuda(),
+                                   torch.from_numpy(ptm).cuda(), [1, 3],
+                                   L.ARITH_AUTO, 0, False).cpu().numpy()
+    with np.errstate(invalid='ignore'):
+        ref = O.apply_ptm(pv, ptm, 1, 3)
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(ref))
+    np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
+    fin = np.isfinite(ref)
+    np.testing.assert_allclose(got[fin], ref[fin], rtol=1e-12, atol=1e-14)
