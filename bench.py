@@ -803,6 +803,32 @@ def run_profile_tc(args):
     print(json.dumps({'profile_case': 'tc', 'trace': s.trace()}))
 
 
+def run_profile_grad(args):
+    """ncu workload for the graphed gradient step of the 249-parameter
+    10-qubit model (--profile-dtype f64 or f32): the graph is captured and
+    replayed once outside the profiled range, then replayed once between
+    cudaProfilerStart and cudaProfilerStop (run ncu with
+    --profile-from-start off): about 1,100 launches, nearly all of them the
+    apply, tensor-core and PTM-gradient kernels."""
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    from quantumsim_gb300 import fitting
+    dtype = torch.float32 if args.profile_dtype == 'f32' else torch.float64
+    m = fitting.NoisyCircuitModel()
+    target = m.probabilities(m.perturbed()).detach()
+    step = fitting.GraphedGradient(m, target, dtype=dtype, checkpoint_every=8,
+                                   fuse=True)
+    step.graph.replay()
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    step.graph.replay()
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    print(json.dumps({'profile_case': 'grad', 'dtype': args.profile_dtype,
+                      'loss': float(step.loss)}))
+
+
 def run_profile_take(args):
     """Small workload for ncu captures of the take-along-an-axis kernels
     (reduce_basis / project): 8 qutrits (9^8 float64 entries, 344 MB); 3x
@@ -959,9 +985,11 @@ def main():
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', nargs='?', const='apply',
                     choices=['apply', 'qutrits', 'tc', 'take', 'batched',
-                             'circuit', 'adjoint2'],
+                             'circuit', 'adjoint2', 'grad'],
                     help='run a small ncu profiling workload and exit')
     ap.add_argument('--profile-qubits', type=int, default=12)
+    ap.add_argument('--profile-dtype', choices=['f64', 'f32'], default='f64',
+                    help='storage of the grad profiling workload')
     ap.add_argument('--profile-pair', default='5,6',
                     help='qubit pair of the adjoint2 profiling workload')
     args = ap.parse_args()
@@ -969,7 +997,8 @@ def main():
         {'apply': run_profile_case, 'qutrits': run_profile_qutrits,
          'tc': run_profile_tc, 'take': run_profile_take,
          'batched': run_profile_batched, 'adjoint2': run_profile_adjoint2,
-         'circuit': run_profile_circuit}[args.profile_case](args)
+         'circuit': run_profile_circuit,
+         'grad': run_profile_grad}[args.profile_case](args)
         return
     if args.warmup < 3 and args.impl == 'gb300':
         print('warning: fewer than 3 warm-up steps', file=sys.stderr)
