@@ -623,6 +623,23 @@ def run_ops_config():
     t = per_call(s.renormalize, 10)
     out['renormalize_ms'] = t * 1e3
     out['renormalize_gbs'] = nbytes / t / 1e9
+    # host time per call on a 6-qubit state (32 KB, kernels of a few us):
+    # apply_ptm calls queued back to back with one synchronisation at the
+    # end; trace and meas_prob return host values, so each call waits for
+    # its own result
+    from quantumsim_gb300 import workloads
+    rng = np.random.default_rng(0)
+    t1, t2 = workloads.coherence_times(rng, 6)
+    cz = workloads.noisy_cz(rng, (1, 2), t1, t2)
+    rot = workloads.noisy_1q(rng, t1[3], t2[3])
+    s6 = qg.PauliVectorGB300([bases.general(2)] * 6)
+    out['apply_ptm_2q_6q_host_us'] = per_call(
+        lambda: s6.apply_ptm(cz, 1, 2), 2000) * 1e6
+    out['apply_ptm_1q_6q_host_us'] = per_call(
+        lambda: s6.apply_ptm(rot, 3), 2000) * 1e6
+    out['trace_6q_us'] = per_call(s6.trace, 200) * 1e6
+    out['meas_prob_6q_us'] = per_call(lambda: s6.meas_prob(3), 200) * 1e6
+    del s6
     del s
     g3 = bases.general(3)
     comp = [g3.computational_basis_indices[i] for i in range(3)]

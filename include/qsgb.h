@@ -251,7 +251,8 @@ int qsgb_marginals_noalloc(const double* diag, int ndim, const int64_t* shape,
  * copy) and waits for it on the stream before returning; with NULL it
  * returns at once, the results on the device.  Diagonals of at most 2^22 entries
  * and axes of at most 64 indices; larger ones return QSGB_ERR_UNSUPPORTED
- * (use qsgb_gather and qsgb_marginals).
+ * (use qsgb_gather and qsgb_marginals).  Without scratch (below) one block
+ * does the whole reduction.
  * Replaces: cuda.py:347-384 (trace and meas_prob: multitake, then a host
  * sum or one ReductionKernel launch and device sync per outcome) and
  * numpy.py:82-84, 97-107.
@@ -260,7 +261,15 @@ int qsgb_diag_marginals(const void* in, int in_dtype, int ndim,
                         const int64_t* in_shape, const int32_t* idx_off,
                         const int32_t* idx, int axis, double* out,
                         const unsigned* dev_status, double* host_out,
-                        void* stream);
+                        void* scratch, int64_t scratch_bytes, void* stream);
+/* Scratch for qsgb_diag_marginals to spread a large diagonal over up to one
+ * block per SM: a 16-byte-aligned device buffer whose first 16 bytes are
+ * zero before its first use (each call leaves them zero again), of this many
+ * bytes (fewer bytes, or scratch == NULL, use fewer blocks, down to one).
+ * The last block to finish adds the per-block partials in block order, so
+ * results stay deterministic for a given device.  Calls that share a
+ * scratch buffer must not overlap on the GPU. */
+int64_t qsgb_diag_marginals_scratch_bytes(void);
 
 /*
  * Partial trace: out[kept...] = sum over traced qudits t of

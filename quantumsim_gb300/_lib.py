@@ -60,7 +60,8 @@ SIGNATURES = {
                            _p_i32, _p_i32, _c_void_p]),
     'qsgb_diag_marginals': (_int, [_c_void_p, _int, _int, _p_i64, _p_i32,
                                    _p_i32, _int, _c_void_p, _c_void_p,
-                                   _c_void_p, _c_void_p]),
+                                   _c_void_p, _c_void_p, _i64, _c_void_p]),
+    'qsgb_diag_marginals_scratch_bytes': (_i64, []),
     'qsgb_take_axis': (_int, [_c_void_p, _c_void_p, _int, _i64, _i64, _i64,
                               _p_i32, _i64, _c_void_p]),
     'qsgb_marginals_scratch_bytes': (_i64, [_i64, _i64]),

@@ -10,6 +10,8 @@ import glob
 import os
 import shutil
 import subprocess
+import sysconfig
+import warnings
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG_DIR, 'csrc')
@@ -65,8 +67,45 @@ def _embed():
                 name, text))
 
 
+PYAPPLY_SRC = os.path.join(CSRC, 'qsgb_pyapply.c')
+
+
+def pyapply_path():
+    suffix = sysconfig.get_config_var('EXT_SUFFIX') or '.so'
+    return os.path.join(PKG_DIR, '_qsgb_pyapply' + suffix)
+
+
+def build_pyapply(force=False, verbose=False):
+    """Compile the CPython entry point of the per-call apply path
+    (``csrc/qsgb_pyapply.c``, host C, no CUDA or torch headers); returns its
+    path, or None when no C compiler or Python headers are available, in
+    which case the ctypes path is used."""
+    out = pyapply_path()
+    if (not force and os.path.exists(out) and
+            os.path.getmtime(out) >= os.path.getmtime(PYAPPLY_SRC)):
+        return out
+    cc = shutil.which('gcc') or shutil.which('cc')
+    inc = sysconfig.get_paths().get('include')
+    if not cc or not inc or not os.path.exists(os.path.join(inc, 'Python.h')):
+        return None
+    tmp = out + '.tmp'
+    cmd = [cc, '-O2', '-shared', '-fPIC', '-std=c11', '-Wall', '-I', inc,
+           PYAPPLY_SRC, '-o', tmp]
+    if verbose:
+        print(' '.join(cmd))
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        warnings.warn('the CPython apply entry point did not build (the '
+                      'ctypes path is used):\n' + res.stderr)
+        return None
+    os.replace(tmp, out)
+    return out
+
+
 def build(force=False, verbose=False, jobs=None):
-    """Compile and link ``libqsgb.so``; returns its path."""
+    """Compile and link ``libqsgb.so`` (and the CPython apply entry
+    point); returns the library's path."""
+    build_pyapply(force=force, verbose=verbose)
     if not force and not is_stale():
         return LIB_PATH
     nvcc = _nvcc()

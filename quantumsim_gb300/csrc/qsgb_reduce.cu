@@ -204,6 +204,8 @@ struct DiagRedParams {
   const void* in;
   double* out;
   const unsigned* status;
+  double* part;      // per-block partial sums [grid][n_out] (grid > 1)
+  unsigned* ticket;  // blocks finished (grid > 1); zero between calls
   int in_dtype;
   int ndim;
   int axis;        // -1: trace
@@ -221,18 +223,25 @@ constexpr int kDiagRedBlock = 1024;
 
 __global__ void __launch_bounds__(kDiagRedBlock) diag_marginals_kernel(const __grid_constant__ DiagRedParams p) {
   __shared__ double sh[32];
+  __shared__ int last;
   const uint64_t d_axis = p.axis < 0 ? 1 : p.div[p.axis].d;
   constexpr int U = 8;  // independent loads in flight per thread
+  // this block's share of each outcome's entries: the scattered diagonal
+  // loads of one SM are bounded by its outstanding misses, so a large
+  // diagonal is spread over many blocks
+  const uint64_t chunk = (p.per_j + gridDim.x - 1) / gridDim.x;
+  const uint64_t m_beg = (uint64_t)blockIdx.x * chunk;
+  const uint64_t m_end = m_beg + chunk < p.per_j ? m_beg + chunk : p.per_j;
   for (int j = 0; j < p.n_out; ++j) {
     double acc = 0.0;
-    for (uint64_t m0 = threadIdx.x; m0 < p.per_j; m0 += (uint64_t)U * kDiagRedBlock) {
+    for (uint64_t m0 = m_beg + threadIdx.x; m0 < m_end; m0 += (uint64_t)U * kDiagRedBlock) {
       double v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         // m-th diagonal entry whose index along `axis` is j
         const uint64_t m = m0 + (uint64_t)u * kDiagRedBlock;
         v[u] = 0.0;
-        if (m < p.per_j) {
+        if (m < m_end) {
           const uint64_t hi = fdiv(m, p.div_s);
           const uint64_t lo = m - hi * p.s_axis;
           uint64_t rem = (hi * d_axis + (uint64_t)j) * p.s_axis + lo;
@@ -253,9 +262,34 @@ __global__ void __launch_bounds__(kDiagRedBlock) diag_marginals_kernel(const __g
       for (int u = 0; u < U; ++u) acc += v[u];  // fixed order
     }
     const double r = block_sum(acc, sh);
-    if (threadIdx.x == 0) p.out[j] = r;
+    if (threadIdx.x == 0) {
+      if (gridDim.x == 1)
+        p.out[j] = r;
+      else
+        p.part[(int64_t)blockIdx.x * p.n_out + j] = r;
+    }
   }
-  if (threadIdx.x == 0) p.out[p.n_out] = p.status ? (double)*p.status : 0.0;
+  if (gridDim.x == 1) {
+    if (threadIdx.x == 0) p.out[p.n_out] = p.status ? (double)*p.status : 0.0;
+    return;
+  }
+  // the last block to finish adds the partials in block order
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(p.ticket, 1u) == gridDim.x - 1 ? 1 : 0;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int j = threadIdx.x; j < p.n_out; j += kDiagRedBlock) {
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(p.part + (int64_t)b * p.n_out + j);
+    p.out[j] = s;
+  }
+  if (threadIdx.x == 0) {
+    p.out[p.n_out] = p.status ? (double)*p.status : 0.0;
+    *p.ticket = 0u;  // ready for the next call
+  }
 }
 
 // ---------------------------------------------------------------- partial trace
@@ -443,9 +477,21 @@ extern "C" int qsgb_take_axis(const void* in, void* out, int dtype, int64_t oute
   return take_launch<kMaxIdx>(in, out, dtype, outer, d_in, inner, idx, d_out, s);
 }
 
+namespace qsgb {
+namespace {
+constexpr int kDiagEntriesPerBlock = 512;  // diagonal entries per block (per outcome)
+constexpr int kDiagMaxOut = 64;
+}  // namespace
+}  // namespace qsgb
+
+extern "C" int64_t qsgb_diag_marginals_scratch_bytes(void) {
+  return 16 + (int64_t)qsgb::sm_count() * qsgb::kDiagMaxOut * (int64_t)sizeof(double);
+}
+
 extern "C" int qsgb_diag_marginals(const void* in, int in_dtype, int ndim, const int64_t* in_shape,
                                    const int32_t* idx_off, const int32_t* idx, int axis, double* out,
-                                   const unsigned* dev_status, double* host_out, void* stream) {
+                                   const unsigned* dev_status, double* host_out, void* scratch,
+                                   int64_t scratch_bytes, void* stream) {
   if (!in || !out || !idx_off || (ndim > 0 && (!in_shape || !idx))) return QSGB_ERR_INVALID;
   if (in_dtype != QSGB_F64 && in_dtype != QSGB_F32) return QSGB_ERR_INVALID;
   if (ndim < 0 || ndim > kMaxDim || axis < -1 || axis >= ndim) return QSGB_ERR_INVALID;
@@ -480,8 +526,19 @@ extern "C" int qsgb_diag_marginals(const void* in, int in_dtype, int ndim, const
   p.div_s = make_fastdiv(p.s_axis);
   for (int a = 0; a <= ndim; ++a) p.idx_off[a] = idx_off[a];
   for (int i = 0; i < idx_off[ndim]; ++i) p.idx[i] = idx[i];
+  // blocks: one per kDiagEntriesPerBlock entries of an outcome, at most one
+  // per SM, and as many as the scratch holds partials for
+  uint64_t grid = (p.per_j + kDiagEntriesPerBlock - 1) / kDiagEntriesPerBlock;
+  grid = std::min<uint64_t>(grid, (uint64_t)sm_count());
+  if (!scratch || scratch_bytes < 16 + (int64_t)sizeof(double) * p.n_out) grid = 1;
+  if (grid > 1) {
+    if ((uintptr_t)scratch % 16 != 0) return QSGB_ERR_INVALID;
+    grid = std::min<uint64_t>(grid, (uint64_t)((scratch_bytes - 16) / ((int64_t)sizeof(double) * p.n_out)));
+    p.ticket = static_cast<unsigned*>(scratch);
+    p.part = reinterpret_cast<double*>(static_cast<unsigned char*>(scratch) + 16);
+  }
   cudaStream_t st = as_stream(stream);
-  diag_marginals_kernel<<<1, kDiagRedBlock, 0, st>>>(p);
+  diag_marginals_kernel<<<(unsigned)std::max<uint64_t>(grid, 1), kDiagRedBlock, 0, st>>>(p);
   const int ls = launch_status();
   if (ls != QSGB_OK || !host_out) return ls;
   QSGB_CUDA_TRY(cudaMemcpyAsync(host_out, out, (d + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -461,9 +461,43 @@ def eager_plan(shape, dtype, qudits, ptm_shape):
             code)
 
 
+_PYAPPLY = None  # the CPython entry point once set up; False when absent
+
+
+def _pyapply():
+    """The compiled per-call entry point (csrc/qsgb_pyapply.c), handed the
+    library's apply addresses and the stream / status lookups once; False
+    when it was not built (no C compiler or Python headers)."""
+    global _PYAPPLY
+    if _PYAPPLY is None:
+        try:
+            from . import _qsgb_pyapply as m
+        except ImportError:
+            _PYAPPLY = False
+            return _PYAPPLY
+        lib = L.load()
+        raw = _RAW_STREAM if _RAW_STREAM is not None else (
+            lambda i: torch.cuda.current_stream(i).cuda_stream)
+        m.set_entry_points(
+            ctypes.cast(lib.qsgb_apply_ptm1, ctypes.c_void_p).value,
+            ctypes.cast(lib.qsgb_apply_ptm2, ctypes.c_void_p).value,
+            raw, status_ptr)
+        _PYAPPLY = m
+    return _PYAPPLY
+
+
 def eager_apply(pv, ptm, plan, arith):
     """Apply the contiguous float64 numpy PTM `ptm` to the contiguous CUDA
-    tensor `pv` with a plan from eager_plan; returns the new tensor."""
+    tensor `pv` with a plan from eager_plan; returns the new tensor, or None
+    when the request needs the general operator path."""
+    fast = _PYAPPLY if _PYAPPLY is not None else _pyapply()
+    if fast:
+        st = fast.apply(pv, ptm, plan, arith)
+        if type(st) is not int:
+            return st
+        if st == L.ERR_UNSUPPORTED:
+            return None
+        L.check(st, 'qsgb_apply_ptm')
     new_shape, two, sizes, flags, code = plan
     out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
     if out.numel() == 0:
@@ -499,10 +533,14 @@ def diag_marginals(pv, plan_arrays, axis):
     index = pv.device.index
     bufs = _DIAG_BUF.get(index)
     if bufs is None:
+        nscr = int(L.load().qsgb_diag_marginals_scratch_bytes())
+        # the scratch's first 16 bytes (the kernel's block ticket) start at
+        # zero and every call leaves them zero
         bufs = (torch.empty(80, dtype=torch.float64, device=pv.device),
-                torch.empty(80, dtype=torch.float64, pin_memory=True))
+                torch.empty(80, dtype=torch.float64, pin_memory=True),
+                torch.zeros(nscr, dtype=torch.uint8, device=pv.device))
         _DIAG_BUF[index] = bufs
-    dev, host = bufs
+    dev, host, scratch = bufs
     n = (1 if axis < 0 else n_out[axis]) + 1
     if n > 65:
         return None
@@ -511,7 +549,8 @@ def diag_marginals(pv, plan_arrays, axis):
     # the library copies the n values into the pinned buffer and waits
     st = L.load().qsgb_diag_marginals(
         pv.data_ptr(), _dtype_code(pv), pv.dim(), shape_c, idx_off_c, idx_c,
-        axis, dev.data_ptr(), status_ptr(index), host.data_ptr(), stream)
+        axis, dev.data_ptr(), status_ptr(index), host.data_ptr(),
+        scratch.data_ptr(), scratch.numel(), stream)
     if st == L.ERR_UNSUPPORTED:
         return None
     L.check(st, 'qsgb_diag_marginals')

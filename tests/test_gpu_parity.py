@@ -610,3 +610,53 @@ def test_exp_value_large_state_storage_types_and_errors():
         s.exp_value('XXXXXXXXXA')
     with pytest.raises(NotImplementedError):
         s.exp_value(np.eye(2 ** n))
+
+
+def test_compiled_entry_point_matches_ctypes_path():
+    """apply_ptm through the CPython entry point (csrc/qsgb_pyapply.c) and
+    through ctypes runs the same kernels: the same bits for one- and
+    two-qudit, swapped, rectangular and qutrit PTMs in FP64 and FP32; and
+    the entry point is the path in use wherever it was built."""
+    from quantumsim_gb300 import ops
+    if not ops._pyapply():
+        pytest.skip('the CPython entry point is not built on this host')
+    rng = np.random.default_rng(77)
+    b2, b3 = B.general(2), B.general(3)
+    cases = [([b2] * 6, rand_ptm(rng, (4, 4, 4, 4), 0.5), (1, 4)),
+             ([b2] * 6, rand_ptm(rng, (4, 4, 4, 4), 0.5), (5, 2)),
+             ([b2] * 6, rand_ptm(rng, (4, 4)), (5,)),
+             ([b2] * 6, np.eye(4)[[0, 3]], (2,)),
+             ([b3, b2, b3], rand_ptm(rng, (9, 9, 9, 9), 0.1), (2, 0))]
+    for dtype in (np.float64, np.float32):
+        for bases, ptm, qs in cases:
+            pv = rand_pv(rng, tuple(b.dim_pauli for b in bases))
+            outs = []
+            for fast in (True, False):
+                saved = ops._PYAPPLY
+                ops._PYAPPLY = saved if fast else False
+                try:
+                    s = GB(bases, pv, dtype=dtype)
+                    s.apply_ptm(ptm, *qs)
+                    outs.append(s.to_pv())
+                finally:
+                    ops._PYAPPLY = saved
+            np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize('n', [6, 12, 13])
+def test_fused_marginals_over_many_blocks(n):
+    """trace and meas_prob through the fused kernel, which spreads diagonals
+    of more than 512 entries per outcome over several blocks (the last block
+    adds the partials in block order): against sums of the state's own
+    diagonal on the host, on repeated calls (the block ticket is left at
+    zero)."""
+    rng = np.random.default_rng(n)
+    s = GB([B.general(2)] * n, force=True)
+    s._data.copy_(torch.rand_like(s._data))
+    diag = s.diagonal().reshape((2,) * n)
+    for _ in range(3):
+        assert abs(s.trace() - diag.sum()) <= 1e-12 * diag.sum()
+        for q in (0, n // 2, n - 1):
+            ref = diag.sum(axis=tuple(a for a in range(n) if a != q))
+            np.testing.assert_allclose(s.meas_prob(q), ref, rtol=1e-12,
+                                       atol=0)
