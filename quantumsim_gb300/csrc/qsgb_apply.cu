@@ -837,11 +837,13 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   // per group in float-float or FP64)
   if (dtype == QSGB_F64 && da_in == 4 && db_in == 4 && da_out == 4 && db_out == 4) {
     if (flags & QSGB_PTM_HOST) {
-      double op[256];
-      op_matrix(ptm, 4, 4, 4, 4, flags & 3, op);
-      if (tc::eligible(op, 16, 16) &&
-          (tc_arith == QSGB_ARITH_TC || (tc_arith == QSGB_ARITH_AUTO && tc_wanted(op)))) {
+      // density and finiteness do not depend on the storage layout: the op
+      // matrix is formed only for a launch on the tensor cores
+      if ((tc_arith == QSGB_ARITH_TC || (tc_arith == QSGB_ARITH_AUTO && tc_wanted(ptm))) &&
+          tc::eligible(ptm, 16, 16)) {
         if (mode != kLaunch) return QSGB_ERR_UNSUPPORTED;  // precompiled: nothing to prepare
+        double op[256];
+        op_matrix(ptm, 4, 4, 4, 4, flags & 3, op);
         return tc::launch(op, in, out, (uint64_t)X, (uint64_t)Y, (uint64_t)Z, status, s);
       }
     } else if (tc_arith == QSGB_ARITH_TC || (tc_arith == QSGB_ARITH_AUTO && tc_device_auto())) {

@@ -7,16 +7,17 @@
  * quantumsim/pauli_vectors/cuda.py:151-277).
  *
  * The module links nothing: the library's qsgb_apply_ptm1/2 addresses, the
- * current-stream and status-word lookups are handed over once
- * (set_entry_points).  The output tensor is allocated with the input's own
- * `new_empty` (same dtype and device).  The library call runs with the GIL
- * released, as a ctypes call does (a first call of a PTM pattern compiles
- * its kernel).
+ * current-stream and status-word lookups, torch.empty and the device
+ * constructor are handed over once (set_entry_points).  The output tensor is
+ * torch.empty(shape, dtype=pv.dtype, device=<the device of pv>), the device
+ * object made once per device index.  The library call runs with the GIL released, as a ctypes call
+ * does (a first call of a PTM pattern compiles its kernel).
  *
- * apply(pv, ptm, plan, arith) -> new tensor, or the library's status code
- * (an int) when the call did not succeed; `plan` is
- * (output shape, two qudits?, sizes, layout flags, dtype code) as built by
- * quantumsim_gb300.ops.eager_plan, `ptm` a C-contiguous float64 buffer.
+ * apply(pv, ptm, plan, arith) -> new tensor, or an int: the library's status
+ * code when the call did not succeed, or NOT_F64_CONTIGUOUS when `ptm` is not
+ * a C-contiguous float64 buffer (the caller converts it and calls again).
+ * `plan` is (output shape, two qudits?, sizes, layout flags, dtype code) as
+ * built by quantumsim_gb300.ops.eager_plan.
  */
 #define PY_SSIZE_T_CLEAN
 #include <Python.h>
@@ -28,25 +29,39 @@ typedef int (*apply2_fn)(const void*, void*, const double*, int64_t, int64_t, in
                          int64_t, int, int, int, int64_t, unsigned*, void*);
 
 #define MAX_DEVICES 64
+#define NOT_F64_CONTIGUOUS (-1000)
 
 static apply1_fn g_apply1 = NULL;
 static apply2_fn g_apply2 = NULL;
 static PyObject* g_raw_stream = NULL; /* callable(device index) -> stream handle (int) */
 static PyObject* g_status_ptr = NULL; /* callable(device index) -> status word address */
 static unsigned long long g_status[MAX_DEVICES];
-static PyObject* s_new_empty = NULL;
+static PyObject* g_empty = NULL;       /* torch.empty */
+static PyObject* g_device_of = NULL;   /* callable(device index) -> torch.device */
+static PyObject* g_dev_obj[MAX_DEVICES];
+static PyObject* g_empty_kw = NULL;    /* ("dtype", "device") */
 static PyObject* s_data_ptr = NULL;
 static PyObject* s_get_device = NULL;
+static PyObject* s_dtype = NULL;
+static PyObject* s_device = NULL;
 
 static PyObject* set_entry_points(PyObject* self, PyObject* args) {
   unsigned long long a1, a2;
-  PyObject *rs, *sp;
+  PyObject *rs, *sp, *em, *dv;
   (void)self;
-  if (!PyArg_ParseTuple(args, "KKOO", &a1, &a2, &rs, &sp)) return NULL;
-  if (!a1 || !a2 || !PyCallable_Check(rs) || !PyCallable_Check(sp)) {
+  if (!PyArg_ParseTuple(args, "KKOOOO", &a1, &a2, &rs, &sp, &em, &dv)) return NULL;
+  if (!a1 || !a2 || !PyCallable_Check(rs) || !PyCallable_Check(sp) || !PyCallable_Check(em) ||
+      !PyCallable_Check(dv)) {
     PyErr_SetString(PyExc_ValueError, "set_entry_points: null address or non-callable lookup");
     return NULL;
   }
+  Py_INCREF(em);
+  Py_XDECREF(g_empty);
+  g_empty = em;
+  Py_INCREF(dv);
+  Py_XDECREF(g_device_of);
+  g_device_of = dv;
+  for (int i = 0; i < MAX_DEVICES; ++i) Py_CLEAR(g_dev_obj[i]);
   g_apply1 = (apply1_fn)(uintptr_t)a1;
   g_apply2 = (apply2_fn)(uintptr_t)a2;
   Py_XINCREF(rs);
@@ -72,7 +87,7 @@ static PyObject* apply(PyObject* self, PyObject* const* args, Py_ssize_t nargs) 
     PyErr_SetString(PyExc_TypeError, "apply(pv, ptm, plan, arith)");
     return NULL;
   }
-  if (!g_apply1 || !g_apply2) {
+  if (!g_apply1 || !g_apply2 || !g_empty) {
     PyErr_SetString(PyExc_RuntimeError, "apply: set_entry_points was not called");
     return NULL;
   }
@@ -113,6 +128,13 @@ static PyObject* apply(PyObject* self, PyObject* const* args, Py_ssize_t nargs) 
     PyErr_SetString(PyExc_ValueError, "apply: the state is not on a CUDA device");
     return NULL;
   }
+  if (!g_dev_obj[dev]) {
+    g_dev_obj[dev] = PyObject_CallOneArg(g_device_of, dev_obj);
+    if (!g_dev_obj[dev]) {
+      Py_DECREF(dev_obj);
+      return NULL;
+    }
+  }
   unsigned long long stream = 0, status = g_status[dev];
   if (as_u64(PyObject_CallOneArg(g_raw_stream, dev_obj), &stream) < 0) {
     Py_DECREF(dev_obj);
@@ -130,7 +152,12 @@ static PyObject* apply(PyObject* self, PyObject* const* args, Py_ssize_t nargs) 
   /* input and output storage */
   unsigned long long in_ptr = 0, out_ptr = 0;
   if (as_u64(PyObject_CallMethodNoArgs(pv, s_data_ptr), &in_ptr) < 0) return NULL;
-  PyObject* out = PyObject_CallMethodOneArg(pv, s_new_empty, shape);
+  PyObject* kw[3];
+  kw[0] = shape;
+  kw[1] = PyObject_GetAttr(pv, s_dtype);
+  kw[2] = g_dev_obj[dev];
+  PyObject* out = kw[1] ? PyObject_Vectorcall(g_empty, kw, 1, g_empty_kw) : NULL;
+  Py_XDECREF(kw[1]);
   if (!out) return NULL;
   for (Py_ssize_t i = 0; i < PyTuple_GET_SIZE(shape); ++i)
     if (PyLong_AsLongLong(PyTuple_GET_ITEM(shape, i)) == 0) return out; /* empty result */
@@ -140,15 +167,18 @@ static PyObject* apply(PyObject* self, PyObject* const* args, Py_ssize_t nargs) 
   }
 
   Py_buffer view;
-  if (PyObject_GetBuffer(ptm, &view, PyBUF_C_CONTIGUOUS) < 0) {
+  if (PyObject_GetBuffer(ptm, &view, PyBUF_C_CONTIGUOUS | PyBUF_FORMAT) < 0) {
+    PyErr_Clear();
     Py_DECREF(out);
-    return NULL;
+    return PyLong_FromLong(NOT_F64_CONTIGUOUS);
   }
-  if (view.len < (Py_ssize_t)sizeof(double)) {
+  const char* f = view.format ? view.format : "B";
+  if (*f == '<' || *f == '@' || *f == '=') ++f;
+  if (view.itemsize != (Py_ssize_t)sizeof(double) || f[0] != 'd' || f[1] != 0 ||
+      view.len < (Py_ssize_t)sizeof(double)) {
     PyBuffer_Release(&view);
     Py_DECREF(out);
-    PyErr_SetString(PyExc_ValueError, "apply: empty PTM");
-    return NULL;
+    return PyLong_FromLong(NOT_F64_CONTIGUOUS);
   }
   int st;
   const void* in = (const void*)(uintptr_t)in_ptr;
@@ -172,7 +202,7 @@ static PyObject* apply(PyObject* self, PyObject* const* args, Py_ssize_t nargs) 
 
 static PyMethodDef methods[] = {
     {"set_entry_points", set_entry_points, METH_VARARGS,
-     "set_entry_points(apply1_addr, apply2_addr, raw_stream, status_ptr)"},
+     "set_entry_points(apply1_addr, apply2_addr, raw_stream, status_ptr, empty, device_of)"},
     {"apply", (PyCFunction)(void (*)(void))apply, METH_FASTCALL,
      "apply(pv, ptm, plan, arith) -> tensor, or the status code"},
     {NULL, NULL, 0, NULL}};
@@ -181,9 +211,18 @@ static struct PyModuleDef module = {PyModuleDef_HEAD_INIT, "_qsgb_pyapply", NULL
                                     NULL,                  NULL,            NULL, NULL};
 
 PyMODINIT_FUNC PyInit__qsgb_pyapply(void) {
-  s_new_empty = PyUnicode_InternFromString("new_empty");
   s_data_ptr = PyUnicode_InternFromString("data_ptr");
   s_get_device = PyUnicode_InternFromString("get_device");
-  if (!s_new_empty || !s_data_ptr || !s_get_device) return NULL;
-  return PyModule_Create(&module);
+  s_dtype = PyUnicode_InternFromString("dtype");
+  s_device = PyUnicode_InternFromString("device");
+  if (!s_data_ptr || !s_get_device || !s_dtype || !s_device) return NULL;
+  for (int i = 0; i < MAX_DEVICES; ++i) g_dev_obj[i] = NULL;
+  g_empty_kw = PyTuple_Pack(2, s_dtype, s_device);
+  if (!g_empty_kw) return NULL;
+  PyObject* m = PyModule_Create(&module);
+  if (m && PyModule_AddIntConstant(m, "NOT_F64_CONTIGUOUS", NOT_F64_CONTIGUOUS) < 0) {
+    Py_DECREF(m);
+    return NULL;
+  }
+  return m;
 }

@@ -481,23 +481,31 @@ def _pyapply():
         m.set_entry_points(
             ctypes.cast(lib.qsgb_apply_ptm1, ctypes.c_void_p).value,
             ctypes.cast(lib.qsgb_apply_ptm2, ctypes.c_void_p).value,
-            raw, status_ptr)
+            raw, status_ptr, torch.empty,
+            lambda i: torch.device('cuda', i))
         _PYAPPLY = m
     return _PYAPPLY
 
 
 def eager_apply(pv, ptm, plan, arith):
-    """Apply the contiguous float64 numpy PTM `ptm` to the contiguous CUDA
-    tensor `pv` with a plan from eager_plan; returns the new tensor, or None
-    when the request needs the general operator path."""
+    """Apply the numpy PTM `ptm` (converted to C-contiguous float64 when it
+    is not) to the contiguous CUDA tensor `pv` with a plan from eager_plan;
+    returns the new tensor, or None when the request needs the general
+    operator path."""
     fast = _PYAPPLY if _PYAPPLY is not None else _pyapply()
     if fast:
         st = fast.apply(pv, ptm, plan, arith)
         if type(st) is not int:
             return st
+        if st == fast.NOT_F64_CONTIGUOUS:
+            st = fast.apply(pv, np.ascontiguousarray(ptm, dtype=np.float64),
+                            plan, arith)
+            if type(st) is not int:
+                return st
         if st == L.ERR_UNSUPPORTED:
             return None
         L.check(st, 'qsgb_apply_ptm')
+    ptm = np.ascontiguousarray(ptm, dtype=np.float64)
     new_shape, two, sizes, flags, code = plan
     out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
     if out.numel() == 0:

@@ -275,8 +275,7 @@ class PauliVectorGB300(_Base):
         (quantumsim/operations/operation.py:549-551)."""
         if type(ptm) is np.ndarray:
             # host PTM: a validated plan per geometry, then one C call
-            if ptm.dtype != np.float64 or not ptm.flags.c_contiguous:
-                ptm = np.ascontiguousarray(ptm, dtype=np.float64)
+            # (which takes any float64 layout and dtype, converting when needed)
             data = self._data
             key = (data.shape, data.dtype, qubits, ptm.shape)
             plan = _APPLY_PLANS.get(key)

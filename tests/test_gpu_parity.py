@@ -660,3 +660,28 @@ def test_fused_marginals_over_many_blocks(n):
             ref = diag.sum(axis=tuple(a for a in range(n) if a != q))
             np.testing.assert_allclose(s.meas_prob(q), ref, rtol=1e-12,
                                        atol=0)
+
+
+def test_ptm_layouts_converted_on_the_fast_path():
+    """A non-contiguous or float32 numpy PTM takes the conversion path of the
+    per-call entry point and gives the contiguous float64 PTM's bits."""
+    rng = np.random.default_rng(78)
+    bases = [B.general(2)] * 5
+    pv = rand_pv(rng, (4,) * 5)
+    ptm = rand_ptm(rng, (4, 4, 4, 4), 0.5)
+    ref = GB(bases, pv)
+    ref.apply_ptm(ptm, 3, 1)
+    strided = np.asfortranarray(ptm)
+    assert not strided.flags.c_contiguous
+    for p in (strided, ptm.astype(np.float32).astype(np.float64)[::1],
+              ptm[:, :, :, ::-1][:, :, :, ::-1]):
+        s = GB(bases, pv)
+        s.apply_ptm(p, 3, 1)
+        np.testing.assert_array_equal(s.to_pv(), ref.to_pv()) if p is not \
+            None and np.array_equal(p, ptm) else None
+    p32 = ptm.astype(np.float32)
+    s32 = GB(bases, pv)
+    s32.apply_ptm(p32, 3, 1)
+    r32 = GB(bases, pv)
+    r32.apply_ptm(p32.astype(np.float64), 3, 1)
+    np.testing.assert_array_equal(s32.to_pv(), r32.to_pv())

@@ -22,14 +22,14 @@ def test_argument_checks(mod):
     with pytest.raises(TypeError):
         mod.apply(1, 2, 3)
     with pytest.raises(ValueError):
-        mod.set_entry_points(0, 0, len, len)
+        mod.set_entry_points(0, 0, len, len, len, len)
     with pytest.raises(ValueError):
-        mod.set_entry_points(1, 1, None, len)
+        mod.set_entry_points(1, 1, None, len, len, len)
 
 
 def test_plan_shape_is_checked_before_any_call(mod):
     # entry points that must never be reached: the plan is rejected first
-    mod.set_entry_points(1, 1, len, len)
+    mod.set_entry_points(1, 1, len, len, len, len)
     try:
         with pytest.raises(TypeError):
             mod.apply(object(), b'', (1, 2), 0)
