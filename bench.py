@@ -382,7 +382,8 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_batched:
         from quantumsim_gb300 import batch as qbatch
         batched = qbatch.benchmark(n_instances=args.batch_instances,
-                                   f64_check='all')
+                                   f64_check='all',
+                                   plain_all=args.plain_all)
         # whole step (forward + adjoint of every circuit) against HBM;
         # instances of up to 10 qubits largely live in L2
         batched['hbm_frac'] = batched['achieved_gbs'] / peak
@@ -996,6 +997,9 @@ def main():
     ap.add_argument('--no-batched', action='store_true',
                     help='skip the batched FP32 forward+adjoint measurement')
     ap.add_argument('--batch-instances', type=int, default=512)
+    ap.add_argument('--plain-all', action='store_true',
+                    help='also time the plain path on every batched instance '
+                         '(about 100 s)')
     ap.add_argument('--no-configs', action='store_true',
                     help='skip the qutrit and differentiation measurements')
     ap.add_argument('--traffic', type=float, default=0.0,

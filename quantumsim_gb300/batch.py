@@ -638,7 +638,8 @@ def plain_gradients(spec, ptms, target, dtype=torch.float32,
 
 
 def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
-              steps=3, autotune=True, f64_check='all', log=None):
+              steps=3, autotune=True, f64_check='all', log=None,
+              plain_all=False):
     """The batched configuration: `n_instances` circuits with qubit counts
     uniform in [q_min, q_max], own seeded noise, `depth` layers; FP32 Pauli
     vectors with FP64 probabilities / losses / PTM gradients.
@@ -648,7 +649,10 @@ def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
     plain GPU path's time (one instance at a time through ApplyPTM autograd,
     timed once per qubit count and summed over the instances) and the
     maximum probability error against FP64 (`f64_check`: 'all' instances or
-    one per qubit count)."""
+    one per qubit count).  With `plain_all` the plain path is also timed on
+    every instance (about 100 s for the default workload).  The gradient
+    mapping's share of the step is its own time (CUDA events over repeated
+    calls on the same stream) over the step's."""
     say = log or (lambda *a: None)
     rng = np.random.default_rng(seed)
     ns = rng.integers(q_min, q_max + 1, n_instances)
@@ -683,6 +687,13 @@ def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
     e1.record()
     torch.cuda.synchronize()
     step_s = e0.elapsed_time(e1) / 1e3 / steps
+    # the torch gradient mapping alone (it follows the kernel in the graph)
+    e0.record()
+    for _ in range(steps):
+        sim._map_gradients()
+    e1.record()
+    torch.cuda.synchronize()
+    map_s = e0.elapsed_time(e1) / 1e3 / steps
     probs, loss, grads = sim.results()
     # plain GPU path, one instance of every qubit count
     plain = {}
@@ -695,6 +706,14 @@ def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
         torch.cuda.synchronize()
         plain[n] = time.perf_counter() - a
     plain_s = float(sum(plain[int(n)] for n in ns))
+    plain_all_s = None
+    if plain_all:
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        for i in range(n_instances):
+            plain_gradients(specs[i], ptms[i], targets[i])
+        torch.cuda.synchronize()
+        plain_all_s = time.perf_counter() - a
     # probabilities against FP64 (the exact-arithmetic plain path)
     from .pauli_vector import PauliVectorGB300
     idx = range(n_instances) if f64_check == 'all' else \
@@ -719,6 +738,11 @@ def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
         'plain_step_s_est': plain_s,
         'plain_per_qubits_s': {str(k): v for k, v in plain.items()},
         'speedup_vs_plain': plain_s / step_s,
+        'plain_step_s_all_instances': plain_all_s,
+        'speedup_vs_plain_all_instances':
+            None if plain_all_s is None else plain_all_s / step_s,
+        'grad_mapping_s': map_s,
+        'grad_mapping_share': map_s / step_s,
         'max_prob_err_vs_f64': err,
         'f64_checked_instances': len(list(idx)),
         'tile': sim.tile, 'autotune_ms': tuned,

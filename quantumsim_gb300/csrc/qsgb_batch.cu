@@ -400,6 +400,32 @@ __device__ __noinline__ void adjoint2_warp(float* __restrict__ x, float* __restr
     const bool have = gi < end;
     const int64_t b = have ? group_base(geo, gi) : 0;
     {
+      // this warp's next tile into L2 while the current one is loaded and
+      // computed (the loads below are bound by their latency): lane l takes
+      // tensor l / 16 and, for Z >= 64, component l % 16 at the tile's first
+      // and last group (one 128-byte run each when the groups are
+      // consecutive along z); for Z == 1, line l % 4 of chunk row
+      // (l / 4) % 4 (the tile's 32 groups are 512 contiguous bytes per
+      // row).  Other strides are not prefetched.  Addresses are those of
+      // groups inside the item.
+      const int64_t tn = t0 + (int64_t)nwarps * 32;
+      if (tn < end) {
+        const float* base = (lane < 16) ? x : gv;
+        if (geo.lz >= 6) {
+          const int off = in_offset<K>(geo, lane & 15);
+          const int64_t last = tn + 31 < end ? tn + 31 : end - 1;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(base + group_base(geo, tn) + off));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(base + group_base(geo, last) + off));
+        } else if (vec && tn + 31 < end) {
+          const int64_t b0 = group_base(geo, tn), b1 = group_base(geo, tn + 31);
+          if (b1 - b0 == 31 * 4) {  // the 32 groups share x: rows are contiguous
+            const int q = (lane >> 2) & 3;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(base + b0 + in_offset<K>(geo, 4 * q) + 32 * (lane & 3)));
+          }
+        }
+      }
+    }
+    {
       float xo[K], go[K];
       if (!have) {
 #pragma unroll
