@@ -33,6 +33,11 @@ job for uncompiled unit lists, with a cost model for this hardware.
 ``__call__`` would apply to a vector with those bases, converting each PTM
 to the vector's bases on the way exactly as ``PTMOperation.__call__`` does.
 
+``reduce_bases(units, dims, keep_out)`` shrinks the bases the units work
+in to the entries that can be non-zero and are needed afterwards, as the
+reference's compiler does for given input and output bases; the reduced
+units are rectangular where a basis shrinks.
+
 ``FusedCircuit(units)`` plans once; calling it on a ``PauliVectorGB300``
 applies the fused PTMs.  ``capture(pv)`` records the fused applications of
 one vector into a CUDA graph (a static input and output buffer), so a
@@ -215,6 +220,153 @@ def plan(units):
     return [(v.ptm, v.qudits) for v in out if v is not None]
 
 
+def reduce_bases(units, dims, keep_out=None, tol=2.0 ** -52):
+    """Shrink the per-qudit Pauli bases a unit list works in, as the
+    reference's compiler does when it compiles an operation for given input
+    and output bases (``optimal_bases`` and its propagation,
+    quantumsim/operations/compiler.py:303-362, 37-96).
+
+    `units` are (ptm, qudits) in the vector's bases, applied in order to a
+    vector of per-qudit Pauli dims `dims`.  `keep_out` (optional, one entry
+    per qudit: None for all, else the indices of the final basis whose
+    entries the caller needs, e.g. the computational subbasis before a
+    measurement) declares what is read afterwards.
+
+    * Forward: the entries that can be non-zero.  After a unit, an output
+      index is active when its PTM row has an entry above `tol` times the
+      PTM's largest in an active input column (the residue the kernels skip
+      anyway); each qudit keeps the projection of that support.
+    * Backward: the entries needed.  Before a unit, an input index is needed
+      when its PTM column has an entry above the same threshold in a needed
+      row.
+    * Each unit's output is cut to the indices both active and needed; its
+      input columns are the vector's entries at that point (dropped columns
+      are either exactly zero or never read, so every kept entry is the same
+      sum as without the reduction).
+
+    The reference keeps basis elements carried by singular vectors above a
+    cutoff (1e-5 by default); the direct test here drops only what is zero
+    to the kernels' own precision.
+
+    Returns (units, kept): the reduced units (rectangular where a qudit's
+    basis shrinks) and, per qudit, the indices of the final basis kept
+    (None when all are)."""
+    n = len(dims)
+    us = [(np.ascontiguousarray(p, dtype=np.float64), tuple(int(q) for q in qs))
+          for p, qs in units]
+    # full per-qudit dims at every cut
+    cur = list(dims)
+    shapes = []
+    for p, qs in us:
+        k = len(qs)
+        din, dout = p.shape[k:], p.shape[:k]
+        if k not in (1, 2) or len(p.shape) != 2 * k:
+            raise ValueError('units act on one or two qudits')
+        for q, d in zip(qs, din):
+            if cur[q] != d:
+                raise ValueError('unit on {} expects dim {} where the vector '
+                                 'has {}'.format(qs, d, cur[q]))
+        shapes.append((tuple(din), tuple(dout)))
+        for q, d in zip(qs, dout):
+            cur[q] = d
+    final = list(cur)
+
+    def sig(p):
+        a = np.abs(p)
+        m = a.max() if a.size else 0.0
+        return a > tol * m if m > 0 else np.zeros(a.shape, dtype=bool)
+
+    def project(mask_nd, k):
+        # per-qudit masks of an index set over k qudits
+        return [mask_nd.any(axis=tuple(a for a in range(k) if a != j))
+                for j in range(k)]
+
+    def outer(masks):
+        m = masks[0]
+        for mm in masks[1:]:
+            m = np.logical_and.outer(m, mm)
+        return m
+
+    # forward: active masks after each unit, on its qudits
+    act = [np.ones(d, dtype=bool) for d in dims]
+    fwd = []
+    for (p, qs), (din, dout) in zip(us, shapes):
+        k = len(qs)
+        s_ = sig(p).reshape(int(np.prod(dout)), int(np.prod(din)))
+        cols = outer([act[q] for q in qs]).reshape(-1)
+        rows = s_[:, cols].any(axis=1).reshape(dout)
+        masks = project(rows, k)
+        fwd.append(masks)
+        for q, m in zip(qs, masks):
+            act[q] = m
+    # backward: needed masks before each unit (and after it)
+    need = [np.ones(d, dtype=bool) for d in final]
+    if keep_out is not None:
+        if len(keep_out) != n:
+            raise ValueError('keep_out needs one entry per qudit')
+        for q, idx in enumerate(keep_out):
+            if idx is not None:
+                m = np.zeros(final[q], dtype=bool)
+                m[np.asarray(idx, dtype=np.int64)] = True
+                need[q] = m
+    bwd = [None] * len(us)
+    for i in range(len(us) - 1, -1, -1):
+        (p, qs), (din, dout) = us[i], shapes[i]
+        k = len(qs)
+        bwd[i] = [need[q].copy() for q in qs]  # needed outputs of unit i
+        s_ = sig(p).reshape(int(np.prod(dout)), int(np.prod(din)))
+        rows = outer([need[q] for q in qs]).reshape(-1)
+        cols = s_[rows, :].any(axis=0).reshape(din)
+        for q, m in zip(qs, project(cols, k)):
+            need[q] = m
+    # rebuild: outputs cut to active and needed, inputs = the vector's
+    # entries at that point
+    phys = [np.arange(d) for d in dims]  # kept indices per qudit, full basis
+    out_units = []
+    for i, ((p, qs), (din, dout)) in enumerate(zip(us, shapes)):
+        k = len(qs)
+        keep = [np.nonzero(f & b)[0] for f, b in zip(fwd[i], bwd[i])]
+        # at least one index per qudit keeps the shapes valid (an all-zero
+        # output would be a zero vector)
+        keep = [kk if len(kk) else np.array([0]) for kk in keep]
+        sub = p
+        for j in range(k):  # rows of qudit j
+            sub = np.take(sub, keep[j], axis=j)
+        for j, q in enumerate(qs):  # columns: the vector's entries now
+            sub = np.take(sub, phys[q], axis=k + j)
+        out_units.append((np.ascontiguousarray(sub), qs))
+        for q, kk in zip(qs, keep):
+            phys[q] = kk
+    kept = [None if len(phys[q]) == final[q] and
+            np.array_equal(phys[q], np.arange(final[q])) else phys[q]
+            for q in range(n)]
+    return out_units, kept
+
+
+def _keep_indices(bases, bases_out):
+    """Per qudit, the indices of `bases[q]` whose elements make up
+    `bases_out[q]` (None: all)."""
+    if bases_out is None:
+        return None
+    if len(bases_out) != len(bases):
+        raise ValueError('bases_out needs one entry per qudit')
+    keep = []
+    for b, bo in zip(bases, bases_out):
+        if bo is None:
+            keep.append(None)
+            continue
+        vb = np.asarray(b.vectors).reshape(b.dim_pauli, -1)
+        idx = []
+        for v in np.asarray(bo.vectors).reshape(bo.dim_pauli, -1):
+            hit = [i for i in range(b.dim_pauli) if np.allclose(vb[i], v)]
+            if not hit:
+                raise ValueError('bases_out is not a subbasis of the '
+                                 'circuit\'s output basis')
+            idx.append(hit[0])
+        keep.append(sorted(idx))
+    return keep
+
+
 def units_of(operation, bases, *qubits):
     """(units, bases_after) of a reference quantumsim operation applied to
     `qubits` (default 0..n-1) of a vector whose bases are `bases`.
@@ -260,10 +412,23 @@ class FusedCircuit:
         self._prepared = set()
 
     @classmethod
-    def from_operation(cls, operation, bases, *qubits, fuse=True):
+    def from_operation(cls, operation, bases, *qubits, fuse=True,
+                       bases_out=None, reduce=False):
         """Fused circuit of a reference operation for vectors with
-        `bases` (see units_of)."""
+        `bases` (see units_of).  With `bases_out` (one entry per qudit of
+        the vector: None, or a subbasis of that qudit's output basis whose
+        elements are all the caller reads afterwards, e.g. the computational
+        subbasis before a measurement) or `reduce=True`, the units first
+        work in the smallest bases that give the same kept entries
+        (reduce_bases), as the reference's ``compile(bases_in, bases_out)``
+        does; the vector ends in the reduced bases."""
         units, after = units_of(operation, bases, *qubits)
+        if reduce or bases_out is not None:
+            keep = _keep_indices(after, bases_out)
+            units, kept = reduce_bases(units, [b.dim_pauli for b in bases],
+                                       keep)
+            after = [b if k is None else b.subbasis(list(int(i) for i in k))
+                     for b, k in zip(after, kept)]
         return cls(units, fuse=fuse, bases_out=after)
 
     @property

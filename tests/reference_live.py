@@ -185,6 +185,16 @@ def compiled_into_reduced_bases():
     same_states(pvs[GB], pvs[PauliVectorNumpy], 'compiled chain')
     print('compiled chain into reduced bases: dims {}'.format(
         [bb.dim_pauli for bb in pvs[GB].bases]))
+    # the same reduction done by this backend's planner on the uncompiled
+    # chain (quantumsim_gb300.circuit.reduce_bases), fused, on the GPU
+    from quantumsim_gb300.circuit import FusedCircuit
+    fc = FusedCircuit.from_operation(chain, list(bases_in), 0, 1, 2,
+                                     bases_out=list(bases_out))
+    gpv = GB.from_dm(dm, list(bases_in))
+    fc(gpv)
+    same_states(gpv, pvs[PauliVectorNumpy], 'planner-reduced chain')
+    print('planner-reduced fused chain: {} units in {} passes, dims {}'.format(
+        fc.n_units, fc.n_passes, [bb.dim_pauli for bb in gpv.bases]))
 
 
 def main():
