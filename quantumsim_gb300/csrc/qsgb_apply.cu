@@ -595,6 +595,69 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
   cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// small device PTMs on FP32 vectors
+// ---------------------------------------------------------------------------
+// Every term of an FP32 application is one FP32 FMA, so for a PTM in device
+// memory the generic kernel's per-block row plan and term lists (rebuilt by
+// every block, the values being on the device) cost more than the
+// arithmetic: ~16 us per launch on a 4 MB vector.  Here each block stages the
+// op matrix as floats (entries at or below 2^-30 of the largest skipped, the
+// generic kernel's FP32 rule) and each thread computes whole groups.
+constexpr int kDenseMaxK = 16;
+constexpr int kDenseBlock = 256;
+
+__global__ void __launch_bounds__(kDenseBlock) apply_dense_f32_kernel(const __grid_constant__ ApplyParams p) {
+  __shared__ float P[kDenseMaxK * kDenseMaxK];
+  __shared__ int64_t offin[kDenseMaxK], offout[kDenseMaxK];
+  __shared__ double wmax[kDenseBlock / 32];
+  const int t = threadIdx.x;
+  const int ne = p.kin * p.kout;  // <= kDenseBlock
+  double v = 0.0;
+  if (t < ne) {
+    const int r = t / p.kin, k = t - r * p.kin;
+    v = p.ptm[ptm_index(p, r, k)];
+  }
+  double m = fabs(v);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((t & 31) == 0) wmax[t >> 5] = m;
+  if (t < p.kin) {
+    const int ka = t / p.db_in, kb = t - ka * p.db_in;
+    offin[t] = ka * p.sai + kb * p.sbi;
+  }
+  if (t < p.kout) {
+    const int ra = t / p.db_out, rb = t - ra * p.db_out;
+    offout[t] = ra * p.sao + rb * p.sbo;
+  }
+  __syncthreads();
+  double amax = 0.0;
+#pragma unroll
+  for (int w = 0; w < kDenseBlock / 32; ++w) amax = fmax(amax, wmax[w]);
+  if (t < ne) P[t] = fabs(v) > amax * 0x1p-30 ? __double2float_rn(v) : 0.0f;
+  __syncthreads();
+  const float* __restrict__ X = static_cast<const float*>(p.in);
+  float* __restrict__ Y = static_cast<float*>(p.out);
+  for (uint64_t g = (uint64_t)blockIdx.x * kDenseBlock + t; g < p.n_items; g += (uint64_t)gridDim.x * kDenseBlock) {
+    const uint64_t t1 = fdiv(g, p.div_z);
+    const uint64_t z = g - t1 * p.div_z.d;
+    const uint64_t x = fdiv(t1, p.div_y);
+    const uint64_t y = t1 - x * p.div_y.d;
+    const int64_t bi = (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
+    const int64_t bo = (int64_t)x * p.sxo + (int64_t)y * p.syo + (int64_t)z;
+    float in[kDenseMaxK];
+#pragma unroll
+    for (int k = 0; k < kDenseMaxK; ++k) in[k] = k < p.kin ? X[bi + offin[k]] : 0.0f;
+#pragma unroll 4
+    for (int r = 0; r < p.kout; ++r) {
+      float a = 0.0f;
+#pragma unroll
+      for (int k = 0; k < kDenseMaxK; ++k)
+        if (k < p.kin) a = fmaf(P[r * p.kin + k], in[k], a);
+      Y[bo + offout[r]] = a;
+    }
+  }
+}
+
 // row groups = min(Kout, 4) rounded down to a power of two; the remaining
 // warps of the 8 are item warps (tile = 32 * 8 / row groups items)
 int pick_iw(int kout) {
@@ -854,6 +917,16 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)
   const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s, mode, src_out);
   if (js != QSGB_ERR_UNSUPPORTED || mode != kLaunch) return js;
+  // 2a. small device PTMs on FP32 vectors, no term limit: the dense kernel
+  if (!(flags & QSGB_PTM_HOST) && dtype == QSGB_F32 && kin <= kDenseMaxK && kout <= kDenseMaxK &&
+      p.max_terms == kin * kout) {
+    p.div_z = make_fastdiv((uint64_t)Z);
+    p.n_items = (uint64_t)X * Y * Z;
+    const uint64_t blocks = (p.n_items + kDenseBlock - 1) / kDenseBlock;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count() * 8));
+    apply_dense_f32_kernel<<<grid, kDenseBlock, 0, s>>>(p);
+    return launch_status();
+  }
   // 2. generic kernel; a host PTM travels inside its launch parameters
   if (flags & QSGB_PTM_HOST) {
     if (kin * kout > kMaxInline) return QSGB_ERR_UNSUPPORTED;

@@ -685,3 +685,34 @@ def test_ptm_layouts_converted_on_the_fast_path():
     r32 = GB(bases, pv)
     r32.apply_ptm(p32.astype(np.float64), 3, 1)
     np.testing.assert_array_equal(s32.to_pv(), r32.to_pv())
+
+
+def test_device_ptms_on_fp32_vectors():
+    """PTMs in device memory on FP32 vectors: the dense FP32 kernel (K <= 16,
+    no term limit: max_terms 0 or the PTM's size) and the generic kernel
+    (the 81 x 81 PTM),
+    against the oracle at FP32 accuracy, forward and transposed, in both
+    argument orders, one and two qudits, rectangular and qutrit PTMs."""
+    rng = np.random.default_rng(79)
+    cases = [((4,) * 6, (1, 4), (4, 4, 4, 4)),
+             ((4,) * 6, (5, 2), (4, 4, 4, 4)),
+             ((4,) * 6, (3,), (4, 4)),
+             ((4,) * 6, (5,), (4, 4)),
+             ((4, 4, 9, 4, 3), (2,), (9, 9)),
+             ((9, 4, 9), (0, 2), (9, 9, 9, 9)),
+             ((9, 4, 9), (1,), (2, 4))]
+    for shape, qs, pshape in cases:
+        x = rand_pv(rng, shape).astype(np.float32)
+        ptm = rand_ptm(rng, pshape, 0.7)
+        for tr in (False, True):
+            if tr and pshape[:len(qs)] != pshape[len(qs):]:
+                continue
+            ref = (O.apply_ptm_transposed(x.astype(np.float64), ptm, *qs)
+                   if tr else O.apply_ptm(x.astype(np.float64), ptm, *qs))
+            scale = np.abs(ref).max()
+            for max_terms in (0, ptm.size):
+                y = torch.ops.qsgb.apply_ptm(
+                    torch.from_numpy(x).cuda(), torch.from_numpy(ptm).cuda(),
+                    list(qs), L.ARITH_F32, max_terms, tr)
+                np.testing.assert_allclose(y.cpu().numpy(), ref, rtol=1e-5,
+                                           atol=1e-5 * scale)
