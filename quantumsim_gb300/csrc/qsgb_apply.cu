@@ -596,19 +596,26 @@ __global__ void __launch_bounds__(kBlock) apply_ptm_kernel(const __grid_constant
 }
 
 // ---------------------------------------------------------------------------
-// small device PTMs on FP32 vectors
+// small device PTMs, plain dense kernel
 // ---------------------------------------------------------------------------
-// Every term of an FP32 application is one FP32 FMA, so for a PTM in device
-// memory the generic kernel's per-block row plan and term lists (rebuilt by
-// every block, the values being on the device) cost more than the
-// arithmetic: ~16 us per launch on a 4 MB vector.  Here each block stages the
-// op matrix as floats (entries at or below 2^-30 of the largest skipped, the
-// generic kernel's FP32 rule) and each thread computes whole groups.
+// For a PTM in device memory the generic kernel's per-block row plan and
+// term lists (rebuilt by every block, the values being on the device) cost
+// more than the arithmetic on small vectors: ~16 us per launch on a 4 MB
+// FP32 vector, ~20 us for a 4 x 4 PTM on an 8 MB FP64 one.  Here each block
+// stages the op matrix in the storage type and each thread computes whole
+// groups: FP32 FMAs for FP32 storage (entries at or below 2^-30 of the
+// largest skipped, the generic kernel's FP32 rule), native FP64 FMAs for
+// FP64 storage (entries at or below 2^-52 of the largest skipped under
+// 'auto', exact zeros under 'f64'; exact IEEE products and sums, so no
+// range fallback is needed).  FP64 takes this path only for one-qubit PTMs
+// on vectors small enough for the FP64 pipe (at most 2^23 FMAs, ~14 us).
 constexpr int kDenseMaxK = 16;
 constexpr int kDenseBlock = 256;
+constexpr double kDenseMaxF64Fma = 8388608.0;  // 2^23
 
-__global__ void __launch_bounds__(kDenseBlock) apply_dense_f32_kernel(const __grid_constant__ ApplyParams p) {
-  __shared__ float P[kDenseMaxK * kDenseMaxK];
+template <typename T, int KMAX>
+__global__ void __launch_bounds__(kDenseBlock) apply_dense_kernel(const __grid_constant__ ApplyParams p) {
+  __shared__ T P[KMAX * KMAX];
   __shared__ int64_t offin[kDenseMaxK], offout[kDenseMaxK];
   __shared__ double wmax[kDenseBlock / 32];
   const int t = threadIdx.x;
@@ -633,10 +640,11 @@ __global__ void __launch_bounds__(kDenseBlock) apply_dense_f32_kernel(const __gr
   double amax = 0.0;
 #pragma unroll
   for (int w = 0; w < kDenseBlock / 32; ++w) amax = fmax(amax, wmax[w]);
-  if (t < ne) P[t] = fabs(v) > amax * 0x1p-30 ? __double2float_rn(v) : 0.0f;
+  const double thr = sizeof(T) == 4 ? amax * 0x1p-30 : (p.arith == QSGB_ARITH_F64 ? 0.0 : amax * 0x1p-52);
+  if (t < ne) P[t] = fabs(v) > thr ? (T)v : (T)0;
   __syncthreads();
-  const float* __restrict__ X = static_cast<const float*>(p.in);
-  float* __restrict__ Y = static_cast<float*>(p.out);
+  const T* __restrict__ X = static_cast<const T*>(p.in);
+  T* __restrict__ Y = static_cast<T*>(p.out);
   for (uint64_t g = (uint64_t)blockIdx.x * kDenseBlock + t; g < p.n_items; g += (uint64_t)gridDim.x * kDenseBlock) {
     const uint64_t t1 = fdiv(g, p.div_z);
     const uint64_t z = g - t1 * p.div_z.d;
@@ -644,15 +652,15 @@ __global__ void __launch_bounds__(kDenseBlock) apply_dense_f32_kernel(const __gr
     const uint64_t y = t1 - x * p.div_y.d;
     const int64_t bi = (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
     const int64_t bo = (int64_t)x * p.sxo + (int64_t)y * p.syo + (int64_t)z;
-    float in[kDenseMaxK];
+    T in[KMAX];
 #pragma unroll
-    for (int k = 0; k < kDenseMaxK; ++k) in[k] = k < p.kin ? X[bi + offin[k]] : 0.0f;
+    for (int k = 0; k < KMAX; ++k) in[k] = k < p.kin ? X[bi + offin[k]] : (T)0;
 #pragma unroll 4
     for (int r = 0; r < p.kout; ++r) {
-      float a = 0.0f;
+      T a = (T)0;
 #pragma unroll
-      for (int k = 0; k < kDenseMaxK; ++k)
-        if (k < p.kin) a = fmaf(P[r * p.kin + k], in[k], a);
+      for (int k = 0; k < KMAX; ++k)
+        if (k < p.kin) a = fma(P[r * p.kin + k], in[k], a);
       Y[bo + offout[r]] = a;
     }
   }
@@ -917,15 +925,25 @@ int apply_common(const void* in, void* out, const double* ptm, int64_t da_out, i
   // 1. kernel specialised to the PTM's sparsity pattern (host PTMs)
   const int js = try_jit(ptm, da_out, db_out, da_in, db_in, Z, flags, dtype, arith, pair, p, s, mode, src_out);
   if (js != QSGB_ERR_UNSUPPORTED || mode != kLaunch) return js;
-  // 2a. small device PTMs on FP32 vectors, no term limit: the dense kernel
-  if (!(flags & QSGB_PTM_HOST) && dtype == QSGB_F32 && kin <= kDenseMaxK && kout <= kDenseMaxK &&
-      p.max_terms == kin * kout) {
-    p.div_z = make_fastdiv((uint64_t)Z);
-    p.n_items = (uint64_t)X * Y * Z;
-    const uint64_t blocks = (p.n_items + kDenseBlock - 1) / kDenseBlock;
-    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count() * 8));
-    apply_dense_f32_kernel<<<grid, kDenseBlock, 0, s>>>(p);
-    return launch_status();
+  // 2a. small device PTMs, no term limit: the dense kernel (FP32 storage up
+  // to 16 x 16; FP64 storage for one-qubit PTMs on small vectors)
+  if (!(flags & QSGB_PTM_HOST) && p.max_terms == kin * kout) {
+    const double fmas = (double)X * (double)Y * (double)Z * (double)(kin * kout);
+    const bool f32 = dtype == QSGB_F32 && kin <= kDenseMaxK && kout <= kDenseMaxK;
+    const bool f64 = dtype == QSGB_F64 && (arith == QSGB_ARITH_AUTO || arith == QSGB_ARITH_F64) && kin <= 4 &&
+                     kout <= 4 && fmas <= kDenseMaxF64Fma;
+    if (f32 || f64) {
+      p.div_z = make_fastdiv((uint64_t)Z);
+      p.n_items = (uint64_t)X * Y * Z;
+      const uint64_t blocks = (p.n_items + kDenseBlock - 1) / kDenseBlock;
+      const unsigned grid =
+          (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count() * 8));
+      if (f32)
+        apply_dense_kernel<float, kDenseMaxK><<<grid, kDenseBlock, 0, s>>>(p);
+      else
+        apply_dense_kernel<double, 4><<<grid, kDenseBlock, 0, s>>>(p);
+      return launch_status();
+    }
   }
   // 2. generic kernel; a host PTM travels inside its launch parameters
   if (flags & QSGB_PTM_HOST) {

@@ -716,3 +716,26 @@ def test_device_ptms_on_fp32_vectors():
                     list(qs), L.ARITH_F32, max_terms, tr)
                 np.testing.assert_allclose(y.cpu().numpy(), ref, rtol=1e-5,
                                            atol=1e-5 * scale)
+
+
+def test_small_device_ptms_fp64():
+    """One-qubit PTMs in device memory on small FP64 vectors take the dense
+    kernel in native FP64 (the same products and sums as numpy): per entry
+    at 1e-12 against the oracle, forward and transposed, every position,
+    including a qubit in a 3-element subbasis; a larger vector takes the
+    generic kernel and agrees too."""
+    rng = np.random.default_rng(80)
+    for shape in ((4,) * 6, (4, 3, 4, 4), (4,) * 11):
+        x = rand_pv(rng, shape)
+        for q in range(len(shape)):
+            d = shape[q]
+            ptm = rand_ptm(rng, (d, d))
+            for tr in (False, True):
+                ref = (O.apply_ptm_transposed(x, ptm, q) if tr
+                       else O.apply_ptm(x, ptm, q))
+                y = torch.ops.qsgb.apply_ptm(
+                    torch.from_numpy(x).cuda(), torch.from_numpy(ptm).cuda(),
+                    [q], L.ARITH_AUTO, 0, tr).cpu().numpy()
+                absref = (O.apply_ptm_transposed(np.abs(x), np.abs(ptm), q)
+                          if tr else O.apply_ptm(np.abs(x), np.abs(ptm), q))
+                assert_close_dot(y, ref, absref)
