@@ -30,8 +30,11 @@
 // Stage 2 adds the per-block partials of each entry in a fixed order
 // (deterministic).
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "qsgb_common.cuh"
+#include "qsgb_tc.h"
 
 namespace qsgb {
 namespace {
@@ -268,7 +271,7 @@ __global__ void __launch_bounds__(kGradBlock) grad_stage1(const __grid_constant_
   const int EP = p.nmt * 16;  // padded entries
   float2* red2 = reinterpret_cast<float2*>(smem + p.off_red2);  // [chunks][EP] (MPT == 1)
   double* fb2 = reinterpret_cast<double*>(smem + p.off_red2 + kGradBlock * sizeof(float2));
-  if (MPT == 1) {
+  if constexpr (MPT == 1) {
     // level 1: entry qp, slice chunk ch (slices ch, ch + nch, ...); with
     // many slices (small PTMs) the chunks spread the sums over the block
     const int nch = EP < kGradBlock ? kGradBlock / EP : 1;
@@ -311,8 +314,7 @@ __global__ void __launch_bounds__(kGradBlock) grad_stage1(const __grid_constant_
         if (r < p.kout && k < p.kin) part[(int64_t)blockIdx.x * E + r * p.kin + k] = d;
       }
     }
-    return;
-  }
+  } else {
   for (int qp = t; qp < EP; qp += kGradBlock) {
     const int mtq = qp >> 4, q = qp & 15;
     const int r = (mtq / p.nmt_c) * 4 + (q >> 2), k = (mtq % p.nmt_c) * 4 + (q & 3);
@@ -329,6 +331,7 @@ __global__ void __launch_bounds__(kGradBlock) grad_stage1(const __grid_constant_
     double d = qsgb_df_to_double(S, C);
     if (any_fb) d += F;
     if (r < p.kout && k < p.kin) part[(int64_t)blockIdx.x * E + r * p.kin + k] = d;
+  }
   }
 }
 
@@ -351,6 +354,248 @@ __global__ void __launch_bounds__(kStage2Entries* kStage2Slices)
     for (int i = 0; i < kStage2Slices; ++i) s += red[i][el];
     out[e] = s;
   }
+}
+
+// ---------------------------------------------------------------------------
+// 16 x 16 gradients on FP64 vectors: the tensor cores
+// ---------------------------------------------------------------------------
+// The same reduction as a product over groups, dP = G^T X per chunk of 16
+// groups, on mma.sync.m16n8k16 (FP16 operands, FP32 accumulators) with the
+// error-free digit split of the apply kernel (qsgb_tc.h): within a chunk,
+// row r of A = G^T is scaled by its largest exponent over the chunk's 16
+// groups and column k of B = X by its own, each value written as a 57-bit
+// fixed-point integer in six balanced base-1024 FP16 digits.  For every digit
+// pair (i, j) with i + j <= 5 two MMAs (k = 0..7, 8..15) add into level
+// i + j; levels 0..3 are exact FP32 integer sums (below 2^24).  The six levels
+// of each entry are combined in int64, scaled by 2^(E_r + E_k - 2098) and
+// added to FP64 accumulators in chunk order.  Error per chunk: about
+// 2^-47.7 max_g |g_out[g, r]| max_g |x_in[g, k]| over the chunk's groups.
+// A chunk holding inf or nan, or with a result outside the normal double
+// range, is recomputed in native FP64 from global memory.
+//
+// A warp takes chunks; lane l = (h, i) = (l / 16, l % 16) loads group i of
+// the chunk, rows r = 8h .. 8h+7 of g_out and k = 8h .. 8h+7 of x_in, and
+// writes their digits into the warp's planes A[d][r][g] and B[d][k][g]
+// (FP16).  The fragments then follow the m16n8k16 layouts: lane
+// (gid, tig) = (l / 4, l % 4) reads A rows gid, gid + 8 at columns 2 tig and
+// 2 tig + 8, B rows (k) nt * 8 + gid, and ends with entries
+// (r, k) = (gid or gid + 8, nt * 8 + 2 tig + {0, 1}).
+constexpr int kTcgBlock = 256;
+constexpr int kTcgWarps = kTcgBlock / 32;
+constexpr int kTcgPlane = 16 * 16;  // halves per digit plane
+
+struct TcgWarpSmem {
+  unsigned short a[tc::kDigits][kTcgPlane];  // digits of g_out: [r][g]
+  unsigned short b[tc::kDigits][kTcgPlane];  // digits of x_in: [k][g]
+  int er[16], ek[16];                        // chunk exponents of rows, columns
+};
+struct TcgSmem {
+  TcgWarpSmem warp[kTcgWarps];
+  int64_t oin[16], oout[16];  // row offsets of x_in and g_out
+};
+
+__device__ __forceinline__ unsigned ld_pair(const unsigned short* plane, int row, int col) {
+  return *reinterpret_cast<const unsigned*>(plane + row * 16 + col);
+}
+
+__global__ void __launch_bounds__(kTcgBlock) grad16_tc_kernel(const __grid_constant__ GradParams p,
+                                                              double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  TcgSmem& sm = *reinterpret_cast<TcgSmem*>(smem);
+  TcgWarpSmem& ws = sm.warp[w];
+  const double* __restrict__ X = static_cast<const double*>(p.x);
+  const double* __restrict__ G = static_cast<const double*>(p.g);
+  const int h = lane >> 4, i = lane & 15;
+  const int gid = lane >> 2, tig = lane & 3;
+  if (threadIdx.x < 16) {
+    const int k = threadIdx.x;
+    const int ka = k / p.db_in, kb = k - ka * p.db_in;
+    sm.oin[k] = ka * p.sai + kb * p.sbi;
+    const int ra = k / p.db_out, rb = k - ra * p.db_out;
+    sm.oout[k] = ra * p.sao + rb * p.sbo;
+  }
+  __syncthreads();
+  auto bases = [&](uint64_t g, int64_t& bi, int64_t& bo) {
+    const uint64_t t1 = fdiv(g, p.div_z);
+    const uint64_t z = g - t1 * p.div_z.d;
+    const uint64_t x = fdiv(t1, p.div_y);
+    const uint64_t y = t1 - x * p.div_y.d;
+    bi = (int64_t)x * p.sxi + (int64_t)y * p.syi + (int64_t)z;
+    bo = (int64_t)x * p.sxo + (int64_t)y * p.syo + (int64_t)z;
+  };
+  double acc[2][4];
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[nt][q] = 0.0;
+
+  const uint64_t n_chunks = (p.n_groups + 15) / 16;
+  const uint64_t wstride = (uint64_t)gridDim.x * kTcgWarps;
+  for (uint64_t c = (uint64_t)blockIdx.x * kTcgWarps + w; c < n_chunks; c += wstride) {
+    const uint64_t g = c * 16 + i;
+    const bool live = g < p.n_groups;
+    double gv[8], xv[8];
+    if (live) {
+      int64_t bi, bo;
+      bases(g, bi, bo);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        gv[j] = G[bo + sm.oout[8 * h + j]];
+        xv[j] = X[bi + sm.oin[8 * h + j]];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) gv[j] = xv[j] = 0.0;
+    }
+    // chunk exponents of rows 8h+j (g_out) and columns 8h+j (x_in): maxima
+    // over the 16 lanes of this half
+    unsigned eg[8], ex[8], nonfinite = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const unsigned hg = (unsigned)__double2hiint(gv[j]), hx = (unsigned)__double2hiint(xv[j]);
+      nonfinite |= (((hg >> 20) & 0x7ffu) == 0x7ffu || ((hx >> 20) & 0x7ffu) == 0x7ffu) ? 1u : 0u;
+      eg[j] = tc::exp_eff(hg);
+      ex[j] = tc::exp_eff(hx);
+#pragma unroll
+      for (int o = 1; o < 16; o <<= 1) {
+        eg[j] = max(eg[j], __shfl_xor_sync(0xffffffffu, eg[j], o));
+        ex[j] = max(ex[j], __shfl_xor_sync(0xffffffffu, ex[j], o));
+      }
+    }
+    if (i == 0) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        ws.er[8 * h + j] = (int)eg[j];
+        ws.ek[8 * h + j] = (int)ex[j];
+      }
+    }
+    // digits: low half of each pair the g_out digit, high half the x_in one
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const unsigned long long ug =
+          tc::fixed_biased((unsigned)__double2hiint(gv[j]), (unsigned)__double2loint(gv[j]), eg[j]);
+      const unsigned long long ux =
+          tc::fixed_biased((unsigned)__double2hiint(xv[j]), (unsigned)__double2loint(xv[j]), ex[j]);
+#pragma unroll
+      for (int d = 0; d < tc::kDigits; ++d) {
+        const unsigned pr = tc::digit_pair(ug, ux, 10 * (tc::kDigits - 1 - d));
+        ws.a[d][(8 * h + j) * 16 + i] = (unsigned short)(pr & 0xffffu);
+        ws.b[d][(8 * h + j) * 16 + i] = (unsigned short)(pr >> 16);
+      }
+    }
+    const bool chunk_bad = __any_sync(0xffffffffu, nonfinite != 0u);
+    __syncwarp();
+    long long v[2][4];
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[nt][q] = 0;
+#pragma unroll
+    for (int L = 0; L < tc::kDigits; ++L) {
+      float dl[2][4];
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dl[nt][q] = 0.f;
+#pragma unroll
+      for (int a = 0; a <= L; ++a) {
+        const unsigned fa[4] = {ld_pair(ws.a[a], gid, 2 * tig), ld_pair(ws.a[a], gid + 8, 2 * tig),
+                                ld_pair(ws.a[a], gid, 2 * tig + 8), ld_pair(ws.a[a], gid + 8, 2 * tig + 8)};
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+          const unsigned fbv[2] = {ld_pair(ws.b[L - a], nt * 8 + gid, 2 * tig),
+                                   ld_pair(ws.b[L - a], nt * 8 + gid, 2 * tig + 8)};
+          tc::mma16816(dl[nt], fa, fbv);
+        }
+      }
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const long long t = (long long)__float2int_rn(dl[nt][q]);
+          v[nt][q] += L < 5 ? (t << (10 * (4 - L))) : (t >> 10);
+        }
+    }
+    // scale and accumulate (in FP64 from global memory when the chunk or a
+    // result is out of range)
+    double y[2][4];
+    unsigned bad = 0;
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = gid + (q >= 2 ? 8 : 0), k = nt * 8 + 2 * tig + (q & 1);
+        const int sc = (ws.er[r] - 1022) + (ws.ek[k] - 1022) - 54;
+        const long long vv = v[nt][q];
+        double d = 0.0;
+        if (vv != 0) {
+          d = __ll2double_rn(vv);
+          const int hi = __double2hiint(d);
+          const int e = ((hi >> 20) & 0x7ff) + sc;
+          bad |= (e < 1 || e > 2046) ? 1u : 0u;
+          d = __hiloint2double(hi + (sc << 20), __double2loint(d));
+        }
+        y[nt][q] = d;
+      }
+    if (chunk_bad || __any_sync(0xffffffffu, bad != 0u)) {
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int r = gid + (q >= 2 ? 8 : 0), k = nt * 8 + 2 * tig + (q & 1);
+          const int ka = k / p.db_in, kb = k - ka * p.db_in, ra = r / p.db_out, rb = r - ra * p.db_out;
+          const int64_t ok = ka * p.sai + kb * p.sbi, orr = ra * p.sao + rb * p.sbo;
+          double s2 = 0.0;
+#pragma unroll 1
+          for (int gg = 0; gg < 16; ++gg) {
+            const uint64_t g2 = c * 16 + gg;
+            if (g2 >= p.n_groups) break;
+            int64_t bi, bo;
+            bases(g2, bi, bo);
+            s2 = fma(G[bo + orr], X[bi + ok], s2);
+          }
+          y[nt][q] = s2;
+        }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[nt][q] += y[nt][q];
+    __syncwarp();  // the planes are rewritten by the next chunk
+  }
+  // block sums over the warps, in warp order
+  __syncthreads();
+  double* red = reinterpret_cast<double*>(smem);  // [warps][256], over the planes
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = gid + (q >= 2 ? 8 : 0), k = nt * 8 + 2 * tig + (q & 1);
+      red[w * 256 + r * 16 + k] = acc[nt][q];
+    }
+  __syncthreads();
+  {
+    const int e = threadIdx.x;  // 256 entries, 256 threads
+    double s2 = 0.0;
+    for (int ww = 0; ww < kTcgWarps; ++ww) s2 += red[ww * 256 + e];
+    part[(int64_t)blockIdx.x * 256 + e] = s2;
+  }
+}
+
+unsigned tcg_blocks(uint64_t n_groups) {
+  const uint64_t chunks = (n_groups + 15) / 16;
+  const uint64_t blocks = (chunks + kTcgWarps - 1) / kTcgWarps;
+  return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sm_count() * 2));
+}
+
+// 16 x 16 FP64 gradients go to the tensor cores unless QSGB_TC_GRAD=0
+bool tc_grad_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("QSGB_TC_GRAD");
+    return !(v && std::strcmp(v, "0") == 0);
+  }();
+  return on;
 }
 
 GradParams make_params(const void* x_in, const void* g_out, int64_t da_out, int64_t db_out, int64_t da_in,
@@ -425,6 +670,16 @@ int grad_common(const void* x_in, const void* g_out, double* dptm, int64_t da_ou
   if (!scratch || scratch_bytes < (int64_t)nb * E * (int64_t)sizeof(double)) return QSGB_ERR_SCRATCH;
   cudaStream_t s = as_stream(stream);
   double* part = static_cast<double*>(scratch);
+  if (dtype == QSGB_F64 && kin == 16 && kout == 16 && tc_grad_enabled()) {
+    const unsigned nbt = tcg_blocks(p.n_groups);  // <= nb: the scratch holds its partials
+    const int smem_bytes = std::max((int)sizeof(TcgSmem), kTcgWarps * 256 * (int)sizeof(double));
+    const int st = allow_dynamic_smem((const void*)grad16_tc_kernel, smem_bytes);
+    if (st != QSGB_OK) return st;
+    grad16_tc_kernel<<<nbt, kTcgBlock, smem_bytes, s>>>(p, part);
+    grad_stage2<<<(E + kStage2Entries - 1) / kStage2Entries, kStage2Entries * kStage2Slices, 0, s>>>(part, (int)nbt,
+                                                                                                     E, dptm);
+    return launch_status();
+  }
   const bool two = p.nmt > kGradBlock;
   int st;
   if (dtype == QSGB_F64)

@@ -54,43 +54,6 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ void mma16816(float* d, const unsigned* a, const unsigned* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// Biased exponent of x as used for scaling (subnormals and zero count as 1)
-// and its 53-bit significand (implicit bit included for normal numbers).
-__device__ __forceinline__ unsigned exp_eff(unsigned hi) {
-  const unsigned e = (hi >> 20) & 0x7ffu;
-  return e == 0u ? 1u : e;
-}
-
-// F + B for input x = (hi, lo) against group exponent emax (biased, >= e):
-// F = sign(x) * (m << 4) >> (emax - e), |F| < 2^57.
-__device__ __forceinline__ unsigned long long fixed_biased(unsigned hi, unsigned lo, unsigned emax) {
-  const unsigned e = (hi >> 20) & 0x7ffu;
-  const unsigned mh = (hi & 0xfffffu) | (e != 0u ? 0x100000u : 0u);
-  const unsigned long long m = ((unsigned long long)mh << 32 | lo) << 4;
-  const unsigned s = emax - (e == 0u ? 1u : e);
-  unsigned long long f = s < 64u ? (m >> s) : 0ull;
-  if (hi & 0x80000000u) f = 0ull - f;
-  return f + kDigitBias;
-}
-
-// FP16x2 register of digit plane j (bit position p = 10 (5 - j)) of two
-// inputs: (v_a - 512, v_b - 512) built from 0x6400 | v = 1024 + v.
-__device__ __forceinline__ unsigned digit_pair(unsigned long long ua, unsigned long long ub, int p) {
-  const unsigned a = (unsigned)(ua >> p) & 0x3ffu;
-  const unsigned b = (unsigned)(ub >> p) & 0x3ffu;
-  const unsigned r = a | (b << 16) | 0x64006400u;
-  unsigned out;
-  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(out) : "r"(r), "r"(0x66006600u));  // - (1536, 1536)
-  return out;
-}
 
 // 2^sc * sum_L A_L 2^(10 (4 - L)); bad |= 1 when the result is not a normal
 // double (or zero).
