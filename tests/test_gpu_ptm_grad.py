@@ -17,6 +17,7 @@ import pytest
 import torch
 
 from oracle import pauli_vector_np as O
+import quantumsim_gb300  # noqa: F401  (registers the torch.ops.qsgb operators)
 
 pytestmark = pytest.mark.gpu
 
@@ -170,3 +171,17 @@ print('float-float ok')
                          capture_output=True, text=True, timeout=600)
     assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
     assert 'float-float ok' in run.stdout
+
+
+def test_tensor_core_gradient_partial_chunks():
+    """16 x 16 gradients whose group count is not a multiple of the 16 of a
+    chunk: 15 groups (bystanders of dims 3 and 5), a single group (the two
+    qubits alone), and 35 groups in both argument orders."""
+    rng = np.random.default_rng(36)
+    for shape, qs in [((4, 3, 4, 5), (0, 2)), ((4, 4), (0, 1)),
+                      ((4, 4), (1, 0)), ((5, 4, 7, 4), (3, 1)),
+                      ((5, 4, 7, 4), (1, 3))]:
+        x = rng.standard_normal(shape)
+        g = rng.standard_normal(shape)
+        assert _tc_path(x, qs, [g.shape[q] for q in qs])
+        _check(x, g, qs)

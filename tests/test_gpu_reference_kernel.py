@@ -13,6 +13,7 @@ import torch
 from conftest import assert_close_dot
 from oracle import pauli_vector_np as O
 from oracle import ref_gpu
+import quantumsim_gb300  # noqa: F401  (registers the torch.ops.qsgb operators)
 
 pytestmark = pytest.mark.gpu
 
