@@ -51,6 +51,14 @@ class NoisyCircuitModel:
             'cz_phase': torch.zeros(n_qubits - 1, dtype=torch.float64),
         }
         self.basis = _bases.general(2)
+        self._dev_consts = {}  # device tensors made once (no copies per step)
+
+    def _device_const(self, key, make):
+        v = self._dev_consts.get(key)
+        if v is None:
+            v = make()
+            self._dev_consts[key] = v
+        return v
 
     @property
     def n_params(self):
@@ -80,7 +88,9 @@ class NoisyCircuitModel:
         n, nl = self.n, self.n_layers
         dev = p['angle_offset'].device
         groups = torch.arange(nl, device=dev) % self.n_groups
-        angles = self.base_angles.to(dev) + p['angle_offset'][groups]
+        base = self._device_const(('angles', str(dev)),
+                                  lambda: self.base_angles.to(dev))
+        angles = base + p['angle_offset'][groups]
         axes = [ax for row in self.axes for ax in row]
         rot = P.rotations_batched(axes, angles.reshape(-1), self.basis)
         gamma, lam = P.damping_rates(p['t1'] * 1e-6, p['t2'] * 1e-6, T_GATE)
@@ -151,13 +161,15 @@ class NoisyCircuitModel:
         two-qubit PTMs (Np, 4, 4, 4, 4) indexed by ``schedule(fuse)``; with
         `fuse` each pair PTM is CZ (R_i (x) R_i+1) of its layer."""
         one_q, cz = self.build_ptms(p)
-        _, singles, pairs = self.schedule(fuse)
         dev = one_q.device
-        ls = torch.tensor([l for l, _ in singles], device=dev)
-        qs = torch.tensor([q for _, q in singles], device=dev)
+
+        def indices():
+            _, singles, pairs = self.schedule(fuse)
+            return tuple(torch.tensor(v, device=dev) for v in (
+                [l for l, _ in singles], [q for _, q in singles],
+                [l for l, _ in pairs], [i for _, i in pairs]))
+        ls, qs, lp, ip = self._device_const(('units', fuse, str(dev)), indices)
         s = one_q[ls, qs]
-        lp = torch.tensor([l for l, _ in pairs], device=dev)
-        ip = torch.tensor([i for _, i in pairs], device=dev)
         c = cz[ip]
         if fuse:
             k = torch.einsum('nac,nbd->nabcd', one_q[lp, ip], one_q[lp, ip + 1])
@@ -203,24 +215,25 @@ class NoisyCircuitModel:
 
 
 class GraphedGradient:
-    """Gradient steps of ``model.loss`` with the circuit replayed from a CUDA
-    graph.
+    """Gradient steps of ``model.loss`` replayed from one CUDA graph.
 
-    A step builds every PTM of the circuit from the parameters on the GPU
-    in batch (``build_units``: a few dozen small torch operations), copies
-    them into the graph's two static PTM buffers, replays the graph -- the
-    circuit forward with checkpoints every `checkpoint_every` layers, the
-    diagonal, the KL loss and the whole backward pass down to the PTM
-    gradients, gathered into two static gradient buffers: about 1,500 kernel
-    launches that would otherwise each cost a host call -- and finishes the
-    backward through the batched builder into the parameters.  The PTMs stay
-    on the device, so the apply kernels read them from device memory and
-    nothing synchronises inside the graph.  Each application's PTM is a leaf
-    of its own (a view of the static buffer), so the backward pass writes
-    each PTM gradient once, with no scatter into a stacked tensor.
+    The graph holds the whole step: the batched PTM builder
+    (``build_units``: rotations, damping, CZs and the fused pair products for
+    all layers) from static copies of the parameters, the circuit forward
+    with checkpoints every `checkpoint_every` layers, the diagonal, the KL
+    loss, the backward pass down to the PTM gradients and on through the
+    builder into the static parameters' gradients: about 1,300 kernel
+    launches that would otherwise each cost a host call.  Each application's
+    PTM is a leaf of its own (a view of a static buffer the builder's output
+    is copied into), so the backward pass writes each PTM gradient once,
+    with no zero-fill of a stacked tensor per use.  The PTMs stay on the
+    device, so the apply kernels read them from device memory; the builder
+    makes its constants once per device, so nothing is copied from the host
+    and nothing synchronises inside the graph.
 
-    ``step(p)`` returns the loss as a device scalar and leaves the gradients
-    in ``p[name].grad`` (accumulated, as in ``loss.backward()``)."""
+    ``step(p)`` copies the parameters in, replays the graph, returns the
+    loss as a device scalar and adds the gradients to ``p[name].grad``
+    (accumulated, as in ``loss.backward()``)."""
 
     def __init__(self, model, target, dtype=torch.float64, checkpoint_every=8,
                  fuse=True, device=None):
@@ -243,9 +256,11 @@ class GraphedGradient:
             self.idx_off.append(len(self.idx_list))
         self._diag = Diagonal
         self.sched = model.schedule(fuse)[0]
+        # static parameters (leaves of the builder inside the graph)
+        self.sp = {k: v.detach().to(self.dev).clone().requires_grad_(True)
+                   for k, v in model.init.items()}
         with torch.no_grad():
-            p0 = {k: v.to(self.dev) for k, v in model.init.items()}
-            s0, c0 = model.build_units(p0, fuse)
+            s0, c0 = model.build_units(self.sp, fuse)
         self.s_buf = s0.detach().clone()
         self.c_buf = c0.detach().clone()
         self.s_leaves = [self.s_buf[i].detach().requires_grad_(True)
@@ -253,25 +268,37 @@ class GraphedGradient:
         self.c_leaves = [self.c_buf[i].detach().requires_grad_(True)
                          for i in range(self.c_buf.shape[0])]
         # warm up on a side stream (compiles nothing: device PTMs use the
-        # precompiled kernels), then capture
+        # precompiled kernels, the builder's constants are made here), then
+        # capture
         side = torch.cuda.Stream(self.dev)
         side.wait_stream(torch.cuda.current_stream(self.dev))
         with torch.cuda.stream(side):
             for _ in range(2):
                 self._clear()
-                self._loss().backward()
+                self._step_body()
             self._clear()
             self.graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self.graph, stream=side):
-                self.loss = self._loss()
-                self.loss.backward()
-                self.s_grad = torch.stack([t.grad for t in self.s_leaves])
-                self.c_grad = torch.stack([t.grad for t in self.c_leaves])
+                self.loss = self._step_body()
+                self.p_grad = {k: v.grad for k, v in self.sp.items()}
         torch.cuda.current_stream(self.dev).wait_stream(side)
 
     def _clear(self):
-        for t in self.s_leaves + self.c_leaves:
+        for t in self.s_leaves + self.c_leaves + list(self.sp.values()):
             t.grad = None
+
+    def _step_body(self):
+        """Builder, circuit, loss, backward to the static parameters."""
+        s, c = self.model.build_units(self.sp, self.fuse)
+        with torch.no_grad():
+            self.s_buf.copy_(s)
+            self.c_buf.copy_(c)
+        loss = self._loss()
+        loss.backward()
+        s_grad = torch.stack([t.grad for t in self.s_leaves])
+        c_grad = torch.stack([t.grad for t in self.c_leaves])
+        torch.autograd.backward([s, c], [s_grad, c_grad])
+        return loss
 
     def _loss(self):
         leaves = {1: self.s_leaves, 2: self.c_leaves}
@@ -288,12 +315,19 @@ class GraphedGradient:
         return torch.sum(t * (torch.log(t) - torch.log(prob)))
 
     def step(self, p):
-        s, c = self.model.build_units(p, self.fuse)
         with torch.no_grad():
-            self.s_buf.copy_(s)
-            self.c_buf.copy_(c)
+            for k, v in self.sp.items():
+                v.copy_(p[k])
         self.graph.replay()
-        torch.autograd.backward([s, c], [self.s_grad, self.c_grad])
+        with torch.no_grad():
+            for k, v in p.items():
+                if not v.requires_grad:
+                    continue
+                g = self.p_grad[k].to(v.device)
+                if v.grad is None:
+                    v.grad = g.clone()
+                else:
+                    v.grad += g
         return self.loss
 
 

@@ -38,8 +38,37 @@ def _t(x, ref=None):
     return torch.tensor(float(x), dtype=torch.float64, device=dev)
 
 
+# Device constants made once per device (and contents), so that building
+# PTMs issues no host-to-device copy: the batched builders can then be
+# captured in a CUDA graph.
+_CONSTS = {}
+
+
+def _const(key, make):
+    v = _CONSTS.get(key)
+    if v is None:
+        if len(_CONSTS) > 4096:
+            _CONSTS.clear()
+        v = make()
+        _CONSTS[key] = v
+    return v
+
+
+def _imag_unit(device):
+    return _const(('1j', str(device)),
+                  lambda: torch.tensor(1j, dtype=_CDTYPE, device=device))
+
+
 def _basis_tensor(bases, device):
-    """Kronecker product of the basis vectors: (prod dim_pauli, D, D)."""
+    """Kronecker product of the basis vectors: (prod dim_pauli, D, D),
+    cached per device and basis contents."""
+    key = ('basis', str(device)) + tuple(
+        (np.asarray(b.vectors).shape, np.asarray(b.vectors).tobytes())
+        for b in bases)
+    return _const(key, lambda: _basis_tensor_make(bases, device))
+
+
+def _basis_tensor_make(bases, device):
     vecs = None
     for b in bases:
         v = torch.as_tensor(np.asarray(b.vectors), dtype=_CDTYPE, device=device)
@@ -244,7 +273,7 @@ def rotations_batched(axes, angles, basis=None):
     a = angles.to(torch.float64)
     c = torch.cos(a / 2).to(_CDTYPE)
     s = torch.sin(a / 2).to(_CDTYPE)
-    j = torch.tensor(1j, dtype=_CDTYPE, device=a.device)
+    j = _imag_unit(a.device)
     e = torch.exp(-j * a.to(_CDTYPE) / 2)
     zero = torch.zeros_like(c)
     kx = torch.stack([torch.stack([c, -j * s], -1),
@@ -252,8 +281,9 @@ def rotations_batched(axes, angles, basis=None):
     ky = torch.stack([torch.stack([c, -s], -1), torch.stack([s, c], -1)], -2)
     kz = torch.stack([torch.stack([e, zero], -1),
                       torch.stack([zero, e.conj()], -1)], -2)
-    code = torch.tensor([{'x': 0, 'y': 1, 'z': 2}[ax] for ax in axes],
-                        device=a.device)
+    axes = tuple(axes)
+    code = _const(('axes', str(a.device), axes), lambda: torch.tensor(
+        [{'x': 0, 'y': 1, 'z': 2}[ax] for ax in axes], device=a.device))
     k = torch.where((code == 0)[:, None, None], kx,
                     torch.where((code == 1)[:, None, None], ky, kz))
     d = basis.dim_hilbert
@@ -290,7 +320,7 @@ def cphase_batched(angles, basis=None):
     """(E,) conditional phases -> (E, 4, 4, 4, 4) cphase PTMs."""
     basis = basis or _bases.general(2)
     a = angles.to(torch.float64)
-    j = torch.tensor(1j, dtype=_CDTYPE, device=a.device)
+    j = _imag_unit(a.device)
     one = torch.ones_like(a).to(_CDTYPE)
     diag = torch.stack([one, one, one, torch.exp(j * a.to(_CDTYPE))], -1)
     return kraus_to_ptm_batched(torch.diag_embed(diag)[:, None],
