@@ -826,8 +826,10 @@ def run_profile_grad(args):
     10-qubit model (--profile-dtype f64 or f32): the graph is captured and
     replayed once outside the profiled range, then replayed once between
     cudaProfilerStart and cudaProfilerStop (run ncu with
-    --profile-from-start off): about 1,100 launches, nearly all of them the
-    apply, tensor-core and PTM-gradient kernels."""
+    --profile-from-start off). The graph holds the whole step: the batched
+    PTM builder and its backward (a few hundred small torch kernels) and
+    about 1,100 launches of the apply, tensor-core and PTM-gradient
+    kernels."""
     import torch
     from quantumsim_gb300 import build as qbuild
     qbuild.build()
