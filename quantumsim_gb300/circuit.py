@@ -161,7 +161,224 @@ def _aligned(unit2, pair):
 
 def plan(units):
     """Fuse a list of (ptm, qudits) units; returns the fused list of
-    (ptm, qudits) in application order."""
+    (ptm, qudits) in application order.
+
+    Two planners run and the plan with the lower modelled time is kept
+    (the greedy one on a tie): the greedy pass (`_plan_greedy`) and the
+    assignment search (`_plan_assigned`), which chooses for every run of
+    one-qudit units the neighbour it joins."""
+    greedy = _plan_greedy(units)
+    assigned = _plan_assigned(units)
+    return assigned if plan_cost(assigned) < plan_cost(greedy) else greedy
+
+
+def plan_cost(fused):
+    """Modelled time (seconds per TB streamed, summed over passes) of a
+    fused unit list; rectangular units count as one K = 16 pass."""
+    t = 0.0
+    for ptm, qs in fused:
+        n = len(qs)
+        if n in (1, 2) and ptm.shape[:n] == ptm.shape[n:]:
+            k = int(np.prod(ptm.shape[:n]))
+            t += pass_cost(ptm.reshape(k, k))
+        else:
+            t += 1.0 / _RATES[16][0][1]
+    return t
+
+
+def _gain(merged, parts):
+    c = pass_cost(merged)
+    return c != float('inf') and c < sum(pass_cost(p) for p in parts)
+
+
+class _Run:
+    """Consecutive one-qudit units on one qudit, merged into one matrix;
+    `prev` / `next` are the two-qudit units it may join (the one before it
+    on its qudit with nothing in between, and the one after it)."""
+
+    __slots__ = ('q', 'mat', 'last', 'prev', 'next', 'choice')
+
+    def __init__(self, q, mat, last, prev):
+        self.q, self.mat, self.last, self.prev = q, mat, last, prev
+        self.next = None
+        self.choice = 'alone'
+
+
+def _plan_assigned(units, max_sweeps=30):
+    """Fusion by assignment.  Consecutive one-qudit units on a qudit merge
+    into runs (while the model says so).  Every run then either stays a
+    pass of its own or joins the two-qudit unit just before or just after it
+    on its qudit (it commutes with everything in between); the choices are
+    made by coordinate descent on the modelled time (each run's best
+    option with the others fixed, until nothing changes), from three
+    starting points: no run joined, runs preferring the unit after, runs
+    preferring the unit before.  Finally two two-qudit units on the same
+    pair with nothing else on either qudit in between merge while that is
+    cheaper.  Rectangular units and units on more qudits are barriers."""
+    U = [_Unit(p, qs) for p, qs in units]
+    runs = []
+    open_run = {}   # qudit -> run still open (nothing else on the qudit since)
+    host_last = {}  # qudit -> last two-qudit unit on it (None after a barrier)
+    for i, u in enumerate(U):
+        if u.square and len(u.qudits) == 1:
+            q = u.qudits[0]
+            j = open_run.get(q)
+            if j is not None:
+                merged = u.mat @ runs[j].mat
+                if _gain(merged, [u.mat, runs[j].mat]):
+                    runs[j].mat = merged
+                    runs[j].last = i
+                    continue
+            # a second run on the qudit cannot reach the unit before
+            runs.append(_Run(q, u.mat, i, host_last.get(q) if j is None else None))
+            open_run[q] = len(runs) - 1
+            continue
+        host = u.square and len(u.qudits) == 2
+        for q in u.qudits:
+            j = open_run.pop(q, None)
+            if j is not None and host:
+                runs[j].next = i
+            host_last[q] = i if host else None
+    hosts = [i for i, u in enumerate(U) if u.square and len(u.qudits) == 2]
+    before = {i: [] for i in hosts}
+    after = {i: [] for i in hosts}
+
+    def embed(r, i):
+        return _embed(_Unit(r.mat, (r.q,)), U[i].qudits, U[i].dims)
+
+    def full(i):
+        m = U[i].mat
+        for j in before[i]:
+            m = m @ embed(runs[j], i)
+        for j in after[i]:
+            m = embed(runs[j], i) @ m
+        return m
+
+    cache = {}
+
+    def host_cost(i):
+        key = (i, tuple(before[i]), tuple(after[i]))
+        c = cache.get(key)
+        if c is None:
+            c = cache[key] = pass_cost(full(i))
+        return c
+
+    run_cost = [pass_cost(r.mat) for r in runs]
+
+    def set_choice(j, c):
+        r = runs[j]
+        if r.choice == 'prev':
+            after[r.prev].remove(j)
+        elif r.choice == 'next':
+            before[r.next].remove(j)
+        r.choice = c
+        if c == 'prev':
+            after[r.prev].append(j)
+            after[r.prev].sort()
+        elif c == 'next':
+            before[r.next].append(j)
+            before[r.next].sort()
+
+    def local(j):
+        r = runs[j]
+        c = run_cost[j] if r.choice == 'alone' else 0.0
+        if r.prev is not None:
+            c += host_cost(r.prev)
+        if r.next is not None:
+            c += host_cost(r.next)
+        return c
+
+    def options(r):
+        return ['alone'] + (['prev'] if r.prev is not None else []) + \
+            (['next'] if r.next is not None else [])
+
+    def descend():
+        for _ in range(max_sweeps):
+            changed = False
+            for j, r in enumerate(runs):
+                cur = r.choice
+                best, best_c = cur, local(j)
+                for c in options(r):
+                    if c == cur:
+                        continue
+                    set_choice(j, c)
+                    lc = local(j)
+                    if lc < best_c * (1 - 1e-12):
+                        best, best_c = c, lc
+                    set_choice(j, cur)
+                if best != cur:
+                    set_choice(j, best)
+                    changed = True
+            if not changed:
+                break
+        return sum(host_cost(i) for i in hosts) + sum(
+            run_cost[j] for j, r in enumerate(runs) if r.choice == 'alone')
+
+    best_total, best_choice = None, None
+    for start in ('alone', 'next', 'prev'):
+        for j, r in enumerate(runs):
+            set_choice(j, 'alone')
+        if start != 'alone':
+            for j, r in enumerate(runs):
+                opts = options(r)
+                pick = start if start in opts else opts[-1]
+                set_choice(j, pick)
+        t = descend()
+        if best_total is None or t < best_total:
+            best_total, best_choice = t, [r.choice for r in runs]
+    for j, c in enumerate(best_choice):
+        set_choice(j, c)
+
+    # two-qudit units on one pair with nothing else on either qudit between
+    mats = {i: full(i) for i in hosts}
+    into = {}       # host merged into a later one
+    last = {}       # qudit -> ('host', i) or another marker
+    alone_end = {r.last: j for j, r in enumerate(runs) if r.choice == 'alone'}
+    for i, u in enumerate(U):
+        if i in mats:
+            a, b = u.qudits
+            la, lb = last.get(a), last.get(b)
+            if la is not None and la == lb and la[0] == 'host':
+                v = la[1]
+                merged = mats[i] @ _aligned_mat(U[v], mats[v], u.qudits)
+                if _gain(merged, [mats[i], mats[v]]):
+                    mats[i] = merged
+                    into[v] = i
+            last[a] = last[b] = ('host', i)
+        elif u.square and len(u.qudits) == 1:
+            if i in alone_end:
+                last[u.qudits[0]] = ('run', i)
+        else:
+            for q in u.qudits:
+                last[q] = ('other', i)
+    out = []
+    for i, u in enumerate(U):
+        if i in mats:
+            if i not in into:
+                out.append((mats[i].reshape(u.dims + u.dims), u.qudits))
+        elif u.square and len(u.qudits) == 1:
+            j = alone_end.get(i)
+            if j is not None:
+                d = runs[j].mat.shape[0]
+                out.append((runs[j].mat.reshape(d, d), (runs[j].q,)))
+        else:
+            out.append((u.ptm, u.qudits))
+    return out
+
+
+def _aligned_mat(unit2, mat, pair):
+    """`mat`, a matrix over unit2's qudits, with its qudits in the order of
+    `pair`."""
+    if unit2.qudits == tuple(pair):
+        return mat
+    da, db = unit2.dims
+    m = mat.reshape(da, db, da, db).transpose(1, 0, 3, 2)
+    return m.reshape(da * db, da * db)
+
+
+def _plan_greedy(units):
+    """Fuse in one pass over the units: each unit merges into what came
+    before when the model says the product is cheaper."""
     out = []
     last = {}  # qudit -> index in `out` of the last unit touching it
 

@@ -227,3 +227,59 @@ def test_plan_random_unit_sequences():
         assert len(fused) <= len(units)
         assert_close_dot(_apply_all(pv, fused), _apply_all(pv, units),
                          _abs_all(np.abs(pv), units) * 16 + 1e-300)
+
+
+def test_both_planners_on_random_sequences():
+    """The greedy planner and the assignment search each give a correct
+    plan on their own (plan() returns whichever the model prefers)."""
+    for seed in range(12):
+        rng = np.random.default_rng(500 + seed)
+        units, n = _random_units(rng)
+        shape = []
+        for q in range(n):
+            first = [u for u in units if q in u[1]]
+            d = 4
+            if first:
+                ptm, qs = first[0]
+                d = ptm.shape[len(qs) + qs.index(q)]
+            shape.append(d)
+        pv = _rand_pv(rng, tuple(shape))
+        ref = _apply_all(pv, units)
+        bound = _abs_all(np.abs(pv), units) * 16 + 1e-300
+        for planner in (C._plan_greedy, C._plan_assigned):
+            fused = planner(units)
+            assert len(fused) <= len(units)
+            assert_close_dot(_apply_all(pv, fused), ref, bound)
+
+
+def test_assignment_search_on_the_noisy_circuit():
+    """Noisy rotations and CZs on random pairs (the 14-qubit circuit's
+    structure at 6 qubits): the assignment plan is correct, and on the
+    14-qubit circuit itself its modelled time is below the greedy plan's
+    with no more passes."""
+    rng = np.random.default_rng(7)
+    units = [(p, qs) for _, p, qs in workloads.config1_circuit(
+        seed=5, n_qubits=6, n_layers=8, n_2q=3)[0]]
+    fused = C._plan_assigned(units)
+    assert len(fused) < len(units)
+    pv = _rand_pv(rng, (4,) * 6)
+    assert_close_dot(_apply_all(pv, fused), _apply_all(pv, units),
+                     _abs_all(np.abs(pv), units), rtol=chain_rtol(units))
+    big = [(p, qs) for _, p, qs in workloads.config1_circuit(seed=1)[0]]
+    g, a = C._plan_greedy(big), C._plan_assigned(big)
+    assert len(a) <= len(g)
+    assert C.plan_cost(a) < 0.95 * C.plan_cost(g)
+    assert C.plan_cost(C.plan(big)) == C.plan_cost(a)
+
+
+def test_runs_join_the_cheaper_neighbour():
+    """A rotation between two CZs on its qubit joins one of them (not
+    both, not neither), and a second run on the qudit (one whose product
+    with the first the model rejects) is left for the unit after it."""
+    rng = np.random.default_rng(8)
+    t1, t2 = workloads.coherence_times(rng, 2)
+    cz = workloads.noisy_cz(rng, (0, 1), t1, t2)
+    r = workloads.noisy_1q(rng, t1[0], t2[0])
+    f = C._plan_assigned([(cz, (0, 1)), (r, (0,)), (cz, (0, 1))])
+    assert [qs for _, qs in f] in ([(0, 1)], [(0, 1), (0, 1)])
+    assert all(len(qs) == 2 for _, qs in f)
