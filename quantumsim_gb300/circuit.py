@@ -20,9 +20,11 @@ A merge is made only when the time model says the merged PTM is cheaper
 than the two passes: an application's time per byte streamed is
 interpolated from rates measured on GB300 for the specialised FP64 kernels,
 by PTM size and non-zero terms per row (denser rows take more float-float
-arithmetic per element, and the 81x81 kernels degrade fastest).  PTM products are formed in
-FP64 on the host; the fused result differs from unit-by-unit application by
-rounding only.
+arithmetic per element, and the 81x81 kernels degrade fastest).  ``plan``
+runs two planners, a greedy pass and a search that chooses for every run of
+one-qudit units which neighbouring two-qudit unit it joins, and keeps the
+plan the model rates faster.  PTM products are formed in FP64 on the host;
+the fused result differs from unit-by-unit application by rounding only.
 
 The reference's compiler merges units too when it compiles an operation
 for given bases (quantumsim/operations/compiler.py); ``plan`` does the same
