@@ -10,17 +10,18 @@ KL(target || prob) and dL/dP for every PTM of its circuit.
 Circuits are the CPU-runnable workload family: per layer a noisy rotation on
 every qubit (rotation, then amplitude + phase damping over 20 ns) and CZs on
 a line matching.  Ops are grouped into units first (`plan_units`): a CZ
-absorbs the rotations before it on its two qubits, so a layer of n rotations
+absorbs the rotations waiting on its two qubits, from its own layer and
+from earlier layers where the qubit had no CZ, so a layer of n rotations
 and ~n/2 CZs costs ~n/2 passes over the state instead of ~3n/2.  The device
 program is built once per circuit structure:
 
     stage 0              INIT  (|0..0>)
     stages ...           APPLY of unit j of every instance (instances aligned
-                         by unit index), SAVE at every `checkpoint_every`
-                         layers
+                         by unit index), SAVE at the unit boundary before
+                         every `checkpoint_every`-th layer
                          ZERO_G, LOSS
     stages ...           ADJOINT of the units in reverse, RESTORE at the
-                         saved layers (drift refresh)
+                         saved boundaries (drift refresh)
     last stage           GRADSUM per unit PTM
 
 after which batched 16 x 16 contractions turn the units' gradients into
@@ -157,46 +158,124 @@ def validate_ops(ops, n, depth, what='circuit'):
 def plan_units(ops, fuse=True):
     """Group a circuit's ops into the units the kernel applies.
 
-    ops: [(layer, qubits)] in application order.  With `fuse`, a two-qubit
-    op absorbs the one-qubit ops still pending on its two qubits in the same
-    layer: the unit's PTM is F = C (R_a (x) R_b), a dense 16 x 16 PTM like any
-    two-qubit PTM of the kernel, so the unit costs one pass where the three
-    ops cost three.  One-qubit ops that meet no two-qubit op in their layer
-    stay single units.  A pending op is only delayed past ops on other
-    qubits, and every layer ends with its own units, so checkpoints still
-    fall between layers.
+    ops: [(layer, qubits)] in application order.  With `fuse`, a one-qubit
+    op waits on its qubit (across layers, past ops on other qubits, which
+    it commutes with) until the next two-qubit op on that qubit absorbs it.
+    That unit's PTM is F = C (A (x) B), with A and B the products of the
+    one-qubit ops waiting on its two qubits (identity where none): a dense
+    16 x 16 PTM like any two-qubit PTM of the kernel, so the unit costs one
+    pass where its ops cost several.  The one-qubit ops that meet no later
+    two-qubit op become one-qubit units (their product) at the end.  Without
+    `fuse` every op is a unit of its own.
 
-    Returns [(layer, qubits, members)]: members = (j,) for a one-qubit unit
-    (qubits = (q,)), (j_c, j_a, j_b) for a two-qubit unit (qubits = (a, b)
-    sorted; j_a / j_b = -1 where no one-qubit op was absorbed)."""
+    A unit's layer is its two-qubit op's layer (for the one-qubit units at
+    the end, the last op's layer), so the layers of the units never
+    decrease; checkpoints sit at unit boundaries (`build_program`).
+
+    Returns [(layer, qubits, members)]: members = (chain,) for a one-qubit
+    unit (qubits = (q,)), (j_c, chain_a, chain_b) for a two-qubit unit
+    (qubits = (a, b) sorted); a chain is the tuple of one-qubit op indices
+    in application order (empty: the identity)."""
     units = []
+    if not fuse:
+        for j, (l, qs) in enumerate(ops):
+            if len(qs) == 1:
+                units.append((l, (qs[0],), ((j,),)))
+            else:
+                units.append((l, (min(qs), max(qs)), (j, (), ())))
+        return units
     pending = {}
-    layer = None
-
-    def flush():
-        for q, j in sorted(pending.items(), key=lambda t: t[1]):
-            units.append((ops[j][0], (q,), (j,)))
-        pending.clear()
-
     for j, (l, qs) in enumerate(ops):
-        if l != layer:
-            flush()
-            layer = l
         if len(qs) == 1:
-            q = qs[0]
-            if not fuse:
-                units.append((l, (q,), (j,)))
-                continue
-            if q in pending:
-                units.append((l, (q,), (pending.pop(q),)))
-            pending[q] = j
+            pending.setdefault(qs[0], []).append(j)
         else:
             a, b = min(qs), max(qs)
-            ja = pending.pop(a, -1)
-            jb = pending.pop(b, -1)
-            units.append((l, (a, b), (j, ja, jb)))
-    flush()
+            units.append((l, (a, b), (j, tuple(pending.pop(a, ())),
+                                      tuple(pending.pop(b, ())))))
+    if pending:
+        last = ops[-1][0]
+        for q, chain in sorted(pending.items(), key=lambda t: t[1][0]):
+            units.append((last, (q,), (tuple(chain),)))
     return units
+
+
+def unit_ops(members):
+    """Every op index of a unit's members."""
+    if len(members) == 1:
+        return list(members[0])
+    return [members[0]] + list(members[1]) + list(members[2])
+
+
+def chain_products(mats, chains):
+    """Products of one-qubit PTM chains and the factors of their gradients.
+
+    mats: (n_ops, 4, 4) float64 tensor (any op's row; only chain members are
+    read); chains: tuples of op indices in application order.  For a chain
+    r_0 .. r_{m-1}, prod = r_{m-1} ... r_0 (the identity for an empty
+    chain), and for its element i, dL/dr_i = L_i^T (dL/dprod) R_i^T with
+    L_i = r_{m-1} ... r_{i+1} and R_i = r_{i-1} ... r_0.
+
+    Returns (prod (n_chains, 4, 4), elem_op, elem_chain, left_t, right_t):
+    one entry per chain element, left_t = L_i^T and right_t = R_i^T."""
+    n = len(chains)
+    dt, dev = mats.dtype, mats.device
+    prod = torch.eye(4, dtype=dt, device=dev).repeat(n, 1, 1)
+    e_op, e_ch, lt, rt = [], [], [], []
+    by_len = {}
+    for c, ch in enumerate(chains):
+        if ch:
+            by_len.setdefault(len(ch), []).append(c)
+    for m, cs in sorted(by_len.items()):
+        idx = torch.as_tensor([chains[c] for c in cs], dtype=torch.long,
+                              device=dev)
+        r = mats[idx]                                   # (k, m, 4, 4)
+        eye = torch.eye(4, dtype=dt, device=dev).expand(len(cs), 4, 4)
+        pre = [eye]                                     # r_{i-1} ... r_0
+        for i in range(1, m):
+            pre.append(torch.bmm(r[:, i - 1], pre[-1]))
+        suf = [eye] * m                                 # r_{m-1} ... r_{i+1}
+        for i in range(m - 2, -1, -1):
+            suf[i] = torch.bmm(suf[i + 1], r[:, i + 1])
+        prod[torch.as_tensor(cs, device=dev)] = torch.bmm(r[:, m - 1],
+                                                          pre[m - 1])
+        for i in range(m):
+            e_op.append(idx[:, i])
+            e_ch.append(torch.as_tensor(cs, dtype=torch.long, device=dev))
+            lt.append(suf[i].transpose(1, 2))
+            rt.append(pre[i].transpose(1, 2))
+    if not e_op:
+        z = torch.zeros(0, dtype=torch.long, device=dev)
+        zz = torch.zeros(0, 4, 4, dtype=dt, device=dev)
+        return prod, z, z, zz, zz
+    return (prod, torch.cat(e_op), torch.cat(e_ch), torch.cat(lt),
+            torch.cat(rt))
+
+
+def map_unit_gradients(g_one, g_two, c, a, b, chain_factors):
+    """dL/dP of the original ops from the units' gradients (any device):
+    g_one (n1, 4, 4) of the one-qubit units, g_two (n2, 16, 16) of the
+    two-qubit units F = C K with K = A (x) B (c, a, b their factors), and
+    chain_factors = (elem_op, elem_chain, left_t, right_t) of the chains
+    ordered one-qubit units, then side a, then side b of the two-qubit
+    units (`chain_products`).  Returns (dL/dC (n2, 16, 16), [(op indices,
+    dL/dr (k, 4, 4))] for the chain elements).
+
+    dL/dC = G K^T; with H = C^T G viewed as [a', b', a, b],
+    dL/dA = sum H B[b', b] and dL/dB = sum H A[a', a]; each chain element
+    then gets L^T (dL/dprod) R^T."""
+    e_op, e_ch, lt, rt = chain_factors
+    parts = [g_one]
+    dc = None
+    if len(g_two):
+        kr = torch.einsum('uac,ubd->uabcd', a, b).reshape(-1, 16, 16)
+        dc = torch.bmm(g_two, kr.transpose(1, 2))
+        h = torch.bmm(c.transpose(1, 2), g_two).view(-1, 4, 4, 4, 4)
+        parts += [torch.einsum('uxyzw,uyw->uxz', h, b),
+                  torch.einsum('uxyzw,uxz->uyw', h, a)]
+    gch = torch.cat(parts)
+    d = torch.bmm(torch.bmm(lt, gch[e_ch]), rt) if len(e_op) else \
+        gch[:0]
+    return dc, (e_op, d)
 
 
 def build_program(units, unit_base, sizes, depths, every, tile,
@@ -219,26 +298,30 @@ def build_program(units, unit_base, sizes, depths, every, tile,
     for i, (unit_list, size, depth) in enumerate(zip(units, sizes, depths)):
         ops = [(l, qs) for l, qs, _ in unit_list]
         layer_of = [l for l, _ in ops]
+        # checkpoint k holds the state at the boundary before the first
+        # unit of layer >= every * (k + 1) (after the last unit if none is)
+        n_ck = max(0, (depth - 1) // every)
+        bound = [int(np.searchsorted(layer_of, every * (k + 1), side='left'))
+                 for k in range(n_ck)]
         seq = [(BOP_INIT, -1, -1, 0, size)]
-        for j, (l, qs) in enumerate(ops):
-            pidx = int(unit_base[i]) + j
-            q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
-            seq.append((BOP_APPLY, q0, q1, pidx,
-                        size // (4 if q1 < 0 else 16)))
-            last_of_layer = j + 1 == len(ops) or layer_of[j + 1] != l
-            if last_of_layer and (l + 1) % every == 0 and l + 1 < depth:
-                seq.append((BOP_SAVE, -1, -1, (l + 1) // every - 1, size))
+        for j in range(len(ops) + 1):
+            seq += [(BOP_SAVE, -1, -1, k, size)
+                    for k, bj in enumerate(bound) if bj == j]
+            if j < len(ops):
+                l, qs = ops[j]
+                q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
+                seq.append((BOP_APPLY, q0, q1, int(unit_base[i]) + j,
+                            size // (4 if q1 < 0 else 16)))
         seq.append((BOP_ZERO_G, -1, -1, 0, size))
         seq.append((BOP_LOSS, -1, -1, 0, 1))
-        for j in reversed(range(len(ops))):
-            l, qs = ops[j]
-            pidx = int(unit_base[i]) + j
-            q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
-            seq.append((BOP_ADJOINT, q0, q1, pidx,
-                        size // (4 if q1 < 0 else 16)))
-            first_of_layer = j == 0 or layer_of[j - 1] != l
-            if first_of_layer and l > 0 and l % every == 0:
-                seq.append((BOP_RESTORE, -1, -1, l // every - 1, size))
+        for j in range(len(ops), -1, -1):
+            if j < len(ops):
+                l, qs = ops[j]
+                q0, q1 = (qs[0], -1) if len(qs) == 1 else (min(qs), max(qs))
+                seq.append((BOP_ADJOINT, q0, q1, int(unit_base[i]) + j,
+                            size // (4 if q1 < 0 else 16)))
+            seq += [(BOP_RESTORE, -1, -1, k, size)
+                    for k, bj in enumerate(bound) if bj == j]
         for k, (op, q0, q1, pp, total) in enumerate(seq):
             ent.append((k, op, i, q0, q1, pp, total))
     e = np.array(ent, dtype=np.int64)
@@ -286,10 +369,10 @@ def build_program(units, unit_base, sizes, depths, every, tile,
 class BatchedSimulator:
     """Forward + adjoint of many circuits in one persistent launch.
 
-    With `fuse` (default) each two-qubit op absorbs the one-qubit ops before
-    it on its qubits (`plan_units`); `results()` still returns dL/dP for
-    every original op: step() maps the units' gradients back with batched
-    16 x 16 contractions on the same stream (inside the CUDA graph)."""
+    With `fuse` (default) each two-qubit op absorbs the one-qubit ops
+    waiting on its qubits (`plan_units`); `results()` still returns dL/dP
+    for every original op: step() maps the units' gradients back with
+    batched contractions on the same stream (inside the CUDA graph)."""
 
     def __init__(self, specs, targets, checkpoint_every=8, tile=None,
                  device=None, cooperative=True, fuse=True):
@@ -409,40 +492,40 @@ class BatchedSimulator:
         return total
 
     def _index_units(self):
-        """Flat index arrays of the units: slot and op of every one-qubit
-        unit; slot, C op, R_a op and R_b op (-1: none) of every two-qubit
-        unit."""
-        one_slot, one_op, two_slot, two_ops = [], [], [], []
+        """Flat index arrays of the units: slot and chain of every one-qubit
+        unit; slot, C op and the two chains of every two-qubit unit.  The
+        chains are listed one-qubit units first, then side a, then side b
+        of the two-qubit units (`chain_products`, `map_unit_gradients`)."""
+        one_slot, one_chain = [], []
+        two_slot, two_c, two_a, two_b = [], [], [], []
         for i, units in enumerate(self.units):
             ub, ob = int(self.unit_base[i]), int(self.op_base[i])
             for u, (_, qs, mem) in enumerate(units):
                 if len(qs) == 1:
                     one_slot.append(ub + u)
-                    one_op.append(ob + mem[0])
+                    one_chain.append(tuple(ob + m for m in mem[0]))
                 else:
                     two_slot.append(ub + u)
-                    two_ops.append([ob + m if m >= 0 else -1 for m in mem])
+                    two_c.append(ob + mem[0])
+                    two_a.append(tuple(ob + m for m in mem[1]))
+                    two_b.append(tuple(ob + m for m in mem[2]))
         dev = self.device
         as_idx = (lambda v: torch.as_tensor(np.asarray(v, dtype=np.int64),
                                             device=dev))
-        self._one_slot, self._one_op = as_idx(one_slot), as_idx(one_op)
-        two = np.asarray(two_ops, dtype=np.int64).reshape(-1, 3)
-        self._two_slot = as_idx(two_slot)
-        self._two_c = as_idx(two[:, 0])
-        self._two_has = [two[:, 1] >= 0, two[:, 2] >= 0]
-        self._two_r = [as_idx(two[:, 1][two[:, 1] >= 0]),
-                       as_idx(two[:, 2][two[:, 2] >= 0])]
-        self._two_r_sel = [as_idx(np.nonzero(h)[0]) for h in self._two_has]
-        self._two_np = two
+        self._one_slot = as_idx(one_slot)
+        self._two_slot, self._two_c = as_idx(two_slot), as_idx(two_c)
+        self._two_c_np = np.asarray(two_c, dtype=np.int64)
+        self._chains = one_chain + two_a + two_b
+        self._n_one, self._n_two = len(one_slot), len(two_slot)
 
     # ------------------------------------------------------------ PTMs
     def set_ptms(self, ptms_per_instance):
         """ptms_per_instance[i][j]: (K, K) float64 PTM of op j of instance i
         (two-qubit ones (16, 16) or (4, 4, 4, 4) in sorted qubit order; any
-        device).  Builds the units' PTMs (F = C (R_a (x) R_b) for fused
-        units) and their inverses in FP64 on the host, and stores them in
-        FP32 on the GPU; keeps C, R_a, R_b and R_a (x) R_b (FP64, GPU) for
-        mapping the gradients back."""
+        device).  Builds the units' PTMs (F = C (A (x) B) for two-qubit
+        units, the chain product for one-qubit ones) and their inverses in
+        FP64 on the host, and stores them in FP32 on the GPU; keeps the
+        factors (FP64, GPU) for mapping the gradients back."""
         flat = [p.detach().to('cpu', torch.float64).reshape(
                     (4, 4) if p.numel() == 16 else (16, 16))
                 for ps in ptms_per_instance for p in ps]
@@ -451,18 +534,17 @@ class BatchedSimulator:
                                                               len(flat)))
         dev = self.device
         eye4 = torch.eye(4, dtype=torch.float64)
-        one = torch.stack([flat[j] for j in self._one_op.tolist()]) \
-            if len(self._one_op) else torch.zeros(0, 4, 4,
-                                                  dtype=torch.float64)
-        two = self._two_np
-        if len(two):
-            c = torch.stack([flat[j] for j in two[:, 0]])
-            ra = torch.stack([flat[j] if j >= 0 else eye4 for j in two[:, 1]])
-            rb = torch.stack([flat[j] if j >= 0 else eye4 for j in two[:, 2]])
-            kr = torch.einsum('uac,ubd->uabcd', ra, rb).reshape(-1, 16, 16)
+        one_q = torch.stack([f if f.shape == (4, 4) else eye4 for f in flat])
+        prod, e_op, e_ch, lt, rt = chain_products(one_q, self._chains)
+        n1, n2 = self._n_one, self._n_two
+        one = prod[:n1]
+        a, b = prod[n1:n1 + n2], prod[n1 + n2:]
+        if n2:
+            c = torch.stack([flat[j] for j in self._two_c_np])
+            kr = torch.einsum('uac,ubd->uabcd', a, b).reshape(-1, 16, 16)
             f = torch.bmm(c, kr)
         else:
-            c = ra = rb = kr = f = torch.zeros(0, 16, 16, dtype=torch.float64)
+            c = f = torch.zeros(0, 16, 16, dtype=torch.float64)
         for slots, m, K in ((self._one_slot, one, 4), (self._two_slot, f, 16)):
             if not len(slots):
                 continue
@@ -475,31 +557,21 @@ class BatchedSimulator:
             ipool[:, :K * K] = inv.reshape(len(slots), -1)
             self.ptm[slots] = pool.to(dev).float()
             self.ptm_inv[slots] = ipool.to(dev).float()
-        self._factors = tuple(t.to(dev) for t in (c, ra, rb, kr))
+        self._factors = tuple(t.to(dev) for t in (c, a, b, e_op, e_ch, lt,
+                                                   rt))
 
     def _map_gradients(self):
         """dL/dP of every original op from the units' dL/dF (device, on the
-        current stream): one-qubit units copy; for F = C K with
-        K = R_a (x) R_b, dL/dC = G K^T and, with H = C^T G viewed as
-        [a', b', a, b], dL/dR_a = sum H R_b[b', b], dL/dR_b = sum H R_a[a', a]."""
-        og = self.op_grad
-        if len(self._one_slot):
-            og[self._one_op] = self.grad[self._one_slot]
-        if len(self._two_slot):
-            c, ra, rb, kr = self._factors
-            g = self.grad[self._two_slot].view(-1, 16, 16)
-            og[self._two_c] = torch.bmm(g, kr.transpose(1, 2)).reshape(-1, 256)
-            h = torch.bmm(c.transpose(1, 2), g).view(-1, 4, 4, 4, 4)
-            for side in (0, 1):
-                sel = self._two_r_sel[side]
-                if not len(sel):
-                    continue
-                hs = h[sel]
-                if side == 0:
-                    d = torch.einsum('uxyzw,uyw->uxz', hs, rb[sel])
-                else:
-                    d = torch.einsum('uxyzw,uxz->uyw', hs, ra[sel])
-                og[self._two_r[side], :16] = d.reshape(-1, 16)
+        current stream), by `map_unit_gradients`."""
+        c, a, b, e_op, e_ch, lt, rt = self._factors
+        g_one = self.grad[self._one_slot, :16].view(-1, 4, 4)
+        g_two = self.grad[self._two_slot].view(-1, 16, 16)
+        dc, (ops, d) = map_unit_gradients(g_one, g_two, c, a, b,
+                                          (e_op, e_ch, lt, rt))
+        if dc is not None:
+            self.op_grad[self._two_c] = dc.reshape(-1, 256)
+        if len(ops):
+            self.op_grad[ops, :16] = d.reshape(-1, 16)
 
     # ------------------------------------------------------------ run
     def _launch(self, grid):
@@ -748,9 +820,10 @@ def benchmark(n_instances=512, depth=30, q_min=4, q_max=12, seed=0,
         'tile': sim.tile, 'autotune_ms': tuned,
         'stages': sim.n_stages, 'items': sim.n_items,
         'ops': sim.n_ops, 'units': sim.n_ptm,
-        'fusion': 'each CZ absorbs the rotations before it on its qubits '
-                  '(F = C (R_a x R_b)); per-op gradients mapped back in the '
-                  'same graph',
+        'fusion': 'each CZ absorbs the rotations waiting on its qubits, '
+                  'across layers (F = C (A x B), A and B rotation '
+                  'products); per-op gradients mapped back in the same '
+                  'graph',
         'program_build_s': build_s,
         'launches_per_step': 1, 'cuda_graph': True,
         'graph_contents': 'the persistent batch kernel, then batched-GEMM '

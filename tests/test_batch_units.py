@@ -1,7 +1,8 @@
 """Host-side planning of the batched kernel's units (no GPU): a two-qubit op
-absorbs the one-qubit ops pending on its qubits within a layer.  Applying
-the units' PTMs F = C (R_a (x) R_b) with the oracle reproduces the ops
-applied one by one."""
+absorbs the one-qubit ops waiting on its qubits (across layers).  Applying
+the units' PTMs F = C (A (x) B) with the oracle reproduces the ops applied
+one by one, and the gradient mapping through the chains A and B matches
+autograd."""
 import numpy as np
 import pytest
 import torch
@@ -17,6 +18,32 @@ def _apply_ops(x, ops, mats):
     return x
 
 
+def _chain(mats, chain):
+    m = np.eye(4)
+    for j in chain:
+        m = mats[j] @ m
+    return m
+
+
+def _unit_matrix(qs, mem, mats):
+    if len(qs) == 1:
+        return _chain(mats, mem[0])
+    return mats[mem[0]] @ np.kron(_chain(mats, mem[1]), _chain(mats, mem[2]))
+
+
+def _check_units(ops, mats, units, x, tol):
+    used = sorted(j for _, _, mem in units for j in BT.unit_ops(mem))
+    assert used == list(range(len(ops)))
+    layers = [l for l, _, _ in units]
+    assert layers == sorted(layers)
+    unit_ops = [(l, qs) for l, qs, _ in units]
+    unit_mats = [_unit_matrix(qs, mem, mats) for _, qs, mem in units]
+    for _, qs, _ in units:
+        assert len(qs) == 1 or qs[0] < qs[1]
+    np.testing.assert_allclose(_apply_ops(x, unit_ops, unit_mats),
+                               _apply_ops(x, ops, mats), rtol=tol, atol=tol)
+
+
 @pytest.mark.parametrize('n,depth,seed', [(5, 4, 0), (6, 3, 1), (4, 5, 2),
                                           (1, 2, 3), (2, 3, 4)])
 def test_units_reproduce_ops(n, depth, seed):
@@ -28,39 +55,30 @@ def test_units_reproduce_ops(n, depth, seed):
     mats = [m if m.shape == (4, 4) else rng.standard_normal((16, 16))
             for m in mats]
     units = BT.plan_units(ops)
-    # every op exactly once; layers contiguous and in order
-    used = sorted(j for _, _, mem in units for j in mem if j >= 0)
-    assert used == list(range(len(ops)))
-    layers = [l for l, _, _ in units]
-    assert layers == sorted(layers)
-    eye = np.eye(4)
-    unit_ops, unit_mats = [], []
-    for l, qs, mem in units:
-        if len(qs) == 1:
-            unit_ops.append((l, qs))
-            unit_mats.append(mats[mem[0]])
-        else:
-            assert qs[0] < qs[1]
-            ra = mats[mem[1]] if mem[1] >= 0 else eye
-            rb = mats[mem[2]] if mem[2] >= 0 else eye
-            unit_ops.append((l, qs))
-            unit_mats.append(mats[mem[0]] @ np.kron(ra, rb))
+    # every op exactly once; unit layers in order; the same map
     x = rng.standard_normal((4,) * n)
-    np.testing.assert_allclose(_apply_ops(x, unit_ops, unit_mats),
-                               _apply_ops(x, ops, mats), rtol=1e-12,
-                               atol=1e-12)
+    _check_units(ops, mats, units, x, 1e-12)
+    # one-qubit units remain only for qubits with no later two-qubit op
+    ones = [qs[0] for _, qs, _ in units if len(qs) == 1]
+    assert len(ones) == len(set(ones))
     # unfused planning keeps one unit per op
-    assert [mem[0] for _, _, mem in BT.plan_units(ops, fuse=False)] == \
-        list(range(len(ops)))
+    plain = BT.plan_units(ops, fuse=False)
+    assert [BT.unit_ops(mem) for _, _, mem in plain] == \
+        [[j] for j in range(len(ops))]
+    _check_units(ops, mats, plain, x, 1e-12)
 
 
 def test_units_fuse_most_one_qubit_ops():
-    """The line-matching circuits pair every qubit but one or two per layer:
-    about a third of the ops remain as units."""
+    """The line-matching circuits leave one or two qubits unpaired per
+    layer; their rotations wait for the next two-qubit op on the qubit, so
+    the units are the two-qubit ops plus at most one unit per qubit at the
+    end."""
     spec = BT.CircuitSpec(12, 30, 0)
     ops = spec.ops()
     units = BT.plan_units(ops)
-    assert len(units) < 0.45 * len(ops)
+    n_two = sum(1 for _, qs in ops if len(qs) == 2)
+    assert n_two <= len(units) <= n_two + spec.n
+    assert len(units) < 0.4 * len(ops)
 
 
 def test_gradient_mapping_matches_autograd():
@@ -85,6 +103,52 @@ def test_gradient_mapping_matches_autograd():
                                rb.grad, rtol=1e-12, atol=1e-11)
 
 
+def test_chain_gradient_mapping_matches_autograd():
+    """map_unit_gradients through chains of one-qubit ops (lengths 0 to 3
+    on either side of a two-qubit op, and a one-qubit unit of three ops),
+    against torch autograd in float64."""
+    rng = np.random.default_rng(10)
+    ops1 = [torch.tensor(rng.standard_normal((4, 4)), requires_grad=True)
+            for _ in range(9)]
+    cs = [torch.tensor(rng.standard_normal((16, 16)), requires_grad=True)
+          for _ in range(3)]
+    # one-qubit unit: ops 0, 1, 2; two-qubit units: (A: (), B: (3,)),
+    # (A: (4, 5), B: ()), (A: (6,), B: (7, 8))
+    one_chains = [(0, 1, 2)]
+    a_chains, b_chains = [(), (4, 5), (6,)], [(3,), (), (7, 8)]
+
+    def prod(ch):
+        m = torch.eye(4, dtype=torch.float64)
+        for j in ch:
+            m = ops1[j] @ m
+        return m
+    f_one = [prod(ch) for ch in one_chains]
+    f_two = [c @ torch.kron(prod(a), prod(b))
+             for c, a, b in zip(cs, a_chains, b_chains)]
+    w1 = [torch.tensor(rng.standard_normal((4, 4))) for _ in f_one]
+    w2 = [torch.tensor(rng.standard_normal((16, 16))) for _ in f_two]
+    loss = sum((w * f).sum() + (f ** 3).sum() for w, f in zip(w1, f_one)) + \
+        sum((w * f).sum() + (f ** 2).sum() for w, f in zip(w2, f_two))
+    loss.backward()
+    g_one = torch.stack([(w + 3 * f ** 2).detach()
+                         for w, f in zip(w1, f_one)])
+    g_two = torch.stack([(w + 2 * f).detach() for w, f in zip(w2, f_two)])
+    mats = torch.stack([o.detach() for o in ops1])
+    prods, e_op, e_ch, lt, rt = BT.chain_products(
+        mats, one_chains + a_chains + b_chains)
+    a = prods[1:4]
+    b = prods[4:7]
+    c = torch.stack([x.detach() for x in cs])
+    dc, (eo, d) = BT.map_unit_gradients(g_one, g_two, c, a, b,
+                                        (e_op, e_ch, lt, rt))
+    for k in range(3):
+        np.testing.assert_allclose(dc[k], cs[k].grad, rtol=1e-12,
+                                   atol=1e-10)
+    assert sorted(eo.tolist()) == list(range(9))
+    for j, dj in zip(eo.tolist(), d):
+        np.testing.assert_allclose(dj, ops1[j].grad, rtol=1e-11, atol=1e-9)
+
+
 @pytest.mark.parametrize('seed', range(6))
 def test_units_reproduce_random_op_sequences(seed):
     """Random layers of one- and two-qubit ops in any order: rotations after
@@ -103,22 +167,8 @@ def test_units_reproduce_random_op_sequences(seed):
                 ops.append((layer, (a, b)))
                 mats.append(rng.standard_normal((16, 16)))
     units = BT.plan_units(ops)
-    used = sorted(j for _, _, mem in units for j in mem if j >= 0)
-    assert used == list(range(len(ops)))
-    eye = np.eye(4)
-    unit_ops, unit_mats = [], []
-    for l, qs, mem in units:
-        unit_ops.append((l, qs))
-        if len(qs) == 1:
-            unit_mats.append(mats[mem[0]])
-        else:
-            ra = mats[mem[1]] if mem[1] >= 0 else eye
-            rb = mats[mem[2]] if mem[2] >= 0 else eye
-            unit_mats.append(mats[mem[0]] @ np.kron(ra, rb))
     x = rng.standard_normal((4,) * n)
-    np.testing.assert_allclose(_apply_ops(x, unit_ops, unit_mats),
-                               _apply_ops(x, ops, mats), rtol=1e-11,
-                               atol=1e-11)
+    _check_units(ops, mats, units, x, 1e-11)
 
 
 @pytest.mark.parametrize('ops,msg', [
@@ -198,6 +248,17 @@ def test_program_invariants(fuse, tile):
         n_ckpt = max(0, (specs[i].depth - 1) // every)
         assert ops.count(BT.BOP_SAVE) == n_ckpt
         assert ops.count(BT.BOP_RESTORE) == n_ckpt
+        # checkpoint k is saved and restored at the same unit boundary:
+        # after the same number of APPLYs as ADJOINTs remain after it
+        for k in range(n_ckpt):
+            ks = [t for t, (o, p) in enumerate(seq)
+                  if o == BT.BOP_SAVE and p == k]
+            kr = [t for t, (o, p) in enumerate(seq)
+                  if o == BT.BOP_RESTORE and p == k]
+            assert len(ks) == len(kr) == 1
+            applied = sum(1 for o, _ in seq[:ks[0]] if o == BT.BOP_APPLY)
+            left = sum(1 for o, _ in seq[kr[0]:] if o == BT.BOP_ADJOINT)
+            assert applied == left
     adj = items[items['op'] == BT.BOP_ADJOINT]
     assert sorted(adj['slot']) == list(range(n_slots))
     for g in last:

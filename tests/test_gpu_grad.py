@@ -164,7 +164,8 @@ def test_graphed_gradient_step_matches_reference():
             p = {k: v.detach().clone().to(dev).requires_grad_(True)
                  for k, v in point.items()}
             loss = step.step(p)
-            grads.append((float(loss), _flat([p[k].grad for k in names])))
+            grads.append((float(loss.detach()),
+                          _flat([p[k].grad for k in names])))
         assert grads[0][0] == grads[1][0]
         assert torch.equal(grads[0][1], grads[1][1])
         pr = {k: v.detach().clone().requires_grad_(True)
