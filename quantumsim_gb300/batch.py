@@ -155,71 +155,90 @@ def validate_ops(ops, n, depth, what='circuit'):
         prev = layer
 
 
+# two-qubit ops one unit may hold (consecutive CZs on one pair, with the
+# rotations between them): bounds the products behind a unit's PTM and its
+# inverse
+MAX_FACTORS = 4
+
+
 def plan_units(ops, fuse=True):
     """Group a circuit's ops into the units the kernel applies.
 
     ops: [(layer, qubits)] in application order.  With `fuse`, a one-qubit
     op waits on its qubit (across layers, past ops on other qubits, which
-    it commutes with) until the next two-qubit op on that qubit absorbs it.
-    That unit's PTM is F = C (A (x) B), with A and B the products of the
-    one-qubit ops waiting on its two qubits (identity where none): a dense
+    it commutes with) until the next two-qubit op on that qubit absorbs it:
+    a factor M = C (A (x) B), with A and B the products of the one-qubit ops
+    waiting on its two qubits (identity where none).  A two-qubit op whose
+    two qubits were last touched by the same unit (the previous op on both
+    is a two-qubit op on the same pair) joins that unit as its next factor,
+    up to MAX_FACTORS; the unit's PTM is the product M_k ... M_1, a dense
     16 x 16 PTM like any two-qubit PTM of the kernel, so the unit costs one
     pass where its ops cost several.  The one-qubit ops that meet no later
-    two-qubit op become one-qubit units (their product) at the end.  Without
-    `fuse` every op is a unit of its own.
+    two-qubit op become one-qubit units (their product) at the end.
+    Without `fuse` every op is a unit of its own.
 
-    A unit's layer is its two-qubit op's layer (for the one-qubit units at
-    the end, the last op's layer), so the layers of the units never
-    decrease; checkpoints sit at unit boundaries (`build_program`).
+    A unit's layer is its first two-qubit op's layer (for the one-qubit
+    units at the end, the last op's layer), so the layers of the units
+    never decrease; checkpoints sit at unit boundaries (`build_program`).
 
     Returns [(layer, qubits, members)]: members = (chain,) for a one-qubit
-    unit (qubits = (q,)), (j_c, chain_a, chain_b) for a two-qubit unit
-    (qubits = (a, b) sorted); a chain is the tuple of one-qubit op indices
-    in application order (empty: the identity)."""
+    unit (qubits = (q,)); for a two-qubit unit (qubits = (a, b) sorted) a
+    tuple of factors (j_c, chain_a, chain_b) in application order.  A chain
+    is the tuple of one-qubit op indices in application order (empty: the
+    identity)."""
     units = []
     if not fuse:
         for j, (l, qs) in enumerate(ops):
             if len(qs) == 1:
                 units.append((l, (qs[0],), ((j,),)))
             else:
-                units.append((l, (min(qs), max(qs)), (j, (), ())))
+                units.append((l, (min(qs), max(qs)), ((j, (), ()),)))
         return units
     pending = {}
+    last = {}  # qubit -> index of the last unit on it
     for j, (l, qs) in enumerate(ops):
         if len(qs) == 1:
             pending.setdefault(qs[0], []).append(j)
-        else:
-            a, b = min(qs), max(qs)
-            units.append((l, (a, b), (j, tuple(pending.pop(a, ())),
-                                      tuple(pending.pop(b, ())))))
+            continue
+        a, b = min(qs), max(qs)
+        factor = (j, tuple(pending.pop(a, ())), tuple(pending.pop(b, ())))
+        k = last.get(a)
+        if k is not None and last.get(b) == k and \
+                len(units[k][2]) < MAX_FACTORS:
+            lk, qk, mem = units[k]
+            units[k] = (lk, qk, mem + (factor,))
+            continue
+        units.append((l, (a, b), (factor,)))
+        last[a] = last[b] = len(units) - 1
     if pending:
-        last = ops[-1][0]
+        lay = ops[-1][0]
         for q, chain in sorted(pending.items(), key=lambda t: t[1][0]):
-            units.append((last, (q,), (tuple(chain),)))
+            units.append((lay, (q,), (tuple(chain),)))
     return units
 
 
-def unit_ops(members):
+def unit_ops(qubits, members):
     """Every op index of a unit's members."""
-    if len(members) == 1:
+    if len(qubits) == 1:
         return list(members[0])
-    return [members[0]] + list(members[1]) + list(members[2])
+    return [o for jc, ca, cb in members for o in (jc,) + ca + cb]
 
 
 def chain_products(mats, chains):
-    """Products of one-qubit PTM chains and the factors of their gradients.
+    """Products of matrix chains and the factors of their gradients.
 
-    mats: (n_ops, 4, 4) float64 tensor (any op's row; only chain members are
-    read); chains: tuples of op indices in application order.  For a chain
+    mats: (n, d, d) float64 tensor (only chain members are read); chains:
+    tuples of indices into mats in application order.  For a chain
     r_0 .. r_{m-1}, prod = r_{m-1} ... r_0 (the identity for an empty
     chain), and for its element i, dL/dr_i = L_i^T (dL/dprod) R_i^T with
     L_i = r_{m-1} ... r_{i+1} and R_i = r_{i-1} ... r_0.
 
-    Returns (prod (n_chains, 4, 4), elem_op, elem_chain, left_t, right_t):
-    one entry per chain element, left_t = L_i^T and right_t = R_i^T."""
-    n = len(chains)
+    Returns (prod (n_chains, d, d), elem, elem_chain, left_t, right_t): one
+    entry per chain element (its index into mats, its chain), with
+    left_t = L_i^T and right_t = R_i^T."""
+    n, d = len(chains), mats.shape[-1]
     dt, dev = mats.dtype, mats.device
-    prod = torch.eye(4, dtype=dt, device=dev).repeat(n, 1, 1)
+    prod = torch.eye(d, dtype=dt, device=dev).repeat(n, 1, 1)
     e_op, e_ch, lt, rt = [], [], [], []
     by_len = {}
     for c, ch in enumerate(chains):
@@ -228,48 +247,60 @@ def chain_products(mats, chains):
     for m, cs in sorted(by_len.items()):
         idx = torch.as_tensor([chains[c] for c in cs], dtype=torch.long,
                               device=dev)
-        r = mats[idx]                                   # (k, m, 4, 4)
-        eye = torch.eye(4, dtype=dt, device=dev).expand(len(cs), 4, 4)
+        r = mats[idx]                                   # (k, m, d, d)
+        eye = torch.eye(d, dtype=dt, device=dev).expand(len(cs), d, d)
         pre = [eye]                                     # r_{i-1} ... r_0
         for i in range(1, m):
             pre.append(torch.bmm(r[:, i - 1], pre[-1]))
         suf = [eye] * m                                 # r_{m-1} ... r_{i+1}
         for i in range(m - 2, -1, -1):
             suf[i] = torch.bmm(suf[i + 1], r[:, i + 1])
-        prod[torch.as_tensor(cs, device=dev)] = torch.bmm(r[:, m - 1],
-                                                          pre[m - 1])
+        cs_t = torch.as_tensor(cs, dtype=torch.long, device=dev)
+        prod[cs_t] = torch.bmm(r[:, m - 1], pre[m - 1])
         for i in range(m):
             e_op.append(idx[:, i])
-            e_ch.append(torch.as_tensor(cs, dtype=torch.long, device=dev))
+            e_ch.append(cs_t)
             lt.append(suf[i].transpose(1, 2))
             rt.append(pre[i].transpose(1, 2))
     if not e_op:
         z = torch.zeros(0, dtype=torch.long, device=dev)
-        zz = torch.zeros(0, 4, 4, dtype=dt, device=dev)
+        zz = torch.zeros(0, d, d, dtype=dt, device=dev)
         return prod, z, z, zz, zz
     return (prod, torch.cat(e_op), torch.cat(e_ch), torch.cat(lt),
             torch.cat(rt))
 
 
-def map_unit_gradients(g_one, g_two, c, a, b, chain_factors):
-    """dL/dP of the original ops from the units' gradients (any device):
-    g_one (n1, 4, 4) of the one-qubit units, g_two (n2, 16, 16) of the
-    two-qubit units F = C K with K = A (x) B (c, a, b their factors), and
-    chain_factors = (elem_op, elem_chain, left_t, right_t) of the chains
-    ordered one-qubit units, then side a, then side b of the two-qubit
-    units (`chain_products`).  Returns (dL/dC (n2, 16, 16), [(op indices,
-    dL/dr (k, 4, 4))] for the chain elements).
+def map_unit_gradients(g_one, g_two, c, a, b, chain_factors,
+                       factor_chains=None):
+    """dL/dP of the original ops from the units' gradients (any device).
 
+    g_one (n1, 4, 4): the one-qubit units' gradients.  g_two: the two-qubit
+    units' gradients (n_units, 16, 16); each unit is the product of factors
+    M = C K, K = A (x) B, whose C, A and B are c, a, b (n_factors, ...);
+    factor_chains = (elem_factor, elem_unit, left_t, right_t) of the units'
+    factor chains (`chain_products` over the factors' M; None when every
+    unit has one factor, listed in unit order).  chain_factors =
+    (elem_op, elem_chain, left_t, right_t) of the one-qubit chains, ordered
+    one-qubit units, then side a, then side b of the factors.
+
+    Returns (dL/dC (n_factors, 16, 16), (op indices, dL/dr (k, 4, 4)) for
+    the one-qubit chain elements).  Per factor, with G its dL/dM:
     dL/dC = G K^T; with H = C^T G viewed as [a', b', a, b],
     dL/dA = sum H B[b', b] and dL/dB = sum H A[a', a]; each chain element
-    then gets L^T (dL/dprod) R^T."""
+    gets L^T (dL/dprod) R^T."""
     e_op, e_ch, lt, rt = chain_factors
     parts = [g_one]
     dc = None
-    if len(g_two):
+    if len(c):
+        if factor_chains is None:
+            gm = g_two
+        else:
+            f_idx, f_unit, flt, frt = factor_chains
+            gm = torch.empty_like(c)
+            gm[f_idx] = torch.bmm(torch.bmm(flt, g_two[f_unit]), frt)
         kr = torch.einsum('uac,ubd->uabcd', a, b).reshape(-1, 16, 16)
-        dc = torch.bmm(g_two, kr.transpose(1, 2))
-        h = torch.bmm(c.transpose(1, 2), g_two).view(-1, 4, 4, 4, 4)
+        dc = torch.bmm(gm, kr.transpose(1, 2))
+        h = torch.bmm(c.transpose(1, 2), gm).view(-1, 4, 4, 4, 4)
         parts += [torch.einsum('uxyzw,uyw->uxz', h, b),
                   torch.einsum('uxyzw,uxz->uyw', h, a)]
     gch = torch.cat(parts)
@@ -432,6 +463,7 @@ class BatchedSimulator:
         self.op_grad = torch.zeros(self.n_ops, 256, dtype=torch.float64,
                                    device=dev)
         self._factors = None
+        self._fchain = None
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.max_grid = self.lib.qsgb_batch_max_grid(BLOCK)
         if self.max_grid < 1:
@@ -493,39 +525,47 @@ class BatchedSimulator:
 
     def _index_units(self):
         """Flat index arrays of the units: slot and chain of every one-qubit
-        unit; slot, C op and the two chains of every two-qubit unit.  The
-        chains are listed one-qubit units first, then side a, then side b
-        of the two-qubit units (`chain_products`, `map_unit_gradients`)."""
+        unit; slot of every two-qubit unit and, per factor, its C op, its
+        two chains and its unit.  The one-qubit chains are listed one-qubit
+        units first, then side a, then side b of the factors
+        (`chain_products`, `map_unit_gradients`)."""
         one_slot, one_chain = [], []
-        two_slot, two_c, two_a, two_b = [], [], [], []
+        two_slot, f_c, f_a, f_b, f_seq = [], [], [], [], []
         for i, units in enumerate(self.units):
             ub, ob = int(self.unit_base[i]), int(self.op_base[i])
             for u, (_, qs, mem) in enumerate(units):
                 if len(qs) == 1:
                     one_slot.append(ub + u)
                     one_chain.append(tuple(ob + m for m in mem[0]))
-                else:
-                    two_slot.append(ub + u)
-                    two_c.append(ob + mem[0])
-                    two_a.append(tuple(ob + m for m in mem[1]))
-                    two_b.append(tuple(ob + m for m in mem[2]))
+                    continue
+                seq = []
+                for jc, ca, cb in mem:
+                    seq.append(len(f_c))
+                    f_c.append(ob + jc)
+                    f_a.append(tuple(ob + m for m in ca))
+                    f_b.append(tuple(ob + m for m in cb))
+                two_slot.append(ub + u)
+                f_seq.append(tuple(seq))
         dev = self.device
         as_idx = (lambda v: torch.as_tensor(np.asarray(v, dtype=np.int64),
                                             device=dev))
         self._one_slot = as_idx(one_slot)
-        self._two_slot, self._two_c = as_idx(two_slot), as_idx(two_c)
-        self._two_c_np = np.asarray(two_c, dtype=np.int64)
-        self._chains = one_chain + two_a + two_b
-        self._n_one, self._n_two = len(one_slot), len(two_slot)
+        self._two_slot, self._f_c = as_idx(two_slot), as_idx(f_c)
+        self._f_c_np = np.asarray(f_c, dtype=np.int64)
+        self._chains = one_chain + f_a + f_b
+        self._f_seq = f_seq
+        self._single = all(len(q) == 1 for q in f_seq)
+        self._n_one, self._n_fac = len(one_slot), len(f_c)
 
     # ------------------------------------------------------------ PTMs
     def set_ptms(self, ptms_per_instance):
         """ptms_per_instance[i][j]: (K, K) float64 PTM of op j of instance i
         (two-qubit ones (16, 16) or (4, 4, 4, 4) in sorted qubit order; any
-        device).  Builds the units' PTMs (F = C (A (x) B) for two-qubit
-        units, the chain product for one-qubit ones) and their inverses in
-        FP64 on the host, and stores them in FP32 on the GPU; keeps the
-        factors (FP64, GPU) for mapping the gradients back."""
+        device).  Builds the units' PTMs (the product of the factors
+        C (A (x) B) for two-qubit units, the chain product for one-qubit
+        ones) and their inverses in FP64 on the host, and stores them in
+        FP32 on the GPU; keeps the factors (FP64, GPU) for mapping the
+        gradients back."""
         flat = [p.detach().to('cpu', torch.float64).reshape(
                     (4, 4) if p.numel() == 16 else (16, 16))
                 for ps in ptms_per_instance for p in ps]
@@ -536,29 +576,36 @@ class BatchedSimulator:
         eye4 = torch.eye(4, dtype=torch.float64)
         one_q = torch.stack([f if f.shape == (4, 4) else eye4 for f in flat])
         prod, e_op, e_ch, lt, rt = chain_products(one_q, self._chains)
-        n1, n2 = self._n_one, self._n_two
+        n1, nf = self._n_one, self._n_fac
         one = prod[:n1]
-        a, b = prod[n1:n1 + n2], prod[n1 + n2:]
-        if n2:
-            c = torch.stack([flat[j] for j in self._two_c_np])
+        a, b = prod[n1:n1 + nf], prod[n1 + nf:]
+        fchain = None
+        if nf:
+            c = torch.stack([flat[j] for j in self._f_c_np])
             kr = torch.einsum('uac,ubd->uabcd', a, b).reshape(-1, 16, 16)
-            f = torch.bmm(c, kr)
+            m = torch.bmm(c, kr)
+            if self._single:
+                f = m
+            else:
+                f, f_idx, f_unit, flt, frt = chain_products(m, self._f_seq)
+                fchain = tuple(t.to(dev) for t in (f_idx, f_unit, flt, frt))
         else:
             c = f = torch.zeros(0, 16, 16, dtype=torch.float64)
-        for slots, m, K in ((self._one_slot, one, 4), (self._two_slot, f, 16)):
+        for slots, mm, K in ((self._one_slot, one, 4), (self._two_slot, f, 16)):
             if not len(slots):
                 continue
             # inverted on the host in float64: the matrices are tiny, and
             # this keeps the device free of the solver libraries
-            inv = torch.linalg.inv(m)
+            inv = torch.linalg.inv(mm)
             pool = torch.zeros(len(slots), 256, dtype=torch.float64)
             ipool = torch.zeros_like(pool)
-            pool[:, :K * K] = m.reshape(len(slots), -1)
+            pool[:, :K * K] = mm.reshape(len(slots), -1)
             ipool[:, :K * K] = inv.reshape(len(slots), -1)
             self.ptm[slots] = pool.to(dev).float()
             self.ptm_inv[slots] = ipool.to(dev).float()
         self._factors = tuple(t.to(dev) for t in (c, a, b, e_op, e_ch, lt,
                                                    rt))
+        self._fchain = fchain
 
     def _map_gradients(self):
         """dL/dP of every original op from the units' dL/dF (device, on the
@@ -567,9 +614,9 @@ class BatchedSimulator:
         g_one = self.grad[self._one_slot, :16].view(-1, 4, 4)
         g_two = self.grad[self._two_slot].view(-1, 16, 16)
         dc, (ops, d) = map_unit_gradients(g_one, g_two, c, a, b,
-                                          (e_op, e_ch, lt, rt))
+                                          (e_op, e_ch, lt, rt), self._fchain)
         if dc is not None:
-            self.op_grad[self._two_c] = dc.reshape(-1, 256)
+            self.op_grad[self._f_c] = dc.reshape(-1, 256)
         if len(ops):
             self.op_grad[ops, :16] = d.reshape(-1, 16)
 

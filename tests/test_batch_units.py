@@ -28,11 +28,14 @@ def _chain(mats, chain):
 def _unit_matrix(qs, mem, mats):
     if len(qs) == 1:
         return _chain(mats, mem[0])
-    return mats[mem[0]] @ np.kron(_chain(mats, mem[1]), _chain(mats, mem[2]))
+    m = np.eye(16)
+    for jc, ca, cb in mem:
+        m = mats[jc] @ np.kron(_chain(mats, ca), _chain(mats, cb)) @ m
+    return m
 
 
 def _check_units(ops, mats, units, x, tol):
-    used = sorted(j for _, _, mem in units for j in BT.unit_ops(mem))
+    used = sorted(j for _, qs, mem in units for j in BT.unit_ops(qs, mem))
     assert used == list(range(len(ops)))
     layers = [l for l, _, _ in units]
     assert layers == sorted(layers)
@@ -63,7 +66,7 @@ def test_units_reproduce_ops(n, depth, seed):
     assert len(ones) == len(set(ones))
     # unfused planning keeps one unit per op
     plain = BT.plan_units(ops, fuse=False)
-    assert [BT.unit_ops(mem) for _, _, mem in plain] == \
+    assert [BT.unit_ops(qs, mem) for _, qs, mem in plain] == \
         [[j] for j in range(len(ops))]
     _check_units(ops, mats, plain, x, 1e-12)
 
@@ -77,8 +80,14 @@ def test_units_fuse_most_one_qubit_ops():
     ops = spec.ops()
     units = BT.plan_units(ops)
     n_two = sum(1 for _, qs in ops if len(qs) == 2)
-    assert n_two <= len(units) <= n_two + spec.n
+    assert len([u for u in units if len(u[1]) == 1]) <= spec.n
+    assert sum(len(mem) for _, qs, mem in units if len(qs) == 2) == n_two
     assert len(units) < 0.4 * len(ops)
+    # odd qubit counts draw the matching's offset per layer: consecutive
+    # layers on the same pairs share units, at most MAX_FACTORS CZs each
+    odd = BT.plan_units(BT.CircuitSpec(11, 30, 3).ops())
+    sizes = [len(mem) for _, qs, mem in odd if len(qs) == 2]
+    assert max(sizes) > 1 and max(sizes) <= BT.MAX_FACTORS
 
 
 def test_gradient_mapping_matches_autograd():
@@ -265,3 +274,55 @@ def test_program_invariants(fuse, tile):
         mine = adj[adj['ptm'] == g['ptm']]
         assert sorted(mine['slot']) == list(range(g['beg'], g['end']))
     assert sorted(last['ptm']) == list(range(int(ubase[-1])))
+
+
+def test_factor_chain_gradient_mapping_matches_autograd():
+    """Units of several factors M = C (A (x) B) (as consecutive CZs on one
+    pair with rotations between them form): map_unit_gradients through the
+    factor chains and the rotation chains, against torch autograd."""
+    rng = np.random.default_rng(11)
+    r = [torch.tensor(rng.standard_normal((4, 4)), requires_grad=True)
+         for _ in range(6)]
+    cs = [torch.tensor(rng.standard_normal((16, 16)), requires_grad=True)
+          for _ in range(5)]
+    # unit 0: factors (C0, A: (0,), B: ()), (C1, A: (1, 2), B: (3,)),
+    #         (C2, (), ()); unit 1: (C3, (4,), ()), (C4, (), (5,))
+    facs = [(0, (0,), ()), (1, (1, 2), (3,)), (2, (), ()), (3, (4,), ()),
+            (4, (), (5,))]
+    seqs = [(0, 1, 2), (3, 4)]
+
+    def chain(ch):
+        m = torch.eye(4, dtype=torch.float64)
+        for j in ch:
+            m = r[j] @ m
+        return m
+    ms = [cs[jc] @ torch.kron(chain(ca), chain(cb)) for jc, ca, cb in facs]
+    units = []
+    for sq in seqs:
+        u = torch.eye(16, dtype=torch.float64)
+        for f in sq:
+            u = ms[f] @ u
+        units.append(u)
+    w = [torch.tensor(rng.standard_normal((16, 16))) for _ in units]
+    loss = sum((wi * u).sum() + (u ** 2).sum() for wi, u in zip(w, units))
+    loss.backward()
+    g_two = torch.stack([(wi + 2 * u).detach() for wi, u in zip(w, units)])
+    mats = torch.stack([x.detach() for x in r])
+    prods, e_op, e_ch, lt, rt = BT.chain_products(
+        mats, [f[1] for f in facs] + [f[2] for f in facs])
+    a, b = prods[:5], prods[5:]
+    c = torch.stack([cs[f[0]].detach() for f in facs])
+    m = torch.bmm(c, torch.einsum('uac,ubd->uabcd', a, b).reshape(-1, 16, 16))
+    fu, f_idx, f_unit, flt, frt = BT.chain_products(m, seqs)
+    for k in range(2):
+        np.testing.assert_allclose(fu[k], units[k].detach(), rtol=1e-12,
+                                   atol=1e-12)
+    g_one = torch.zeros(0, 4, 4, dtype=torch.float64)
+    dc, (eo, d) = BT.map_unit_gradients(g_one, g_two, c, a, b,
+                                        (e_op, e_ch, lt, rt),
+                                        (f_idx, f_unit, flt, frt))
+    for f, (jc, _, _) in enumerate(facs):
+        np.testing.assert_allclose(dc[f], cs[jc].grad, rtol=1e-11, atol=1e-8)
+    assert sorted(eo.tolist()) == list(range(6))
+    for j, dj in zip(eo.tolist(), d):
+        np.testing.assert_allclose(dj, r[j].grad, rtol=1e-11, atol=1e-7)
