@@ -233,16 +233,23 @@ def chain_products(mats, chains):
     chain), and for its element i, dL/dr_i = L_i^T (dL/dprod) R_i^T with
     L_i = r_{m-1} ... r_{i+1} and R_i = r_{i-1} ... r_0.
 
-    Returns (prod (n_chains, d, d), elem, elem_chain, left_t, right_t): one
-    entry per chain element (its index into mats, its chain), with
-    left_t = L_i^T and right_t = R_i^T."""
+    Returns (prod (n_chains, d, d), factors) with factors = (direct_elem,
+    direct_chain, elem, elem_chain, left_t, right_t): the elements of
+    one-element chains (dL/dr = dL/dprod) by index into mats and chain,
+    then the others with left_t = L_i^T and right_t = R_i^T."""
     n, d = len(chains), mats.shape[-1]
     dt, dev = mats.dtype, mats.device
     prod = torch.eye(d, dtype=dt, device=dev).repeat(n, 1, 1)
+    one = [c for c, ch in enumerate(chains) if len(ch) == 1]
+    d_op = torch.as_tensor([chains[c][0] for c in one], dtype=torch.long,
+                           device=dev)
+    d_ch = torch.as_tensor(one, dtype=torch.long, device=dev)
+    if one:
+        prod[d_ch] = mats[d_op]
     e_op, e_ch, lt, rt = [], [], [], []
     by_len = {}
     for c, ch in enumerate(chains):
-        if ch:
+        if len(ch) > 1:
             by_len.setdefault(len(ch), []).append(c)
     for m, cs in sorted(by_len.items()):
         idx = torch.as_tensor([chains[c] for c in cs], dtype=torch.long,
@@ -262,12 +269,27 @@ def chain_products(mats, chains):
             e_ch.append(cs_t)
             lt.append(suf[i].transpose(1, 2))
             rt.append(pre[i].transpose(1, 2))
-    if not e_op:
+    if e_op:
+        rest = (torch.cat(e_op), torch.cat(e_ch), torch.cat(lt),
+                torch.cat(rt))
+    else:
         z = torch.zeros(0, dtype=torch.long, device=dev)
         zz = torch.zeros(0, d, d, dtype=dt, device=dev)
-        return prod, z, z, zz, zz
-    return (prod, torch.cat(e_op), torch.cat(e_ch), torch.cat(lt),
-            torch.cat(rt))
+        rest = (z, z, zz, zz)
+    return prod, (d_op, d_ch) + rest
+
+
+def chain_gradients(g_prod, factors):
+    """(element indices, dL/dr per element) from the chains' dL/dprod
+    `g_prod` (n_chains, d, d) and `factors` from chain_products."""
+    d_op, d_ch, e_op, e_ch, lt, rt = factors
+    if not len(e_op):
+        return d_op, g_prod[d_ch]
+    if not len(d_op):
+        return e_op, torch.bmm(torch.bmm(lt, g_prod[e_ch]), rt)
+    return (torch.cat([d_op, e_op]),
+            torch.cat([g_prod[d_ch], torch.bmm(torch.bmm(lt, g_prod[e_ch]),
+                                               rt)]))
 
 
 def map_unit_gradients(g_one, g_two, c, a, b, chain_factors,
@@ -277,36 +299,32 @@ def map_unit_gradients(g_one, g_two, c, a, b, chain_factors,
     g_one (n1, 4, 4): the one-qubit units' gradients.  g_two: the two-qubit
     units' gradients (n_units, 16, 16); each unit is the product of factors
     M = C K, K = A (x) B, whose C, A and B are c, a, b (n_factors, ...);
-    factor_chains = (elem_factor, elem_unit, left_t, right_t) of the units'
-    factor chains (`chain_products` over the factors' M; None when every
-    unit has one factor, listed in unit order).  chain_factors =
-    (elem_op, elem_chain, left_t, right_t) of the one-qubit chains, ordered
-    one-qubit units, then side a, then side b of the factors.
+    factor_chains: the factors of the units' factor chains
+    (`chain_products` over the factors' M; None when every unit has one
+    factor, listed in unit order).  chain_factors: those of the one-qubit
+    chains, ordered one-qubit units, then side a, then side b of the
+    factors.
 
     Returns (dL/dC (n_factors, 16, 16), (op indices, dL/dr (k, 4, 4)) for
     the one-qubit chain elements).  Per factor, with G its dL/dM:
     dL/dC = G K^T; with H = C^T G viewed as [a', b', a, b],
     dL/dA = sum H B[b', b] and dL/dB = sum H A[a', a]; each chain element
     gets L^T (dL/dprod) R^T."""
-    e_op, e_ch, lt, rt = chain_factors
     parts = [g_one]
     dc = None
     if len(c):
         if factor_chains is None:
             gm = g_two
         else:
-            f_idx, f_unit, flt, frt = factor_chains
+            f_idx, g_f = chain_gradients(g_two, factor_chains)
             gm = torch.empty_like(c)
-            gm[f_idx] = torch.bmm(torch.bmm(flt, g_two[f_unit]), frt)
+            gm[f_idx] = g_f
         kr = torch.einsum('uac,ubd->uabcd', a, b).reshape(-1, 16, 16)
         dc = torch.bmm(gm, kr.transpose(1, 2))
         h = torch.bmm(c.transpose(1, 2), gm).view(-1, 4, 4, 4, 4)
         parts += [torch.einsum('uxyzw,uyw->uxz', h, b),
                   torch.einsum('uxyzw,uxz->uyw', h, a)]
-    gch = torch.cat(parts)
-    d = torch.bmm(torch.bmm(lt, gch[e_ch]), rt) if len(e_op) else \
-        gch[:0]
-    return dc, (e_op, d)
+    return dc, chain_gradients(torch.cat(parts), chain_factors)
 
 
 def build_program(units, unit_base, sizes, depths, every, tile,
@@ -575,7 +593,7 @@ class BatchedSimulator:
         dev = self.device
         eye4 = torch.eye(4, dtype=torch.float64)
         one_q = torch.stack([f if f.shape == (4, 4) else eye4 for f in flat])
-        prod, e_op, e_ch, lt, rt = chain_products(one_q, self._chains)
+        prod, cfac = chain_products(one_q, self._chains)
         n1, nf = self._n_one, self._n_fac
         one = prod[:n1]
         a, b = prod[n1:n1 + nf], prod[n1 + nf:]
@@ -587,8 +605,8 @@ class BatchedSimulator:
             if self._single:
                 f = m
             else:
-                f, f_idx, f_unit, flt, frt = chain_products(m, self._f_seq)
-                fchain = tuple(t.to(dev) for t in (f_idx, f_unit, flt, frt))
+                f, ffac = chain_products(m, self._f_seq)
+                fchain = tuple(t.to(dev) for t in ffac)
         else:
             c = f = torch.zeros(0, 16, 16, dtype=torch.float64)
         for slots, mm, K in ((self._one_slot, one, 4), (self._two_slot, f, 16)):
@@ -603,18 +621,18 @@ class BatchedSimulator:
             ipool[:, :K * K] = inv.reshape(len(slots), -1)
             self.ptm[slots] = pool.to(dev).float()
             self.ptm_inv[slots] = ipool.to(dev).float()
-        self._factors = tuple(t.to(dev) for t in (c, a, b, e_op, e_ch, lt,
-                                                   rt))
+        self._factors = tuple(t.to(dev) for t in (c, a, b))
+        self._cchain = tuple(t.to(dev) for t in cfac)
         self._fchain = fchain
 
     def _map_gradients(self):
         """dL/dP of every original op from the units' dL/dF (device, on the
         current stream), by `map_unit_gradients`."""
-        c, a, b, e_op, e_ch, lt, rt = self._factors
+        c, a, b = self._factors
         g_one = self.grad[self._one_slot, :16].view(-1, 4, 4)
         g_two = self.grad[self._two_slot].view(-1, 16, 16)
         dc, (ops, d) = map_unit_gradients(g_one, g_two, c, a, b,
-                                          (e_op, e_ch, lt, rt), self._fchain)
+                                          self._cchain, self._fchain)
         if dc is not None:
             self.op_grad[self._f_c] = dc.reshape(-1, 256)
         if len(ops):

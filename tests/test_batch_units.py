@@ -143,13 +143,11 @@ def test_chain_gradient_mapping_matches_autograd():
                          for w, f in zip(w1, f_one)])
     g_two = torch.stack([(w + 2 * f).detach() for w, f in zip(w2, f_two)])
     mats = torch.stack([o.detach() for o in ops1])
-    prods, e_op, e_ch, lt, rt = BT.chain_products(
-        mats, one_chains + a_chains + b_chains)
+    prods, cfac = BT.chain_products(mats, one_chains + a_chains + b_chains)
     a = prods[1:4]
     b = prods[4:7]
     c = torch.stack([x.detach() for x in cs])
-    dc, (eo, d) = BT.map_unit_gradients(g_one, g_two, c, a, b,
-                                        (e_op, e_ch, lt, rt))
+    dc, (eo, d) = BT.map_unit_gradients(g_one, g_two, c, a, b, cfac)
     for k in range(3):
         np.testing.assert_allclose(dc[k], cs[k].grad, rtol=1e-12,
                                    atol=1e-10)
@@ -308,19 +306,17 @@ def test_factor_chain_gradient_mapping_matches_autograd():
     loss.backward()
     g_two = torch.stack([(wi + 2 * u).detach() for wi, u in zip(w, units)])
     mats = torch.stack([x.detach() for x in r])
-    prods, e_op, e_ch, lt, rt = BT.chain_products(
+    prods, cfac = BT.chain_products(
         mats, [f[1] for f in facs] + [f[2] for f in facs])
     a, b = prods[:5], prods[5:]
     c = torch.stack([cs[f[0]].detach() for f in facs])
     m = torch.bmm(c, torch.einsum('uac,ubd->uabcd', a, b).reshape(-1, 16, 16))
-    fu, f_idx, f_unit, flt, frt = BT.chain_products(m, seqs)
+    fu, ffac = BT.chain_products(m, seqs)
     for k in range(2):
         np.testing.assert_allclose(fu[k], units[k].detach(), rtol=1e-12,
                                    atol=1e-12)
     g_one = torch.zeros(0, 4, 4, dtype=torch.float64)
-    dc, (eo, d) = BT.map_unit_gradients(g_one, g_two, c, a, b,
-                                        (e_op, e_ch, lt, rt),
-                                        (f_idx, f_unit, flt, frt))
+    dc, (eo, d) = BT.map_unit_gradients(g_one, g_two, c, a, b, cfac, ffac)
     for f, (jc, _, _) in enumerate(facs):
         np.testing.assert_allclose(dc[f], cs[jc].grad, rtol=1e-11, atol=1e-8)
     assert sorted(eo.tolist()) == list(range(6))
