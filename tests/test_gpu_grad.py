@@ -172,7 +172,7 @@ def test_graphed_gradient_step_matches_reference():
               for k, v in point.items()}
         ref = m.loss(pr, target, backend='einsum', fuse=False)
         ref.backward()
-        assert grads[0][0] == pytest.approx(float(ref), rel=1e-10)
+        assert grads[0][0] == pytest.approx(float(ref.detach()), rel=1e-10)
         np.testing.assert_allclose(grads[0][1].cpu(),
                                    _flat([pr[k].grad for k in names]),
                                    rtol=1e-8, atol=1e-12)
