@@ -13,11 +13,14 @@
  * object made once per device index.  The library call runs with the GIL released, as a ctypes call
  * does (a first call of a PTM pattern compiles its kernel).
  *
- * apply(pv, ptm, plan, arith) -> new tensor, or an int: the library's status
- * code when the call did not succeed, or NOT_F64_CONTIGUOUS when `ptm` is not
- * a C-contiguous float64 buffer (the caller converts it and calls again).
- * `plan` is (output shape, two qudits?, sizes, layout flags, dtype code) as
- * built by quantumsim_gb300.ops.eager_plan.
+ * apply(pv, ptm, plan, arith[, out]) -> the output tensor, or an int: the
+ * library's status code when the call did not succeed, or NOT_F64_CONTIGUOUS
+ * when `ptm` is not a C-contiguous float64 buffer (the caller converts it and
+ * calls again).  `plan` is (output shape, two qudits?, sizes, layout flags,
+ * dtype code) as built by quantumsim_gb300.ops.eager_plan.  `out` (optional,
+ * None for a new tensor) is a contiguous tensor of the output shape, dtype
+ * and device that the caller owns and no longer reads, such as the state
+ * buffer two applications back: writing into it saves the allocation.
  */
 #define PY_SSIZE_T_CLEAN
 #include <Python.h>
@@ -83,10 +86,11 @@ static int as_u64(PyObject* o, unsigned long long* v) {
 
 static PyObject* apply(PyObject* self, PyObject* const* args, Py_ssize_t nargs) {
   (void)self;
-  if (nargs != 4) {
-    PyErr_SetString(PyExc_TypeError, "apply(pv, ptm, plan, arith)");
+  if (nargs != 4 && nargs != 5) {
+    PyErr_SetString(PyExc_TypeError, "apply(pv, ptm, plan, arith[, out])");
     return NULL;
   }
+  PyObject* given = (nargs == 5 && args[4] != Py_None) ? args[4] : NULL;
   if (!g_apply1 || !g_apply2 || !g_empty) {
     PyErr_SetString(PyExc_RuntimeError, "apply: set_entry_points was not called");
     return NULL;
@@ -152,13 +156,19 @@ static PyObject* apply(PyObject* self, PyObject* const* args, Py_ssize_t nargs) 
   /* input and output storage */
   unsigned long long in_ptr = 0, out_ptr = 0;
   if (as_u64(PyObject_CallMethodNoArgs(pv, s_data_ptr), &in_ptr) < 0) return NULL;
-  PyObject* kw[3];
-  kw[0] = shape;
-  kw[1] = PyObject_GetAttr(pv, s_dtype);
-  kw[2] = g_dev_obj[dev];
-  PyObject* out = kw[1] ? PyObject_Vectorcall(g_empty, kw, 1, g_empty_kw) : NULL;
-  Py_XDECREF(kw[1]);
-  if (!out) return NULL;
+  PyObject* out;
+  if (given) {
+    Py_INCREF(given);
+    out = given;
+  } else {
+    PyObject* kw[3];
+    kw[0] = shape;
+    kw[1] = PyObject_GetAttr(pv, s_dtype);
+    kw[2] = g_dev_obj[dev];
+    out = kw[1] ? PyObject_Vectorcall(g_empty, kw, 1, g_empty_kw) : NULL;
+    Py_XDECREF(kw[1]);
+    if (!out) return NULL;
+  }
   for (Py_ssize_t i = 0; i < PyTuple_GET_SIZE(shape); ++i)
     if (PyLong_AsLongLong(PyTuple_GET_ITEM(shape, i)) == 0) return out; /* empty result */
   if (PyErr_Occurred() || as_u64(PyObject_CallMethodNoArgs(out, s_data_ptr), &out_ptr) < 0) {
@@ -204,7 +214,7 @@ static PyMethodDef methods[] = {
     {"set_entry_points", set_entry_points, METH_VARARGS,
      "set_entry_points(apply1_addr, apply2_addr, raw_stream, status_ptr, empty, device_of)"},
     {"apply", (PyCFunction)(void (*)(void))apply, METH_FASTCALL,
-     "apply(pv, ptm, plan, arith) -> tensor, or the status code"},
+     "apply(pv, ptm, plan, arith[, out]) -> tensor, or the status code"},
     {NULL, NULL, 0, NULL}};
 
 static struct PyModuleDef module = {PyModuleDef_HEAD_INIT, "_qsgb_pyapply", NULL, -1, methods,

@@ -487,19 +487,21 @@ def _pyapply():
     return _PYAPPLY
 
 
-def eager_apply(pv, ptm, plan, arith):
+def eager_apply(pv, ptm, plan, arith, out=None):
     """Apply the numpy PTM `ptm` (converted to C-contiguous float64 when it
     is not) to the contiguous CUDA tensor `pv` with a plan from eager_plan;
-    returns the new tensor, or None when the request needs the general
-    operator path."""
+    returns the output tensor, or None when the request needs the general
+    operator path.  `out`, when given, is a contiguous tensor of the output
+    shape, dtype and device that the caller owns and no longer reads; the
+    result is written there instead of into a new tensor."""
     fast = _PYAPPLY if _PYAPPLY is not None else _pyapply()
     if fast:
-        st = fast.apply(pv, ptm, plan, arith)
+        st = fast.apply(pv, ptm, plan, arith, out)
         if type(st) is not int:
             return st
         if st == fast.NOT_F64_CONTIGUOUS:
             st = fast.apply(pv, np.ascontiguousarray(ptm, dtype=np.float64),
-                            plan, arith)
+                            plan, arith, out)
             if type(st) is not int:
                 return st
         if st == L.ERR_UNSUPPORTED:
@@ -507,7 +509,8 @@ def eager_apply(pv, ptm, plan, arith):
         L.check(st, 'qsgb_apply_ptm')
     ptm = np.ascontiguousarray(ptm, dtype=np.float64)
     new_shape, two, sizes, flags, code = plan
-    out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
+    if out is None:
+        out = torch.empty(new_shape, dtype=pv.dtype, device=pv.device)
     if out.numel() == 0:
         return out
     lib = L.load()

@@ -235,11 +235,20 @@ class PauliVectorGB300(_Base):
             raise ValueError('`pv` should be a numpy array, a torch tensor or '
                              'None, got type `{}`'.format(type(pv)))
         self._data = data
+        # the state buffer of two applications back, written by the next
+        # apply_ptm instead of a new tensor (the reference swaps two
+        # buffers the same way, cuda.py:113-115, 221); only tensors this
+        # object allocated and never handed out take that role
+        self._owned = False
+        self._work = None
 
     # ------------------------------------------------------------ accessors
     @property
     def data(self):
-        """The device tensor (shape ``dim_pauli``)."""
+        """The device tensor (shape ``dim_pauli``).  A tensor handed out
+        here is never reused as a work buffer: later operations leave it
+        as it is."""
+        self._owned = False
         return self._data
 
     @property
@@ -286,9 +295,14 @@ class PauliVectorGB300(_Base):
                 if len(_APPLY_PLANS) > 4096:
                     _APPLY_PLANS.clear()
                 _APPLY_PLANS[key] = plan
-            out = ops.eager_apply(data, ptm, plan, self._arith)
+            work = self._work
+            if work is not None and work.shape != plan[0]:
+                self._work = work = None
+            out = ops.eager_apply(data, ptm, plan, self._arith, work)
             if out is not None:
+                self._work = data if self._owned else None
                 self._data = out
+                self._owned = True
                 return
         self._apply_general(ptm, *qubits)
 
@@ -358,7 +372,7 @@ class PauliVectorGB300(_Base):
         """FP64 device tensor of length prod(dim_hilbert)."""
         plan = _diag_plan(self.bases)
         if self.n_qubits == 0:
-            return self._data.reshape(1).to(torch.float64)
+            return self._data.reshape(1).to(torch.float64, copy=True)
         if plan is not None:
             idx_off, idx = plan
             return torch.ops.qsgb.gather(self._data, idx_off, idx, True)
@@ -499,6 +513,7 @@ class PauliVectorGB300(_Base):
         if not indices or any(i < 0 or i >= d for i in indices):
             raise ValueError('basis indices must be within [0, {})'.format(d))
         self._data = torch.ops.qsgb.take_axis(self._data, qubit, indices)
+        self._work = None
         self.bases[qubit] = self.bases[qubit].subbasis(indices)
 
     def project(self, qubit, state):

@@ -12,7 +12,8 @@ import pytest
 import torch
 
 from conftest import (ATOL_F64, ATOL_PROB, RTOL_F64, assert_close_dot,
-                      assert_close_f64, golden_bases, golden_cases)
+                      assert_close_f64, chain_rtol, golden_bases,
+                      golden_cases)
 from oracle import pauli_vector_np as O
 import quantumsim_gb300 as qg
 from quantumsim_gb300 import _lib as L
@@ -739,3 +740,54 @@ def test_small_device_ptms_fp64():
                 absref = (O.apply_ptm_transposed(np.abs(x), np.abs(ptm), q)
                           if tr else O.apply_ptm(np.abs(x), np.abs(ptm), q))
                 assert_close_dot(y, ref, absref)
+
+
+def test_state_buffers_swap_and_handed_out_tensors_stay():
+    """apply_ptm writes each result into the buffer of two applications
+    back (no new tensor per call, as the reference swaps two buffers):
+    the chain of applications still matches the oracle bit for bit against
+    fresh tensors, a tensor passed to the constructor or handed out by
+    `data` is never written, and a shape change drops the spare buffer."""
+    from quantumsim_gb300 import ops
+    rng = np.random.default_rng(91)
+    bases = [B.general(2)] * 6
+    pv = rand_pv(rng, (4,) * 6)
+    ptms = [(rand_ptm(rng, (4, 4, 4, 4), 0.5), (1, 4)),
+            (rand_ptm(rng, (4, 4)), (5,)),
+            (rand_ptm(rng, (4, 4, 4, 4), 0.5), (3, 0)),
+            (rand_ptm(rng, (4, 4)), (2,)),
+            (rand_ptm(rng, (4, 4, 4, 4), 0.5), (2, 5))]
+    user = torch.from_numpy(pv).cuda()
+    keep = user.clone()
+    s = GB(bases, user)
+    ref, absref = pv, np.abs(pv)
+    ptrs = []
+    for k, (ptm, qs) in enumerate(ptms):
+        s.apply_ptm(ptm, *qs)
+        ptrs.append(s._data.data_ptr())
+        ref = O.apply_ptm(ref, ptm, *qs)
+        absref = O.apply_ptm(absref, np.abs(ptm), *qs)
+        assert_close_dot(s.to_pv(), ref, absref,
+                         rtol=chain_rtol(ptms[:k + 1]))
+    assert torch.equal(user, keep)
+    if ops._pyapply():
+        # from the third application on, the results alternate between two
+        # buffers
+        assert ptrs[2] == ptrs[0] and ptrs[3] == ptrs[1] and \
+            ptrs[4] == ptrs[2]
+    # the same chain with a fresh tensor per call gives the same bits
+    fresh = GB(bases, pv)
+    for ptm, qs in ptms:
+        fresh.apply_ptm(ptm, *qs)
+        fresh._owned = False
+    np.testing.assert_array_equal(fresh.to_pv(), s.to_pv())
+    # a handed-out tensor keeps its values through later applications
+    out = s.data
+    snap = out.clone()
+    for ptm, qs in ptms:
+        s.apply_ptm(ptm, *qs)
+    assert torch.equal(out, snap)
+    # a rectangular PTM changes the shape; the spare buffer goes
+    s.apply_ptm(np.eye(4)[[0, 3]], 2)
+    s.apply_ptm(rand_ptm(rng, (4, 4)), 1)
+    assert s._work is None or tuple(s._work.shape) == tuple(s._data.shape)

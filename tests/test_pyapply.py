@@ -39,3 +39,17 @@ def test_plan_shape_is_checked_before_any_call(mod):
         # leave no dangling addresses for a later GPU test in this process
         import quantumsim_gb300.ops as ops
         ops._PYAPPLY = None
+
+
+def test_optional_output_argument(mod):
+    """apply takes an optional fifth argument (the output tensor, or None);
+    more arguments are refused before anything is called."""
+    mod.set_entry_points(1, 1, len, len, len, len)
+    try:
+        with pytest.raises(TypeError):
+            mod.apply(1, 2, 3, 4, None, 6)
+        with pytest.raises(TypeError):
+            mod.apply(object(), b'', (1, 2), 0, None)
+    finally:
+        import quantumsim_gb300.ops as ops
+        ops._PYAPPLY = None
