@@ -849,6 +849,43 @@ def run_profile_grad(args):
                       'loss': float(step.loss)}))
 
 
+def run_profile_fused(args):
+    """ncu workload for the specialised kernels on fused passes of the
+    14-qubit noisy circuit: a 12-qubit FP64 state (268 MB) and three fused
+    two-qubit PTMs from the assignment plan of that circuit -- the first
+    off the last qubit, at least two qubits apart, with 3.12, 4.38 and 6.25
+    non-zero terms per row -- each applied three times on its own pair.
+    Launch order: 3 per PTM."""
+    import numpy as np
+    import torch
+    from quantumsim_gb300 import build as qbuild
+    qbuild.build()
+    import quantumsim_gb300 as qg
+    from quantumsim_gb300 import bases, workloads, circuit as qc
+    ops, _ = workloads.config1_circuit(seed=1)
+    plan = qc._plan_assigned([(p, qs) for _, p, qs in ops])
+    n = 12
+    pick = {}
+    for p, qs in plan:
+        k = int(np.prod(p.shape[:len(qs)]))
+        t = qc.terms_per_row(p.reshape(k, k))
+        if len(qs) != 2 or max(qs) >= n or abs(qs[0] - qs[1]) < 2:
+            continue
+        for target in (3.12, 4.38, 6.25):
+            if abs(t - target) < 0.01 and target not in pick:
+                pick[target] = (p, qs)
+    s = qg.PauliVectorGB300([bases.general(2)] * n, force=True)
+    s._data.copy_(torch.rand_like(s._data) * 2.0 ** -12)
+    out = {}
+    for target in (3.12, 4.38, 6.25):
+        p, qs = pick[target]
+        for _ in range(3):
+            s.apply_ptm(p, *qs)
+        out[str(target)] = list(qs)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_case': 'fused', 'pairs': out}))
+
+
 def run_profile_take(args):
     """Small workload for ncu captures of the take-along-an-axis kernels
     (reduce_basis / project): 8 qutrits (9^8 float64 entries, 344 MB); 3x
@@ -1008,7 +1045,7 @@ def main():
                     help='dram bytes per launch from an ncu capture')
     ap.add_argument('--profile-case', nargs='?', const='apply',
                     choices=['apply', 'qutrits', 'tc', 'take', 'batched',
-                             'circuit', 'adjoint2', 'grad'],
+                             'circuit', 'adjoint2', 'grad', 'fused'],
                     help='run a small ncu profiling workload and exit')
     ap.add_argument('--profile-qubits', type=int, default=12)
     ap.add_argument('--profile-dtype', choices=['f64', 'f32'], default='f64',
@@ -1020,7 +1057,7 @@ def main():
         {'apply': run_profile_case, 'qutrits': run_profile_qutrits,
          'tc': run_profile_tc, 'take': run_profile_take,
          'batched': run_profile_batched, 'adjoint2': run_profile_adjoint2,
-         'circuit': run_profile_circuit,
+         'circuit': run_profile_circuit, 'fused': run_profile_fused,
          'grad': run_profile_grad}[args.profile_case](args)
         return
     if args.warmup < 3 and args.impl == 'gb300':
