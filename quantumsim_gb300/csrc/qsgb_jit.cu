@@ -699,9 +699,19 @@ int compile(const std::string& src, cudaKernel_t* out) {
 // Row modes for the specialised kernel under QSGB_ARITH_AUTO: rows in
 // ascending term count are computed in FP64 while that lowers the combined
 // estimated times per group (SM clock cycles) of HBM traffic, the FP64
-// pipe (~1.6 ops/clk sustained in these kernels), the integer pipe (64 lanes/clk: ~16 ops per split
+// pipe (kDpRate ops/clk), the integer pipe (64 lanes/clk: ~16 ops per split
 // input, ~30 per float-float row result) and instruction issue (128/clk;
 // ~12 per float-float term).
+//
+// The FP64 pipe sustains ~1.6-1.9 FMA/clk per SM (kDpRate).  Two-qubit
+// PTMs denser than 2.5 terms per row are credited with kDpRateDense: the
+// fused passes of the 14-qubit circuit (3-7 terms per row) left the FP64
+// pipe 36-42 % busy while issue sat at 72-78 %, and moving more of their
+// rows to FP64 took that circuit from 0.3053 to 0.2970 s (2.4: 0.2981 s).
+// The same credit on every PTM cost 18 % on one-qubit rotations and 17 %
+// on the 9x9 qutrit rotation.
+constexpr double kDpRate = 1.6;
+constexpr double kDpRateDense = 3.2;
 void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, size_t esz, std::vector<int>& mode) {
   const int kout = (int)cols.size();
   mode.assign(kout, kModeZero);
@@ -726,6 +736,7 @@ void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, s
   size_t n_terms = 0;
   for (const auto& c : cols) n_terms += c.size();
   const double sparse_bias = n_terms <= 3 * (size_t)kout ? 2.0 : 1.0;
+  const double dp_rate = (kin == 16 && kout == 16 && (double)n_terms > 2.5 * kout) ? kDpRateDense : kDpRate;
   auto cost = [&](const std::vector<int>& m) {
     double dp = 0, alu = 0, issue = 0;
     std::vector<char> split(kin, 0);
@@ -758,7 +769,7 @@ void plan_modes(const std::vector<std::vector<int>>& cols, int kin, int arith, s
     // (measured on GB300: 9x9 qutrit PTM 4853 -> 5539 GB/s, dense 16x16 and
     // the qubit PTMs unchanged)
     auto p6 = [](double t) { return t * t * t * t * t * t; };
-    return std::pow(p6(hbm) + p6(dp / 1.6) + p6(sparse_bias * alu / 64.0) + p6(sparse_bias * issue / 128.0),
+    return std::pow(p6(hbm) + p6(dp / dp_rate) + p6(sparse_bias * alu / 64.0) + p6(sparse_bias * issue / 128.0),
                     1.0 / 6.0);
   };
   std::vector<int> m = mode;
