@@ -58,11 +58,11 @@ import torch
 #   K = 4:  noisy rotation 2.5 terms/row 5.8; two rotations 3.75 5.0
 #   K = 9:  qutrit rotation 2.56 5.5; two rotations 2.78 5.2
 #   K = 16: CZ with rotations merged in, every fused pass of the 14-qubit
-#           noisy circuit under both planners timed alone (591 passes;
-#           harmonic means per density): 1.56 6.48 (noisy CZ), 2.19 6.03,
-#           3.12 5.18, 3.75 4.49, 4.38 4.29, 5.0 3.85, 5.5 3.75,
-#           6.25 3.68, 7.0 3.14; float-float dense rows 11.25 2.46,
-#           16 1.65 (beyond the tensor-core threshold, for 'df64')
+#           noisy circuit under both planners timed alone (615 passes;
+#           harmonic means per density): 1.56 6.49 (noisy CZ), 2.19 6.03,
+#           3.12 5.35, 3.75 4.83, 4.38 4.66, 5.0 4.05, 6.25 4.01,
+#           7.0 3.53; float-float dense rows 11.25 2.46, 16 1.65 (beyond
+#           the tensor-core threshold, for 'df64')
 #   K = 81: leakage CZ 2.14 4.7; after one rotation 5.16 2.5; between
 #           rotations 12.26 0.80 -- the 81x81 kernels lose registers and
 #           instruction cache quickly, so merging into them rarely pays.
@@ -71,9 +71,8 @@ import torch
 _RATES = {
     4: [(1.0, 7.0), (2.5, 5.8), (3.75, 5.0)],
     9: [(1.0, 6.5), (2.56, 5.5), (2.78, 5.2)],
-    16: [(1.56, 6.48), (2.19, 6.03), (3.12, 5.18), (3.75, 4.49), (4.38, 4.29),
-         (5.0, 3.85), (5.5, 3.75), (6.25, 3.68), (7.0, 3.14), (11.25, 2.46),
-         (16.0, 1.65)],
+    16: [(1.56, 6.49), (2.19, 6.03), (3.12, 5.35), (3.75, 4.83), (4.38, 4.66),
+         (5.0, 4.05), (6.25, 4.01), (7.0, 3.53), (11.25, 2.46), (16.0, 1.65)],
     81: [(1.0, 5.0), (2.14, 4.7), (5.16, 2.5), (12.26, 0.80)],
 }
 
@@ -95,10 +94,10 @@ MAX_SPECIALISED_TERMS = 1024
 # Two-qubit (16 x 16) PTMs with more than TC_MIN_TERMS non-zero terms per
 # row run on the tensor cores (the library's QSGB_TC_MIN_TERMS rule) at a
 # rate that does not depend on the density: the fused passes of the
-# 14-qubit circuit above 8 terms per row ran at 3.12 TB/s (68 passes, 3.07
+# 14-qubit circuit above 8 terms per row ran at 3.13 TB/s (75 passes, 3.07
 # to 3.22).
 TC_MIN_TERMS = 8.0
-TC_RATE = 3.12
+TC_RATE = 3.13
 
 
 def pass_cost(m):
