@@ -159,11 +159,7 @@ def _embed(unit1, pair, dims):
 
 def _aligned(unit2, pair):
     """unit2's matrix with its qudits in the order of `pair`."""
-    if unit2.qudits == tuple(pair):
-        return unit2.mat
-    da, db = unit2.dims  # unit2 is on (pair[1], pair[0])
-    m = unit2.mat.reshape(da, db, da, db).transpose(1, 0, 3, 2)
-    return m.reshape(da * db, da * db)
+    return _aligned_mat(unit2, unit2.mat, pair)
 
 
 def plan(units):
@@ -378,7 +374,7 @@ def _aligned_mat(unit2, mat, pair):
     `pair`."""
     if unit2.qudits == tuple(pair):
         return mat
-    da, db = unit2.dims
+    da, db = unit2.dims  # unit2 is on (pair[1], pair[0])
     m = mat.reshape(da, db, da, db).transpose(1, 0, 3, 2)
     return m.reshape(da * db, da * db)
 
@@ -388,11 +384,7 @@ def _plan_greedy(units):
     before when the model says the product is cheaper."""
     out = []
     last = {}  # qudit -> index in `out` of the last unit touching it
-
-    def gain(merged, parts):
-        c = pass_cost(merged)
-        return c != float('inf') and c < sum(pass_cost(p) for p in parts)
-
+    gain = _gain
     for ptm, qudits in units:
         u = _Unit(ptm, qudits)
         if u.square and len(u.qudits) == 1:

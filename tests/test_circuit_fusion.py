@@ -283,3 +283,26 @@ def test_runs_join_the_cheaper_neighbour():
     f = C._plan_assigned([(cz, (0, 1)), (r, (0,)), (cz, (0, 1))])
     assert [qs for _, qs in f] in ([(0, 1)], [(0, 1), (0, 1)])
     assert all(len(qs) == 2 for _, qs in f)
+
+
+def test_assignment_search_respects_barriers():
+    """A rectangular unit on a qudit is a barrier for the assignment search
+    too: the rotation before the projection stays on its side of it, and
+    the fused list applied by the oracle equals the units one by one."""
+    rng = np.random.default_rng(12)
+    t1, t2 = workloads.coherence_times(rng, 3)
+    r1 = workloads.noisy_1q(rng, t1[1], t2[1])
+    r0 = workloads.noisy_1q(rng, t1[0], t2[0])
+    cz = workloads.noisy_cz(rng, (0, 1), t1, t2)
+    proj = np.eye(4)[[0, 3]]
+    units = [(cz, (0, 1)), (r1, (1,)), (proj, (1,)), (r0, (0,)),
+             (workloads.noisy_cz(rng, (0, 2), t1, t2), (0, 2))]
+    fused = C._plan_assigned(units)
+    shapes = [(p.shape, qs) for p, qs in fused]
+    k = shapes.index(((2, 4), (1,)))
+    # everything on qudit 1 before the projection is applied before it
+    before = [qs for _, qs in shapes[:k]]
+    assert any(1 in qs for qs in before)
+    pv = _rand_pv(rng, (4, 4, 4))
+    assert_close_dot(_apply_all(pv, fused), _apply_all(pv, units),
+                     _abs_all(np.abs(pv), units) * 4)
