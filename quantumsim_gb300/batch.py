@@ -481,6 +481,7 @@ class BatchedSimulator:
         self.op_grad = torch.zeros(self.n_ops, 256, dtype=torch.float64,
                                    device=dev)
         self._factors = None
+        self._cchain = None
         self._fchain = None
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.max_grid = self.lib.qsgb_batch_max_grid(BLOCK)
@@ -621,9 +622,27 @@ class BatchedSimulator:
             ipool[:, :K * K] = inv.reshape(len(slots), -1)
             self.ptm[slots] = pool.to(dev).float()
             self.ptm_inv[slots] = ipool.to(dev).float()
-        self._factors = tuple(t.to(dev) for t in (c, a, b))
-        self._cchain = tuple(t.to(dev) for t in cfac)
-        self._fchain = fchain
+        self._keep('_factors', (c, a, b))
+        self._keep('_cchain', cfac)
+        self._keep('_fchain', fchain)
+
+    def _keep(self, name, tensors):
+        """Store `tensors` (or None) on the device under `name`: in place
+        when the attribute already holds tensors of the same shapes and
+        dtypes, so that a captured graph reads the new values; otherwise as
+        new tensors, dropping the graph (it would read the old ones)."""
+        old = getattr(self, name, None)
+        new = None if tensors is None else tuple(
+            t.to(self.device) for t in tensors)
+        if old is not None and new is not None and len(old) == len(new) and \
+                all(o.shape == n.shape and o.dtype == n.dtype
+                    for o, n in zip(old, new)):
+            for o, n in zip(old, new):
+                o.copy_(n)
+            return
+        if old is not None or new is not None:
+            self.graph = None
+        setattr(self, name, new)
 
     def _map_gradients(self):
         """dL/dP of every original op from the units' dL/dF (device, on the

@@ -201,3 +201,33 @@ def test_malformed_items_are_skipped_and_reported(field, value):
     torch.cuda.synchronize()
     for a, b in zip(p0, sim.results()[0]):
         assert torch.equal(a, b)
+
+
+def test_new_ptms_after_the_graph_is_captured():
+    """set_ptms after the step's graph was captured: the replayed graph
+    reads the new unit PTMs and the new gradient-mapping factors (updated
+    in place), giving bit for bit what a fresh simulator gives."""
+    ns = [5, 4, 7, 6]
+    specs, targets, ptms = _setup(ns, depth=9, every=4, seed=3)
+    other = [BT.instance_ptms(s, angle_offset=torch.from_numpy(
+        np.random.default_rng(40 + i).normal(0, 0.1, (s.depth, s.n))))
+        for i, s in enumerate(specs)]
+    sim = BT.BatchedSimulator(specs, targets, checkpoint_every=4, tile=64)
+    sim.set_ptms(ptms)
+    sim.step(use_graph=True)
+    graph = sim.graph
+    sim.set_ptms(other)
+    assert sim.graph is graph  # same structure: the graph is kept
+    sim.step(use_graph=True)
+    torch.cuda.synchronize()
+    p1, l1, g1 = sim.results()
+    fresh = BT.BatchedSimulator(specs, targets, checkpoint_every=4, tile=64)
+    fresh.set_ptms(other)
+    fresh.step(use_graph=True)
+    torch.cuda.synchronize()
+    p2, l2, g2 = fresh.results()
+    assert torch.equal(l1, l2)
+    for i in range(len(specs)):
+        assert torch.equal(p1[i], p2[i])
+        for a, b in zip(g1[i], g2[i]):
+            assert torch.equal(a, b)
