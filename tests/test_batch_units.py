@@ -322,3 +322,31 @@ def test_factor_chain_gradient_mapping_matches_autograd():
     assert sorted(eo.tolist()) == list(range(6))
     for j, dj in zip(eo.tolist(), d):
         np.testing.assert_allclose(dj, r[j].grad, rtol=1e-11, atol=1e-7)
+
+
+def test_factors_kept_in_place_for_a_captured_graph():
+    """BatchedSimulator._keep: new values of the same shapes are copied
+    into the stored tensors (a captured graph reads them) and the graph is
+    kept; other shapes, or None where tensors were, replace the tensors
+    and drop the graph."""
+    class Holder:
+        device = torch.device('cpu')
+        graph = 'captured'
+    h = Holder()
+    keep = BT.BatchedSimulator._keep
+    a = (torch.zeros(2, 4, 4), torch.arange(3))
+    keep(h, '_f', a)
+    first = h._f
+    h.graph = 'captured'
+    keep(h, '_f', (torch.ones(2, 4, 4), torch.arange(3) + 5))
+    assert h._f is first and h.graph == 'captured'
+    assert torch.equal(first[0], torch.ones(2, 4, 4))
+    assert torch.equal(first[1], torch.arange(3) + 5)
+    keep(h, '_f', (torch.ones(3, 4, 4), torch.arange(3)))
+    assert h._f is not first and h.graph is None
+    h.graph = 'captured'
+    keep(h, '_f', None)
+    assert h._f is None and h.graph is None
+    h.graph = 'captured'
+    keep(h, '_f', None)
+    assert h.graph == 'captured'
